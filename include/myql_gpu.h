@@ -1,0 +1,284 @@
+/*
+ * myql_gpu.h -- C ABI of the GB300 (sm_103a) Monte Carlo path-simulation engine.
+ *
+ * This is the drop-in boundary for MyQuantLib's Monte Carlo hot path.  The
+ * reference exposes the path as C++ templates; every entry point below lowers
+ * one of those template calls to plain C types (PODs, pointers, sizes) so any
+ * host language can bind it (ctypes, cgo, JNI, N-API).  No C++ or torch type
+ * crosses this boundary.
+ *
+ *   reference call (MyQuantLib, header-only C++20)            entry point here
+ *   ---------------------------------------------------------  ------------------------
+ *   MonteCarloPricer<Model,Stepper,Instr,Mode>::calculate       myql_mc_price
+ *       (include/myql/pricers/montecarlo/MonteCarloPricer.hpp:95)
+ *   dispatcher::price_mc<Mode,Scheme>(AnyModel, AnyMCInstrument) myql_mc_price_batch
+ *       (include/myql/dispatcher/PricingDispatch.hpp:93-126)     (many jobs, one launch)
+ *   MultiLevelMonteCarloPricer<...>::calculate                  myql_mlmc_price
+ *       (include/myql/pricers/mlmc/MultiLevelMonteCarloPricer.hpp:46)
+ *   boost::random::xoshiro256pp(seed) + jump()                  myql_rng_stream_states
+ *       (seeded at MonteCarloPricer.hpp:191)
+ *
+ * Ownership: the caller owns every buffer it passes.  A myql_ctx owns device
+ * memory (stream-state tables, chi-squared tables, scratch) and is meant to be
+ * used by one host thread at a time.  All calls are blocking unless they take
+ * a cudaStream_t (passed as void*).
+ *
+ * Errors: every entry point returns a myql_status; myql_last_error() gives a
+ * one-line message for the calling thread.  Invalid parameters (including the
+ * SchemeNV condition sigma^2 <= 4 kappa theta, which the reference enforces by
+ * throwing from VolSchemes.hpp:40-41) are rejected on the host before launch.
+ */
+#ifndef MYQL_GPU_H
+#define MYQL_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MYQL_ABI_VERSION 1
+
+typedef enum myql_status {
+  MYQL_OK = 0,
+  MYQL_ERR_INVALID_ARG = 1,  /* bad pointer, size or parameter            */
+  MYQL_ERR_NV_CONDITION = 2, /* SchemeNV with sigma^2 > 4 kappa theta     */
+  MYQL_ERR_OOM = 3,          /* device allocation failed                  */
+  MYQL_ERR_CUDA = 4,         /* any other CUDA runtime error              */
+  MYQL_ERR_LOOP_CAP = 5,     /* a bounded device loop hit its cap         */
+  MYQL_ERR_TIMEOUT = 6,      /* a device wait gave up                     */
+  MYQL_ERR_NO_DEVICE = 7,    /* no usable sm_103 device                   */
+  MYQL_ERR_UNSUPPORTED = 8,  /* combination the engine does not provide   */
+  MYQL_ERR_TOO_LARGE = 9     /* request exceeds a documented size limit   */
+} myql_status;
+
+/* --- policy choices (the reference's template parameters) ---------------- */
+typedef enum myql_scheme { /* VolSchemes.hpp */
+  MYQL_SCHEME_NONE = 0,    /* NullVolScheme (unused factor)          :19  */
+  MYQL_SCHEME_NV = 1,      /* SchemeNV (Ninomiya-Victoir)            :24  */
+  MYQL_SCHEME_EXACT = 2,   /* SchemeExact (Poisson-Gamma)            :71  */
+  MYQL_SCHEME_NCI = 3      /* SchemeNCI (chi-squared inversion)      :230 */
+} myql_scheme;
+
+typedef enum myql_jump { /* JumpPolicies.hpp */
+  MYQL_JUMP_NONE = 0,    /* NoJumps    :15 */
+  MYQL_JUMP_MERTON = 1,  /* MertonJump :32 */
+  MYQL_JUMP_KOU = 2      /* KouJump    :81 */
+} myql_jump;
+
+typedef enum myql_instrument_kind {
+  MYQL_INSTR_EUROPEAN = 0,    /* EuropeanOption  (European.hpp:10)              */
+  MYQL_INSTR_ASIAN_GEO = 1,   /* AsianOption<TrackerGeoAsian>   (Asian.hpp:7)   */
+  MYQL_INSTR_ASIAN_ARITH = 2, /* AsianOption<TrackerArithAsian> (Asian.hpp:7)   */
+  MYQL_INSTR_LOOKBACK = 3,    /* LookbackOption  (Lookback.hpp:8)               */
+  MYQL_INSTR_BARRIER = 4      /* BarrierOption   (Barrier.hpp:17)               */
+} myql_instrument_kind;
+
+typedef enum myql_payoff { /* Payoffs.hpp */
+  MYQL_PAYOFF_VANILLA = 0, /* PayoffVanilla        :14 */
+  MYQL_PAYOFF_CASH = 1,    /* PayoffCashOrNothing  :39 */
+  MYQL_PAYOFF_ASSET = 2    /* PayoffAssetOrNothing :57 */
+} myql_payoff;
+
+typedef enum myql_option_type { MYQL_CALL = 0, MYQL_PUT = 1 } myql_option_type;
+typedef enum myql_greek_mode { /* PricingTypes.hpp:8-12 */
+  MYQL_GREEKS_NONE = 0,
+  MYQL_GREEKS_ESSENTIAL = 1,
+  MYQL_GREEKS_FULL = 2
+} myql_greek_mode;
+typedef enum myql_barrier_action { MYQL_BARRIER_IN = 0, MYQL_BARRIER_OUT = 1 } myql_barrier_action;
+typedef enum myql_rebate_timing { /* Barrier.hpp:12 */
+  MYQL_REBATE_NONE = 0,
+  MYQL_REBATE_AT_HIT = 1,
+  MYQL_REBATE_AT_MATURITY = 2
+} myql_rebate_timing;
+
+/* --- model --------------------------------------------------------------- */
+typedef struct myql_heston_params { /* HestonParams, ModelParams.hpp:7-25 */
+  double kappa, theta, sigma, rho, v0;
+} myql_heston_params;
+
+typedef struct myql_model { /* ZeroFactorModel / SingleFactorModel / DoubleFactorModel, ASVJmodel.hpp:14-50 */
+  int32_t num_factors;          /* 0 (GBM), 1 (Heston/Bates), 2 (double Heston/Bates) */
+  int32_t jump;                 /* myql_jump */
+  double vol;                   /* ZeroFactorModel::vol (num_factors == 0)            */
+  myql_heston_params heston[2]; /* heston[0] = heston / heston1, heston[1] = heston2  */
+  double jump_lambda;           /* MertonParams::lambda or KouParams::lambda         */
+  double merton_mu, merton_delta;        /* MertonParams (ModelParams.hpp:35-39)      */
+  double kou_p_up, kou_eta1, kou_eta2;   /* KouParams    (ModelParams.hpp:42-47)      */
+} myql_model;
+
+/* --- instrument ---------------------------------------------------------- */
+typedef struct myql_instrument {
+  int32_t kind;           /* myql_instrument_kind                                   */
+  int32_t payoff;         /* myql_payoff                                            */
+  int32_t option_type;    /* myql_option_type                                       */
+  int32_t fixed_strike;   /* Asian/Lookback: 1 = fixed strike, 0 = floating strike  */
+  int32_t barrier_up;     /* Barrier: 1 = BarrierDirection::Up, 0 = Down            */
+  int32_t barrier_action; /* myql_barrier_action                                    */
+  int32_t rebate_timing;  /* myql_rebate_timing                                     */
+  int32_t is_strip;       /* 1 = ResultType std::vector<double>, 0 = double         */
+  double maturity;        /* T                                                      */
+  double barrier;         /* B                                                      */
+  double rebate;          /* rebate amount                                          */
+  double barrier_rate;    /* rate_ used for AtHit rebates (Barrier.hpp:36)          */
+  double payoff_eps;      /* digital smoothing bandwidth; < 0 = automatic           */
+  const double *strikes;  /* host array of n_strikes strikes                        */
+  int64_t n_strikes;      /* 1 for scalar instruments                               */
+  /* in-flight history (Asian.hpp:105-107, Lookback.hpp:184-185)                    */
+  double past_avg_log, past_avg_S, t_elapsed;
+  double hist_min_S, hist_max_S; /* 0 = not set                                     */
+} myql_instrument;
+
+/* --- Monte Carlo configuration (MonteCarloConfig, MonteCarloPricer.hpp:16-26) --- */
+typedef struct myql_mc_config {
+  uint64_t num_paths;
+  uint64_t time_steps;
+  uint64_t seed;
+  double fd_bump, vol_bump, t_bump, r_bump;
+  int32_t scheme[2];  /* myql_scheme per variance factor (the Stepper's VolScheme1/2) */
+  int32_t greek_mode; /* myql_greek_mode (the pricer's GreekMode template argument)   */
+  uint64_t n_streams; /* xoshiro streams (0 = default 131072, capped at num_paths)    */
+} myql_mc_config;
+
+typedef struct myql_mc_job {
+  myql_model model;
+  myql_instrument instrument;
+  myql_mc_config config;
+  double S0, r, q;
+} myql_mc_job;
+
+/* --- results ------------------------------------------------------------- */
+/* Quantities, in the order of MonteCarloResult<Full> (PricingTypes.hpp:68-97). */
+typedef enum myql_quantity {
+  MYQL_Q_PRICE = 0,
+  MYQL_Q_DELTA = 1,
+  MYQL_Q_GAMMA = 2,
+  MYQL_Q_VEGA0 = 3,
+  MYQL_Q_VEGA1 = 4,
+  MYQL_Q_THETA = 5,
+  MYQL_Q_RHO = 6,
+  MYQL_Q_VANNA0 = 7,
+  MYQL_Q_VANNA1 = 8,
+  MYQL_Q_CHARM = 9,
+  MYQL_Q_COUNT = 10
+} myql_quantity;
+
+/* Output layout for one job with n = instrument.n_strikes:
+ *   out[(2*quantity + 0) * n + k] = value       of strike k
+ *   out[(2*quantity + 1) * n + k] = std. error  of strike k
+ * i.e. 2 * MYQL_Q_COUNT * n doubles.  Quantities the GreekMode does not
+ * produce are written as 0. */
+#define MYQL_OUT_DOUBLES(n_strikes) ((size_t)2 * MYQL_Q_COUNT * (size_t)(n_strikes))
+
+typedef struct myql_mc_stats {
+  uint64_t paths;              /* paths priced                                   */
+  uint64_t path_steps;         /* simulated path-steps (base + bumped scenarios) */
+  uint32_t scenarios;          /* simulated scenarios per path (1, 7 or 9)       */
+  uint32_t loop_cap_hits;      /* bounded device loops that hit their cap        */
+  uint32_t table_fallbacks;    /* NCI draws outside the chi-squared table        */
+  uint32_t kernel_launches;    /* kernels launched by this call                  */
+  double device_ms;            /* device time of the call (CUDA events)          */
+} myql_mc_stats;
+
+/* --- context ------------------------------------------------------------- */
+typedef struct myql_ctx myql_ctx;
+
+myql_status myql_ctx_create(myql_ctx **ctx, int device);
+myql_status myql_ctx_destroy(myql_ctx *ctx);
+/* Copies the last error message of the calling thread (NUL-terminated). */
+size_t myql_last_error(char *buf, size_t len);
+int myql_abi_version(void);
+
+/* Debug/limit knobs.  max_loop_iters caps every bounded device loop (Poisson,
+ * Gamma rejection, Kou jump counts); 0 restores the defaults.  Used by tests
+ * to provoke MYQL_ERR_LOOP_CAP without touching the GPU's health. */
+myql_status myql_ctx_set_loop_cap(myql_ctx *ctx, uint32_t max_loop_iters);
+
+/* --- pricing entry points ------------------------------------------------ */
+
+/* One pricing request: replaces MonteCarloPricer::calculate (MonteCarloPricer.hpp:95).
+ * out: host buffer of MYQL_OUT_DOUBLES(n_strikes) doubles.  stats may be NULL. */
+myql_status myql_mc_price(myql_ctx *ctx, const myql_mc_job *job, double *out,
+                          myql_mc_stats *stats);
+
+/* Same, with device-resident output (out_dev: device pointer, same layout) and
+ * an explicit CUDA stream (cudaStream_t as void*; NULL = the legacy default
+ * stream).  Returns once the work is enqueued; host-side validation and table
+ * builds happen synchronously. */
+myql_status myql_mc_price_async(myql_ctx *ctx, const myql_mc_job *job,
+                                double *out_dev, void *stream);
+
+/* Many uneven requests in one persistent launch: replaces a loop of
+ * dispatcher::price_mc calls (PricingDispatch.hpp:93-126).
+ * outs[j] is the host output buffer of job j (MYQL_OUT_DOUBLES of its strikes). */
+myql_status myql_mc_price_batch(myql_ctx *ctx, const myql_mc_job *jobs,
+                                size_t n_jobs, double *const *outs,
+                                myql_mc_stats *stats);
+
+/* Per-path terminal records of one request (debug / parity): writes
+ * n_scenarios * n_fields * num_paths floats in [scenario][field][path] order.
+ * Fields per tracker: European {X}; Geo/Arith Asian {X, A}; Lookback
+ * {X, minX, maxX}; Barrier {X, t_hit_base, t_hit_up, t_hit_dn} with
+ * X = log(S_T / S0) and t_hit = -1 when the barrier was not hit. */
+myql_status myql_mc_paths(myql_ctx *ctx, const myql_mc_job *job, float *records,
+                          size_t records_len, uint32_t *n_scenarios,
+                          uint32_t *n_fields);
+
+/* --- MLMC (MultiLevelMonteCarloPricer.hpp:16-30, :46-241) --------------- */
+typedef struct myql_mlmc_config {
+  double epsilon;
+  uint64_t L_min, L_max, N0, base_steps;
+  double alpha, beta;
+  int32_t adaptive_rates;
+  uint64_t seed;
+  double fd_bump;
+  uint64_t n_streams; /* 0 = default */
+} myql_mlmc_config;
+
+#define MYQL_MLMC_MAX_LEVELS 24
+typedef struct myql_mlmc_result { /* MlmcResult<None,double>, PricingTypes.hpp:104-115 */
+  double price, price_std_err;
+  uint64_t total_steps;
+  uint32_t n_levels;
+  uint64_t paths_per_level[MYQL_MLMC_MAX_LEVELS];
+  double mean_diffs[MYQL_MLMC_MAX_LEVELS];
+  double var_diffs[MYQL_MLMC_MAX_LEVELS];
+  double alpha_estimated, beta_estimated;
+  double device_ms;
+} myql_mlmc_result;
+
+/* job->config supplies scheme[] (the coupled stepper's VolScheme1/2); its
+ * num_paths/time_steps/seed are ignored in favour of mlmc. */
+myql_status myql_mlmc_price(myql_ctx *ctx, const myql_mc_job *job,
+                            const myql_mlmc_config *mlmc,
+                            myql_mlmc_result *result);
+
+/* --- RNG streams (bit-exact against boost::random::xoshiro256pp) -------- */
+/* Writes the xoshiro256++ state of streams first..first+n-1 for `seed`:
+ * stream k = state seeded by splitmix64(seed), advanced by k * 2^128 steps
+ * (k applications of the standard xoshiro256 jump()).  out: host buffer of
+ * 4*n uint64 in [stream][word] order.  Computed on the device. */
+myql_status myql_rng_stream_states(myql_ctx *ctx, uint64_t seed, uint64_t first,
+                                   uint64_t n, uint64_t *out);
+/* Draws `count` consecutive 64-bit outputs of each listed stream on the
+ * device: out[stream][i], host buffer of n*count uint64. */
+myql_status myql_rng_draws(myql_ctx *ctx, uint64_t seed, uint64_t first,
+                           uint64_t n, uint64_t count, uint64_t *out);
+
+/* --- numerics probes (device functions evaluated on host-provided inputs) -- */
+/* FP64 chi-squared quantiles computed on the device, as used to build the
+ * SchemeNCI tables (VolSchemes.hpp:240-313). */
+myql_status myql_chi2_quantile(myql_ctx *ctx, const double *dof, const double *p,
+                               double *out, size_t n);
+/* FP32 device samplers on given 64-bit draws: kind 0 = inverse normal of the
+ * uniform of x, kind 1 = inverse Poisson CDF with mean lambda[i] of the uniform
+ * of x.  out: n floats. */
+myql_status myql_probe_sampler(myql_ctx *ctx, int kind, const uint64_t *x,
+                               const double *lambda, float *out, size_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MYQL_GPU_H */

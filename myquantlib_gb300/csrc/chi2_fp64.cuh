@@ -1,0 +1,121 @@
+// chi2_fp64.cuh -- FP64 chi-squared quantiles on the device.
+//
+// Used once per degrees-of-freedom offset d to build the SchemeNCI tables
+// (the reference builds them with boost::math::quantile, VolSchemes.hpp:266-311).
+// Method: regularized incomplete gamma by its power series (x < a + 1) or by
+// the Legendre continued fraction evaluated with the modified Lentz algorithm
+// (x >= a + 1); the quantile is a safeguarded Newton iteration on
+// log P(a, x) (lower tail) or log Q(a, x) (upper tail) in u = log x, started
+// from the Wilson-Hilferty cube or, for small P and shape below 1, from the
+// leading power term x^a / Gamma(a + 1).  chi2_nu^-1(p) = 2 * x with a = nu / 2.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace myql {
+namespace dev {
+
+struct GammaEval {
+  double logP, logQ;  // log of the regularized lower / upper incomplete gamma
+  double xpdf_P;      // x * pdf(x) / P
+  double xpdf_Q;      // x * pdf(x) / Q
+};
+
+__device__ inline GammaEval gamma_eval(double a, double x, double lga) {
+  GammaEval g;
+  const double lpre = -x + a * log(x) - lga;  // log(x^a e^-x / Gamma(a))
+  if (x < a + 1.0) {
+    // P = x^a e^-x / Gamma(a+1) * sum_{n>=0} x^n / ((a+1)...(a+n))
+    double term = 1.0, sum = 1.0, ap = a;
+    for (int n = 0; n < 2000; ++n) {
+      ap += 1.0;
+      term *= x / ap;
+      sum += term;
+      if (term < sum * 1e-17) break;
+    }
+    g.logP = lpre - log(a) + log(sum);
+    const double P = exp(g.logP);
+    g.logQ = log1p(-P);
+    g.xpdf_P = a / sum;
+    g.xpdf_Q = exp(lpre - g.logQ);
+  } else {
+    // Q = x^a e^-x / Gamma(a) * h, h the continued fraction
+    const double tiny = 1e-300;
+    double b = x + 1.0 - a, c = 1.0 / tiny, d = 1.0 / b, h = d;
+    for (int i = 1; i < 2000; ++i) {
+      const double an = -i * (i - a);
+      b += 2.0;
+      d = an * d + b;
+      if (fabs(d) < tiny) d = tiny;
+      c = b + an / c;
+      if (fabs(c) < tiny) c = tiny;
+      d = 1.0 / d;
+      const double del = d * c;
+      h *= del;
+      if (fabs(del - 1.0) < 1e-16) break;
+    }
+    g.logQ = lpre + log(h);
+    const double Q = exp(g.logQ);
+    g.logP = log1p(-Q);
+    g.xpdf_Q = 1.0 / h;
+    g.xpdf_P = exp(lpre - g.logP);
+  }
+  return g;
+}
+
+// Quantile of chi-squared with nu degrees of freedom at lower-tail probability p
+// (upper = false) or upper-tail probability p (upper = true).
+__device__ inline double chi2_quantile(double nu, double p, bool upper) {
+  if (p <= 0.0) return upper ? INFINITY : 0.0;
+  if (p >= 1.0) return upper ? 0.0 : INFINITY;
+  const double a = 0.5 * nu;
+  const double lga = lgamma(a);
+  const double lp = log(p);
+  // initial guess
+  const double z = upper ? -normcdfinv(p) : normcdfinv(p);
+  const double h = 1.0 / (9.0 * a);
+  const double cwh = 1.0 - h + z * sqrt(h);
+  double u;
+  const double u_small = (lp + lgamma(a + 1.0)) / a;  // log of (p Gamma(a+1))^(1/a)
+  if (cwh > 0.0) {
+    u = log(a) + 3.0 * log(cwh);
+    if (!upper && a < 1.0 && u_small < u) u = u_small;
+  } else {
+    u = upper ? log(a + 1.0) : u_small;
+  }
+  double lo = -INFINITY, hi = INFINITY;
+  for (int it = 0; it < 200; ++it) {
+    const double x = exp(u);
+    if (x <= 0.0) { u = -700.0; break; }
+    const GammaEval g = gamma_eval(a, x, lga);
+    double G, dG;  // G increasing in u
+    if (!upper) {
+      G = g.logP - lp;
+      dG = g.xpdf_P;
+    } else {
+      G = lp - g.logQ;
+      dG = g.xpdf_Q;
+    }
+    if (G < 0.0) lo = u; else hi = u;
+    double un = u - G / dG;
+    if (!(un > lo && un < hi)) {
+      if (isinf(lo)) un = u - 2.0;
+      else if (isinf(hi)) un = u + 2.0;
+      else un = 0.5 * (lo + hi);
+    }
+    if (fabs(un - u) < 1e-14 * fmax(1.0, fabs(u))) {
+      u = un;
+      break;
+    }
+    u = un;
+  }
+  return 2.0 * exp(u);
+}
+
+// chi-squared density (for the exact tail slopes)
+__device__ inline double chi2_logpdf(double nu, double y) {
+  const double a = 0.5 * nu, x = 0.5 * y;
+  return (a - 1.0) * log(x) - x - lgamma(a) - log(2.0);
+}
+
+}  // namespace dev
+}  // namespace myql

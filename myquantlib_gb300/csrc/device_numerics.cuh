@@ -1,0 +1,354 @@
+// device_numerics.cuh -- FP32 samplers of the path kernels (sm_103a).
+//
+// Random numbers: xoshiro256++ (Blackman & Vigna), one 64-bit draw per uniform,
+// exactly as boost::random::uniform_real_distribution<double>(0,1) consumes
+// them (draws whose double rounds to 1.0 are rejected and redrawn).  Uniforms
+// are formed in "q-space": the 64-bit integer is converted so that FP32 keeps
+// full relative precision in BOTH tails (min(p, 1-p) is taken on the integer,
+// before any rounding), which is what the inverse-normal and inverse-Poisson
+// tails need.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace myql {
+namespace dev {
+
+struct Xo {
+  unsigned long long a, b, c, d;
+};
+
+__device__ __forceinline__ unsigned long long rotl64(unsigned long long x, int k) {
+  return (x << k) | (x >> (64 - k));
+}
+
+// xoshiro256++ next(): output rotl(s0 + s3, 23) + s0, then the linear state update.
+__device__ __forceinline__ unsigned long long xo_next(Xo &s) {
+  const unsigned long long out = rotl64(s.a + s.d, 23) + s.a;
+  const unsigned long long t = s.b << 17;
+  s.c ^= s.a;
+  s.d ^= s.b;
+  s.b ^= s.c;
+  s.a ^= s.d;
+  s.c ^= t;
+  s.d = rotl64(s.d, 45);
+  return out;
+}
+
+// One uniform_real_distribution<double>(0,1) draw: the double of x / 2^64 is
+// rejected when it rounds to 1.0, i.e. for x >= 2^64 - 2^10.
+__device__ __forceinline__ unsigned long long draw(Xo &s) {
+  unsigned long long x = xo_next(s);
+  while (x >= 0xFFFFFFFFFFFFFC00ull) x = xo_next(s);
+  return x;
+}
+
+// x * 2^-64 rounded down to 24 significant bits (relative precision at any scale).
+__device__ __forceinline__ float u01_bits(unsigned long long x) {
+  x |= 1ull;
+  const int n = __clzll(x);
+  const unsigned long long m = x << n;
+  const unsigned int bits =
+      ((unsigned int)(126 - n) << 23) | ((unsigned int)(m >> 40) & 0x7FFFFFu);
+  return __uint_as_float(bits);
+}
+
+// 1 - x * 2^-64, with the same relative precision near 0.
+__device__ __forceinline__ float u01c_bits(unsigned long long x) { return u01_bits(~x); }
+
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float r;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// Inverse normal CDF of p = x * 2^-64 with Acklam's rational approximation
+// (P. J. Acklam, 2003), the algorithm of Numerics::normcdfinv_as241
+// (math/Numerics.hpp:12-47): one rational in (p - 1/2) on |p - 1/2| < 0.47575,
+// one rational in sqrt(-2 log q) on the tails.  The coefficients are those of
+// the published approximation.
+__device__ __forceinline__ float inv_normal_bits(unsigned long long x) {
+  const long long d = (long long)(x ^ 0x8000000000000000ull);  // (p - 1/2) * 2^64
+  const float q = (float)(int)(d >> 32) * 2.3283064365386963e-10f;
+  if (fabsf(q) < 0.47575f) {
+    const float r = q * q;
+    const float num =
+        fmaf(fmaf(fmaf(fmaf(fmaf(-3.969683028665376e+01f, r, 2.209460984245205e+02f), r,
+                            -2.759285104469687e+02f), r, 1.383577518672690e+02f), r,
+                  -3.066479806614716e+01f), r, 2.506628277459239e+00f);
+    const float den =
+        fmaf(fmaf(fmaf(fmaf(fmaf(-5.447609879822406e+01f, r, 1.615858368580409e+02f), r,
+                            -1.556989798598866e+02f), r, 6.680131188771972e+01f), r,
+                  -1.328068155288572e+01f), r, 1.0f);
+    return __fdividef(num * q, den);
+  }
+  const unsigned long long ad =
+      d < 0 ? (unsigned long long)(-(d + 1)) + 1ull : (unsigned long long)d;
+  const float tq = u01_bits(0x8000000000000000ull - ad);  // min(p, 1-p)
+  const float r = sqrt_approx(-2.0f * __logf(tq));
+  const float num =
+      fmaf(fmaf(fmaf(fmaf(fmaf(-7.784894002430293e-03f, r, -3.223964580411365e-01f), r,
+                          -2.400758277161838e+00f), r, -2.549732539343734e+00f), r,
+                4.374664141464968e+00f), r, 2.938163982698783e+00f);
+  const float den =
+      fmaf(fmaf(fmaf(fmaf(7.784695709041462e-03f, r, 3.224671290700398e-01f), r,
+                     2.445134137142996e+00f), r, 3.754408661907416e+00f), r, 1.0f);
+  const float z = __fdividef(num, den);
+  return d < 0 ? z : -z;
+}
+
+// (1 + e) log(1 + e) - e, accurate for small |e| (series) and large (direct).
+__device__ __forceinline__ float xlogx_m1(float e) {
+  if (fabsf(e) < 0.25f) {
+    // sum_{n>=2} (-1)^n e^n / (n (n-1))
+    float s = 1.0f / 110.0f;
+    s = fmaf(s, -e, 1.0f / 90.0f);
+    s = fmaf(s, -e, 1.0f / 72.0f);
+    s = fmaf(s, -e, 1.0f / 56.0f);
+    s = fmaf(s, -e, 1.0f / 42.0f);
+    s = fmaf(s, -e, 1.0f / 30.0f);
+    s = fmaf(s, -e, 1.0f / 20.0f);
+    s = fmaf(s, -e, 1.0f / 12.0f);
+    s = fmaf(s, -e, 1.0f / 6.0f);
+    s = fmaf(s, -e, 0.5f);
+    return s * e * e;
+  }
+  return (1.0f + e) * log1pf(e) - e;
+}
+
+// log(1 + w) - w, accurate for small |w|.
+__device__ __forceinline__ float log1p_m(float w) {
+  if (fabsf(w) < 0.25f) {
+    // -w^2/2 + w^3/3 - w^4/4 + ...
+    float s = -1.0f / 12.0f;
+    s = fmaf(s, w, 1.0f / 11.0f);
+    s = fmaf(s, w, -1.0f / 10.0f);
+    s = fmaf(s, w, 1.0f / 9.0f);
+    s = fmaf(s, w, -1.0f / 8.0f);
+    s = fmaf(s, w, 1.0f / 7.0f);
+    s = fmaf(s, w, -1.0f / 6.0f);
+    s = fmaf(s, w, 1.0f / 5.0f);
+    s = fmaf(s, w, -1.0f / 4.0f);
+    s = fmaf(s, w, 1.0f / 3.0f);
+    s = fmaf(s, w, -0.5f);
+    return s * w * w;
+  }
+  return log1pf(w) - w;
+}
+
+// Inverse Poisson CDF: smallest N with F_lambda(N) >= U, U = x * 2^-64.
+// Follows the structure of Giles' algorithm (ACM TOMS 955), as used by
+// Numerics::poissinvcdf (math/Numerics.hpp:49-272): for lambda > 4 a
+// normal-asymptotic estimate (with a Newton solve in the tails) whose floor is
+// checked with Temme's uniform expansion when it lies within 2*Delta of an
+// integer; below 10 an explicit summation.  FP32 throughout; the summation
+// runs in plain (unscaled) form, which is exact up to FP32 rounding of the CDF.
+static __device__ __noinline__ int poisson_inv(float lam, unsigned long long x, unsigned int cap,
+                                        unsigned int &caphits) {
+  const float U = u01_bits(x);
+  float X = 0.0f;
+  if (lam > 4.0f) {
+    const float W = inv_normal_bits(x);
+    const float rl = sqrt_approx(lam);
+    const float li = 1.0f / lam;
+    float S, Del;
+    if (fabsf(W) < 3.0f) {
+      S = rl * W + (1.0f / 3.0f + (1.0f / 6.0f) * W * W) * (1.0f - W / (12.0f * rl));
+      Del = fmaf(fmaf(1.0f / 160.0f, W * W, 1.0f / 80.0f), W * W, 1.0f / 40.0f) * li;
+      S = lam + (S + Del);
+    } else {
+      // Newton on sqrt(2((1-R) + R log R)) = W / sqrt(lambda); quadratic
+      // convergence reaches FP32 resolution in a few steps, so a fixed small
+      // budget replaces the FP64 tolerance loop.
+      const float s = W / rl;
+      float R = fmaxf(1.0f + s, 0.1f), R2;
+      for (int it = 0; it < 12; ++it) {
+        R2 = R;
+        const float T = log1pf(R - 1.0f);
+        float S2 = sqrtf(2.0f * xlogx_m1(R - 1.0f));
+        if (R < 1.0f) S2 = -S2;
+        R = R2 - (S2 - s) * S2 / T;
+        if (R < 0.1f * R2) R = 0.1f * R2;
+        if (fabsf(R - R2) <= 2e-7f * R) break;
+      }
+      const float T = log1pf(R - 1.0f);
+      S = lam * R + __logf(sqrtf(2.0f * R * xlogx_m1(R - 1.0f)) / fabsf(R - 1.0f)) / T;
+      S = S - 0.0218f / (S + 0.065f * lam);
+      Del = 0.01f / S;
+      S = S + Del;
+    }
+    X = floorf(S);
+    if (S > 10.0f && S < X + 2.0f * Del) {
+      if (X > 0.5f * lam && X < 2.0f * lam) {
+        // Temme's uniform asymptotic expansion of the CDF at X - 1 (TOMS 955).
+        const float Xi = 1.0f / X;
+        float Eta = sqrtf(2.0f * xlogx_m1(X * li - 1.0f) / (X * li));
+        if (X > lam) Eta = -Eta;
+        float B1 = 8.0995211567045583e-16f, B0;
+        float T = B1;
+        B0 = -1.9752288294349411e-15f;  T = B0 + T * Eta;
+        B1 = -5.1391118342426808e-16f + 25.0f * B1 * Xi;  T = B1 + T * Eta;
+        B0 = 2.8534893807047458e-14f + 24.0f * B0 * Xi;   T = B0 + T * Eta;
+        B1 = -1.3923887224181616e-13f + 23.0f * B1 * Xi;  T = B1 + T * Eta;
+        B0 = 3.3717632624009806e-13f + 22.0f * B0 * Xi;   T = B0 + T * Eta;
+        B1 = 1.1004392031956284e-13f + 21.0f * B1 * Xi;   T = B1 + T * Eta;
+        B0 = -5.0276692801141763e-12f + 20.0f * B0 * Xi;  T = B0 + T * Eta;
+        B1 = 2.4361948020667402e-11f + 19.0f * B1 * Xi;   T = B1 + T * Eta;
+        B0 = -5.8307721325504166e-11f + 18.0f * B0 * Xi;  T = B0 + T * Eta;
+        B1 = -2.5514193994946487e-11f + 17.0f * B1 * Xi;  T = B1 + T * Eta;
+        B0 = 9.1476995822367933e-10f + 16.0f * B0 * Xi;   T = B0 + T * Eta;
+        B1 = -4.3820360184533521e-09f + 15.0f * B1 * Xi;  T = B1 + T * Eta;
+        B0 = 1.0261809784240299e-08f + 14.0f * B0 * Xi;   T = B0 + T * Eta;
+        B1 = 6.7078535434015332e-09f + 13.0f * B1 * Xi;   T = B1 + T * Eta;
+        B0 = -1.7665952736826086e-07f + 12.0f * B0 * Xi;  T = B0 + T * Eta;
+        B1 = 8.2967113409530833e-07f + 11.0f * B1 * Xi;   T = B1 + T * Eta;
+        B0 = -1.8540622107151585e-06f + 10.0f * B0 * Xi;  T = B0 + T * Eta;
+        B1 = -2.1854485106799979e-06f + 9.0f * B1 * Xi;   T = B1 + T * Eta;
+        B0 = 3.9192631785224383e-05f + 8.0f * B0 * Xi;    T = B0 + T * Eta;
+        B1 = -0.00017875514403292177f + 7.0f * B1 * Xi;   T = B1 + T * Eta;
+        B0 = 0.00035273368606701921f + 6.0f * B0 * Xi;    T = B0 + T * Eta;
+        B1 = 0.0011574074074074078f + 5.0f * B1 * Xi;     T = B1 + T * Eta;
+        B0 = -0.014814814814814815f + 4.0f * B0 * Xi;     T = B0 + T * Eta;
+        B1 = 0.083333333333333329f + 3.0f * B1 * Xi;      T = B1 + T * Eta;
+        B0 = -0.33333333333333331f + 2.0f * B0 * Xi;      T = B0 + T * Eta;
+        T = T / (1.0f + B1 * Xi);
+        T = T * __expf(-0.5f * X * Eta * Eta) * rsqrtf(2.0f * 3.14159265358979f * X);
+        if (X < lam) {
+          T += 0.5f * erfcf(Eta * sqrtf(0.5f * X));
+          if (T > U) X -= 1.0f;
+        } else {
+          T -= 0.5f * erfcf(-Eta * sqrtf(0.5f * X));
+          if (T > -u01c_bits(x)) X -= 1.0f;
+        }
+      } else {
+        // Stirling-corrected ratio, then a 50-term summation (tails only).
+        float Xi = 1.0f / X;
+        float T = -(691.0f / 360360.0f);
+        T = (1.0f / 1188.0f) + T * Xi * Xi;
+        T = -(1.0f / 1680.0f) + T * Xi * Xi;
+        T = (1.0f / 1260.0f) + T * Xi * Xi;
+        T = -(1.0f / 360.0f) + T * Xi * Xi;
+        T = (1.0f / 12.0f) + T * Xi * Xi;
+        T = T * Xi;
+        T = (X - lam) - X * __logf(X * li) - T;
+        if (X < lam) {
+          const float E = __expf(-0.5f * T);
+          float Ssum = 1.0f - E * (U * E) * sqrtf(2.0f * 3.14159265358979f * Xi) * lam;
+          float Tt = 1.0f, Xr = X;
+          for (int i = 1; i < 50; ++i) {
+            Xr -= 1.0f;
+            Tt *= Xr * li;
+            Ssum += Tt;
+          }
+          if (Ssum > 0.0f) X -= 1.0f;
+        } else {
+          const float E = __expf(-0.5f * T);
+          float Ssum = 1.0f - E * (u01c_bits(x) * E) * sqrtf(2.0f * 3.14159265358979f * X);
+          float Xr = X;
+          for (int i = 0; i < 50; ++i) {
+            Xr += 1.0f;
+            Ssum = Ssum * Xr * li + 1.0f;
+          }
+          if (Ssum < 0.0f) X -= 1.0f;
+        }
+      }
+    }
+  }
+  if (X < 10.0f) {
+    // explicit summation of the CDF from 0
+    float p = __expf(-lam);
+    float F = p;
+    unsigned int n = 0;
+    while (U > F) {
+      if (++n > cap) {
+        ++caphits;
+        break;
+      }
+      p *= lam / (float)n;
+      F += p;
+      if (p < F * 5.0e-8f) break;  // F has stopped moving: deep upper tail
+    }
+    X = (float)n;
+  }
+  return (int)X;
+}
+
+// Poisson draw by sequential inversion, as boost::random::poisson_distribution
+// does for means below 10: one uniform_01 draw, subtract pmf terms.
+__device__ __forceinline__ int poisson_small(float mean, float exp_neg_mean, Xo &rng,
+                                             unsigned int cap, unsigned int &caphits) {
+  float u = u01_bits(draw(rng));
+  float p = exp_neg_mean;
+  int k = 0;
+  while (u > p) {
+    if ((unsigned int)k >= cap) {
+      ++caphits;
+      break;
+    }
+    u -= p;
+    ++k;
+    p = mean * p / (float)k;
+  }
+  return k;
+}
+
+// Exponential(rate) draw: -log(1 - U) / rate from one uniform.
+__device__ __forceinline__ float exp_draw(Xo &rng, float inv_rate) {
+  return -__logf(u01c_bits(draw(rng))) * inv_rate;
+}
+
+// Gamma(alpha_base + N, 1) draw of SchemeExact::generate_gamma
+// (VolSchemes.hpp:128-203): Marsaglia-Tsang for alpha > 1, the reference's
+// exponential-rejection sampler for alpha <= 1.  Loops are capped.
+static __device__ __noinline__ float gamma_draw(float alpha_base, int N, Xo &rng, float sm_p,
+                                         float sm_inv_p, float sm_1mp, float sm_1ma,
+                                         float sm_inv_a, unsigned int cap,
+                                         unsigned int &caphits) {
+  const float alpha = alpha_base + (float)N;
+  if (alpha > 1.0f) {
+    const float d = alpha - (1.0f / 3.0f);
+    const float c = rsqrtf(9.0f * d);
+    for (unsigned int it = 0; it < cap; ++it) {
+      float Z, v;
+      unsigned int jt = 0;
+      do {
+        Z = inv_normal_bits(draw(rng));
+        v = 1.0f + c * Z;
+      } while (v <= 0.0f && ++jt < cap);
+      const float cz = c * Z;
+      const float w = cz * (3.0f + cz * (3.0f + cz));  // (1 + cZ)^3 - 1
+      v = 1.0f + w;
+      const float U = u01_bits(draw(rng));
+      const float Z2 = Z * Z;
+      if (U < 1.0f - 0.0331f * Z2 * Z2) return d * v;
+      if (__logf(U) < 0.5f * Z2 + d * log1p_m(w)) return d * v;
+    }
+    ++caphits;
+    return d;
+  }
+  for (unsigned int it = 0; it < cap; ++it) {
+    const float u = u01_bits(draw(rng));
+    const float y = -__logf(u01c_bits(draw(rng)));
+    if (u < sm_p) {
+      const float xg = __expf(-y * sm_inv_a);
+      if (u * sm_inv_p < 1.0f - xg) return xg;
+      if (u < sm_p * __expf(-xg)) return xg;
+    } else {
+      const float xg = 1.0f + y;
+      const float inv_h = 1.0f / (1.0f + sm_1ma * y);
+      if (u < sm_p + sm_1mp * inv_h) return xg;
+      if (u < sm_p + sm_1mp * __powf(xg, -sm_1ma)) return xg;
+    }
+  }
+  ++caphits;
+  return alpha;
+}
+
+}  // namespace dev
+}  // namespace myql

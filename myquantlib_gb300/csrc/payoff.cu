@@ -1,0 +1,309 @@
+// payoff.cu -- phase 2 and 3 of a pricing request.
+//
+// payoff_reduce_kernel turns the per-path terminal records into the per-path
+// estimators of MonteCarloPricer.hpp:261-276 (price, pathwise FD delta and
+// gamma) and :302-410 (CRN vega, vanna, theta, charm, rho), for every strike
+// of the strip, and reduces sum and sum of squares over a tile of paths:
+// FP32 over a batch of <= 32 paths, FP64 across batches and tiles.
+//   * scalar instruments: each thread evaluates its own paths;
+//   * strips: a warp stages 32 paths' records in shared memory and each lane
+//     owns one strike of a 32-strike chunk (gridDim.y chunks), so the payoff
+//     work is one evaluation per (path, strike) with no per-strike reduction.
+// finalize_kernel sums the tile partials in a fixed order (deterministic) and
+// applies compute_stats (MonteCarloPricer.hpp:448-457).
+#include "engine_types.h"
+
+namespace myql {
+namespace dev {
+
+// Payoffs.hpp:14-69 applied to diff = (+/-)(spot - strike); spot for asset-or-nothing.
+__device__ __forceinline__ float payoff_value(const PayoffParams &P, float diff, float spot,
+                                              bool smooth) {
+  if (P.payoff == 0) return fmaxf(diff, 0.0f);
+  float h;
+  if (smooth)
+    h = 0.5f * erfcf(-diff * P.smooth_eps);  // smooth_eps holds 1 / (eps * sqrt(2))
+  else
+    h = diff > 0.0f ? 1.0f : 0.0f;
+  return P.payoff == 1 ? h : spot * h;
+}
+
+// Value of one (scenario, spot bump s in {-1, 0, +1}) for strike K.
+// View: S = terminal spot, Y = average / extreme, hit[3] = hit times (base, up, dn).
+struct PathView {
+  float S, Y;
+  float hit[3];
+};
+
+__device__ __forceinline__ float scenario_value(const PayoffParams &P, const PathView &v, float K,
+                                                int s) {
+  const bool call = P.option_type == 0;
+  float x, d0, slope;
+  switch (P.kind) {
+    case 1:  // Asian (Asian.hpp:114-121)
+    case 2:
+      if (P.fixed_strike) {
+        x = v.Y;
+        d0 = v.Y - K;
+        slope = v.Y;
+      } else {
+        x = v.S;
+        d0 = v.S - v.Y;
+        slope = d0;
+      }
+      break;
+    case 3:  // Lookback (Lookback.hpp:191-202, 237-242); Y carries the extreme in use
+      if (P.fixed_strike) {
+        x = v.Y;
+        d0 = v.Y - K;
+        slope = v.Y;
+      } else {
+        x = v.S;
+        d0 = v.S - v.Y;
+        slope = d0;
+      }
+      break;
+    default:  // European, Barrier
+      x = v.S;
+      d0 = v.S - K;
+      slope = v.S;
+      break;
+  }
+  const float fs = (float)s;
+  const float d = fmaf(fs * P.eps_rel, slope, d0);
+  const float spot = fmaf(fs * P.eps_rel, x, x);
+  const float diff = call ? d : -d;
+  if (P.kind != 4) return payoff_value(P, diff, spot, P.smooth != 0);
+  // Barrier (Barrier.hpp:29-45): the wrapped payoff is always the sharp one.
+  const float th = s == 0 ? v.hit[0] : (s > 0 ? v.hit[1] : v.hit[2]);
+  const bool is_hit = th >= 0.0f;
+  float rebate = 0.0f;
+  if (P.rebate_timing != 0) {
+    rebate = P.rebate;
+    if (P.rebate_timing == 1 && is_hit) rebate = P.rebate * __expf(P.barrier_rate * (P.T_instr - th));
+  }
+  const float pay = payoff_value(P, diff, spot, false);
+  if (P.barrier_action == 0) return is_hit ? pay : rebate;
+  return is_hit ? rebate : pay;
+}
+
+template <class FLD>
+__device__ __forceinline__ PathView make_view(const PayoffParams &P, FLD fld, int sc) {
+  PathView v;
+  const float X = fld(sc, 0);
+  v.S = P.S0 * __expf(X);
+  v.Y = 0.0f;
+  v.hit[0] = v.hit[1] = v.hit[2] = -1.0f;
+  switch (P.tracker) {
+    case TRK_GEO_ASIAN: v.Y = P.S0 * __expf(fmaf(P.avg_c1[sc], fld(sc, 1), P.avg_c0[sc])); break;
+    case TRK_ARITH_ASIAN: v.Y = P.S0 * fmaf(P.avg_c1[sc], fld(sc, 1), P.avg_c0[sc]); break;
+    case TRK_LOOKBACK: {
+      // fixed strike: call uses the max, put the min; floating: call min, put max
+      const bool use_max = (P.option_type == 0) == (P.fixed_strike != 0);
+      v.Y = P.S0 * __expf(use_max ? fld(sc, 2) : fld(sc, 1));
+      break;
+    }
+    case TRK_BARRIER_UP:
+    case TRK_BARRIER_DOWN:
+      v.hit[0] = fld(sc, 1);
+      v.hit[1] = fld(sc, 2);
+      v.hit[2] = fld(sc, 3);
+      break;
+    default: break;
+  }
+  return v;
+}
+
+// Per-path estimators of every quantity for strike K.
+template <class FLD>
+__device__ __forceinline__ void path_quantities(const PayoffParams &P, FLD fld, float K,
+                                                float (&q)[kQ]) {
+  const PathView b = make_view(P, fld, 0);
+  const float p = scenario_value(P, b, K, 0);
+  q[0] = p;
+  if (P.mode == 0) return;
+  const float up = scenario_value(P, b, K, 1);
+  const float dn = scenario_value(P, b, K, -1);
+  q[1] = (up - dn) * P.inv_2h;
+  q[2] = ((up - p) + (dn - p)) * P.inv_h2;
+  if (P.mode == 1) return;
+  const int nv = P.n_factors >= 2 ? 2 : 1;
+  for (int fct = 0; fct < nv; ++fct) {
+    const int su = fct == 0 ? SC_VUP0 : SC_VUP1;
+    const int sd = fct == 0 ? SC_VDN0 : SC_VDN1;
+    const PathView vu = make_view(P, fld, su);
+    const PathView vd = make_view(P, fld, sd);
+    const float pu = scenario_value(P, vu, K, 0);
+    const float pd = scenario_value(P, vd, K, 0);
+    const float du = scenario_value(P, vu, K, 1) - scenario_value(P, vu, K, -1);
+    const float dd = scenario_value(P, vd, K, 1) - scenario_value(P, vd, K, -1);
+    q[fct == 0 ? 3 : 4] = (pu - pd) * P.vega_c[fct];
+    q[fct == 0 ? 7 : 8] = (du - dd) * P.vanna_c[fct];
+  }
+  {
+    const PathView tu = make_view(P, fld, SC_TUP);
+    const PathView td = make_view(P, fld, SC_TDN);
+    const float pu = scenario_value(P, tu, K, 0);
+    const float pd = scenario_value(P, td, K, 0);
+    q[5] = ((pu - pd) + (pu * P.dfm1_tup - pd * P.dfm1_tdn)) * P.theta_c;
+    const float du = scenario_value(P, tu, K, 1) - scenario_value(P, tu, K, -1);
+    const float dd = scenario_value(P, td, K, 1) - scenario_value(P, td, K, -1);
+    q[9] = ((du - dd) + (du * P.dfm1_tup - dd * P.dfm1_tdn)) * P.charm_c;
+  }
+  {
+    const PathView ru = make_view(P, fld, SC_RUP);
+    const PathView rd = make_view(P, fld, SC_RDN);
+    const float pu = scenario_value(P, ru, K, 0);
+    const float pd = scenario_value(P, rd, K, 0);
+    q[6] = ((pu - pd) + (pu * P.dfm1_rup - pd * P.dfm1_rdn)) * P.rho_c;
+  }
+}
+
+__device__ __forceinline__ int active_q(int mode) { return mode == 0 ? 1 : (mode == 1 ? 3 : kQ); }
+
+__global__ void __launch_bounds__(kPayoffBlock) payoff_reduce_kernel(const __grid_constant__ PayoffParams P) {
+  __shared__ float stage[kPayoffBlock / 32][kMaxScenarios * kMaxFields][33];
+  __shared__ double red[kPayoffBlock / 32][2 * kQ][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned long long tile = blockIdx.x;
+  const unsigned long long t0 = tile * (unsigned long long)P.tile_paths;
+  const unsigned long long t1 = min(t0 + (unsigned long long)P.tile_paths, P.n_paths);
+  const int nq = active_q(P.mode);
+  const int F = P.n_fields;
+  const size_t stride = P.rec_stride;
+
+  if (P.n_strikes == 1) {
+    const float K = (float)P.strikes[0];
+    float s1[kQ], s2[kQ];
+#pragma unroll
+    for (int q = 0; q < kQ; ++q) s1[q] = s2[q] = 0.0f;
+    for (unsigned long long i = t0 + threadIdx.x; i < t1; i += kPayoffBlock) {
+      auto fld = [&](int sc, int f) { return P.records[(size_t)(sc * F + f) * stride + i]; };
+      float q[kQ];
+#pragma unroll
+      for (int k = 0; k < kQ; ++k) q[k] = 0.0f;
+      path_quantities(P, fld, K, q);
+#pragma unroll
+      for (int k = 0; k < kQ; ++k) {
+        s1[k] += q[k];
+        s2[k] = fmaf(q[k], q[k], s2[k]);
+      }
+    }
+    // block reduction in FP64
+#pragma unroll
+    for (int k = 0; k < kQ; ++k) {
+      double a = s1[k], b = s2[k];
+      for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+      }
+      if (lane == 0) {
+        red[warp][2 * k][0] = a;
+        red[warp][2 * k + 1][0] = b;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x < 2 * kQ) {
+      double t = 0.0;
+      for (int w = 0; w < kPayoffBlock / 32; ++w) t += red[w][threadIdx.x][0];
+      const int k = threadIdx.x >> 1;
+      if (k >= nq) t = 0.0;
+      P.partials[((P.tile0 + tile) * 1 + 0) * (2 * kQ) + threadIdx.x] = t;
+    }
+    return;
+  }
+
+  // Strip: lane = strike within a 32-strike chunk; a warp walks 32-path batches.
+  const int kidx = blockIdx.y * 32 + lane;
+  const bool kvalid = kidx < P.n_strikes;
+  const float K = kvalid ? (float)P.strikes[kidx] : 0.0f;
+  double d1[kQ], d2[kQ];
+#pragma unroll
+  for (int q = 0; q < kQ; ++q) d1[q] = d2[q] = 0.0;
+  const int nsf = P.n_sc * F;
+  const unsigned long long per_warp = (unsigned long long)P.tile_paths / (kPayoffBlock / 32);
+  const unsigned long long w0 = t0 + (unsigned long long)warp * per_warp;
+  const unsigned long long w1 = min(w0 + per_warp, t1);
+  for (unsigned long long b0 = w0; b0 < w1; b0 += 32) {
+    const unsigned long long i = b0 + lane;
+    for (int j = 0; j < nsf; ++j) stage[warp][j][lane] = i < w1 ? P.records[(size_t)j * stride + i] : 0.0f;
+    __syncwarp();
+    const int nb = (int)min((unsigned long long)32, w1 - b0);
+    float s1[kQ], s2[kQ];
+#pragma unroll
+    for (int q = 0; q < kQ; ++q) s1[q] = s2[q] = 0.0f;
+    if (kvalid) {
+      for (int pth = 0; pth < nb; ++pth) {
+        auto fld = [&](int sc, int f) { return stage[warp][sc * F + f][pth]; };
+        float q[kQ];
+#pragma unroll
+        for (int k = 0; k < kQ; ++k) q[k] = 0.0f;
+        path_quantities(P, fld, K, q);
+#pragma unroll
+        for (int k = 0; k < kQ; ++k) {
+          s1[k] += q[k];
+          s2[k] = fmaf(q[k], q[k], s2[k]);
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kQ; ++q) {
+      d1[q] += (double)s1[q];
+      d2[q] += (double)s2[q];
+    }
+    __syncwarp();
+  }
+#pragma unroll
+  for (int q = 0; q < kQ; ++q) {
+    red[warp][2 * q][lane] = d1[q];
+    red[warp][2 * q + 1][lane] = d2[q];
+  }
+  __syncthreads();
+  if (warp == 0 && kvalid) {
+    double *dst = P.partials + ((P.tile0 + tile) * (unsigned long long)P.n_strikes + kidx) * (2 * kQ);
+    for (int j = 0; j < 2 * kQ; ++j) {
+      double t = 0.0;
+      for (int w = 0; w < kPayoffBlock / 32; ++w) t += red[w][j][lane];
+      if ((j >> 1) >= nq) t = 0.0;
+      dst[j] = t;
+    }
+  }
+}
+
+// One thread per (strike, quantity): fixed-order FP64 sum over tiles, then
+// mean * df and sqrt((E[x^2] - E[x]^2) / M) * df (MonteCarloPricer.hpp:448-457).
+__global__ void finalize_kernel(const FinalizeParams P) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= P.n_strikes * kQ) return;
+  const int k = idx / kQ, q = idx % kQ;
+  double s = 0.0, ss = 0.0;
+  if ((P.active_mask >> q) & 1) {
+    for (unsigned long long t = 0; t < P.n_tiles; ++t) {
+      const double *src = P.partials + (t * (unsigned long long)P.n_strikes + k) * (2 * kQ);
+      s += src[2 * q];
+      ss += src[2 * q + 1];
+    }
+  }
+  const double mean = s * P.inv_m;
+  double var = ss * P.inv_m - mean * mean;
+  if (var < 0.0) var = 0.0;
+  P.out[(size_t)(2 * q) * P.n_strikes + k] = mean * P.df;
+  P.out[(size_t)(2 * q + 1) * P.n_strikes + k] = sqrt(var * P.inv_m) * P.df;
+}
+
+}  // namespace dev
+
+cudaError_t launch_payoff(const PayoffParams &P, unsigned long long n_tiles, cudaStream_t stream) {
+  if (n_tiles == 0) return cudaSuccess;
+  const dim3 grid((unsigned int)n_tiles, P.n_strikes == 1 ? 1u : (unsigned int)((P.n_strikes + 31) / 32));
+  dev::payoff_reduce_kernel<<<grid, kPayoffBlock, 0, stream>>>(P);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const FinalizeParams &P, cudaStream_t stream) {
+  const int n = P.n_strikes * kQ;
+  dev::finalize_kernel<<<(n + 127) / 128, 128, 0, stream>>>(P);
+  return cudaGetLastError();
+}
+
+}  // namespace myql

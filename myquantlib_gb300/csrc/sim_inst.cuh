@@ -1,0 +1,15 @@
+// sim_inst.cuh -- launch helper shared by the simulate instantiation units.
+#pragma once
+#include "simulate.cuh"
+
+namespace myql {
+template <int NF, int S1, int S2>
+cudaError_t launch_sim_t(const SimParams &P, bool path_dep, cudaStream_t stream) {
+  const unsigned int grid = (P.n_streams + kSimBlock - 1) / kSimBlock;
+  if (path_dep)
+    dev::simulate_kernel<NF, S1, S2, true><<<grid, kSimBlock, 0, stream>>>(P);
+  else
+    dev::simulate_kernel<NF, S1, S2, false><<<grid, kSimBlock, 0, stream>>>(P);
+  return cudaGetLastError();
+}
+}  // namespace myql

@@ -1,0 +1,242 @@
+// simulate.cuh -- phase 1 of a pricing request: path simulation.
+//
+// One thread owns one xoshiro256++ stream and simulates the paths
+// i = s, s + S, s + 2S, ... of that stream (S = number of streams), keeping
+// log-spot X = log(S_t / S0), the CIR variances and the tracker state in FP32
+// registers.  For GreekMode::Full every path is replayed from the stream state
+// saved at its start for each bumped scenario (common random numbers), exactly
+// as MonteCarloPricer.hpp:302-410 replays `rng_start`; the base scenario is the
+// one that advances the stream.  Each (scenario, path) leaves a compact
+// terminal record that the payoff pass turns into prices and Greeks.
+//
+// Template parameters: number of CIR factors and the scheme of each factor
+// (the Stepper's VolScheme1 / VolScheme2), and whether the instrument's tracker
+// is path dependent.  Jump policy and tracker kind are uniform runtime values.
+#pragma once
+#include "device_numerics.cuh"
+#include "engine_types.h"
+
+namespace myql {
+namespace dev {
+
+enum { SCH_NONE = 0, SCH_NV = 1, SCH_EXACT = 2, SCH_NCI = 3 };
+
+// Chi-squared quantile of the SchemeNCI table (VolSchemes.hpp:334-370): cubic
+// Hermite cell of row N on the U grid, or the tail grid for U >= 0.999.
+__device__ __forceinline__ float nci_quantile(const NciTable &tab, int N,
+                                              unsigned long long x2,
+                                              unsigned long long u999,
+                                              unsigned int &fallbacks) {
+  if (N < tab.rows) {
+    if (x2 < u999) {
+      const unsigned long long hi = __umul64hi(x2, tab.pos_scale);  // U*inv_dx * 2^50
+      int i = (int)(hi >> 50);
+      i = min(i, kNciGrid - 2);
+      const float t = (float)((unsigned int)(hi >> 26) & 0xFFFFFFu) * 5.9604644775390625e-8f;
+      const float4 c = __ldg(tab.main + (size_t)N * (kNciGrid - 1) + i);
+      return fmaf(fmaf(fmaf(c.w, t, c.z), t, c.y), t, c.x);
+    }
+    const float w = -__logf(u01c_bits(x2));
+    float pos = (w - tab.tail_w0) * tab.tail_inv_dw;
+    pos = fminf(fmaxf(pos, 0.0f), (float)(kNciTail - 1) - 1e-3f);
+    const int i = (int)pos;
+    const float t = pos - (float)i;
+    const float4 c = __ldg(tab.tail + (size_t)N * (kNciTail - 1) + i);
+    return fmaf(fmaf(fmaf(c.w, t, c.z), t, c.y), t, c.x);
+  }
+  // Beyond the table (dof >= d + 2*rows): Wilson-Hilferty cube.
+  ++fallbacks;
+  const float nu = tab.d + 2.0f * (float)N;
+  const float z = inv_normal_bits(x2);
+  const float h = 2.0f / (9.0f * nu);
+  const float b = 1.0f - h + z * sqrtf(h);
+  return fmaxf(nu * b * b * b, 0.0f);
+}
+
+// One step of the CIR variance under scheme SCH (VolSchemes.hpp evolve()).
+template <int SCH>
+__device__ __forceinline__ float evolve(float v, Xo &rng, const FactorConst &f,
+                                        const SimParams &P, int fi, unsigned int &caphits,
+                                        unsigned int &fallbacks) {
+  if (SCH == SCH_NV) {
+    // VolSchemes.hpp:52-57: v' = ex (sqrt(ex v + D psi) + s* Z)^2 + D psi
+    const float Z = inv_normal_bits(draw(rng));
+    const float root = sqrt_approx(fmaf(f.w0, v, f.w1)) + f.w2 * Z;
+    return fmaf(f.w0 * root, root, f.w1);
+  } else if (SCH == SCH_EXACT) {
+    // VolSchemes.hpp:207-218: N ~ Poisson(C0 v), v' = Gamma(alpha + N) * scale
+    const int N = poisson_inv(f.w0 * v, draw(rng), P.loop_cap, caphits);
+    const float g = gamma_draw(f.w1, N, rng, P.sm_p[fi], P.sm_inv_p[fi], P.sm_1mp[fi],
+                               P.sm_1ma[fi], P.sm_inv_a[fi], P.loop_cap, caphits);
+    return g * f.w2;
+  } else {
+    // VolSchemes.hpp:334-370: N ~ Poisson(C0 v), v' = chi2_{d+2N}^{-1}(U) * scale
+    const int N = poisson_inv(f.w0 * v, draw(rng), P.loop_cap, caphits);
+    const unsigned long long x2 = draw(rng);
+    return nci_quantile(P.nci[fi], N, x2, P.nci_u999, fallbacks) * f.w2;
+  }
+}
+
+// Compound-Poisson log jump of one window (JumpPolicies.hpp:55-75, :111-135).
+__device__ __forceinline__ float jump_draw(const SimParams &P, const ScenarioConst &C, Xo &rng,
+                                           unsigned int &caphits) {
+  const int n = poisson_small(C.jump_mean, C.jump_exp_neg_mean, rng, P.loop_cap, caphits);
+  if (n == 0) return C.jump_comp;
+  if (P.jump_kind == 1) {
+    const float Z = inv_normal_bits(draw(rng));
+    const float fn = (float)n;
+    return C.jump_comp + fn * P.merton_mu + sqrtf(fn) * P.merton_delta * Z;
+  }
+  float total = 0.0f;
+  const int m = min(n, (int)P.loop_cap);
+  for (int k = 0; k < m; ++k) {
+    const float u = u01_bits(draw(rng));
+    if (u < P.kou_p_up)
+      total += exp_draw(rng, P.kou_inv_eta1);
+    else
+      total -= exp_draw(rng, P.kou_inv_eta2);
+  }
+  return C.jump_comp + total;
+}
+
+// Simulates one path of one scenario; writes the tracker's terminal record.
+template <int NF, int S1, int S2, bool PD>
+__device__ __forceinline__ void sim_path(const SimParams &P, const ScenarioConst &C, Xo &rng,
+                                         float (&out)[kMaxFields], unsigned int &caphits,
+                                         unsigned int &fallbacks) {
+  float X = 0.0f;
+  float va = C.f[0].v0, vb = C.f[1].v0;
+  const int trk = P.tracker;
+  float acc = 0.0f, mn = P.lb_min0, mx = P.lb_max0;
+  float tb = -1.0f, tu = -1.0f, td = -1.0f;
+  if (PD && trk >= TRK_BARRIER_UP) {  // Day-0 breach (PathTrackers.hpp:194-215)
+    if (trk == TRK_BARRIER_UP) {
+      if (0.0f >= P.b_log[0]) tb = 0.0f;
+      if (0.0f >= P.b_log[1]) tu = 0.0f;
+      if (0.0f >= P.b_log[2]) td = 0.0f;
+    } else {
+      if (0.0f <= P.b_log[0]) tb = 0.0f;
+      if (0.0f <= P.b_log[1]) tu = 0.0f;
+      if (0.0f <= P.b_log[2]) td = 0.0f;
+    }
+  }
+  const int n = P.n_steps;
+  if (NF == 0 && !PD) {
+    // GBM European: one Gaussian over T plus one jump (ASVJstepper.hpp:145-161)
+    const float G = inv_normal_bits(draw(rng));
+    X = fmaf(C.gbm_vol, G, C.gbm_drift);
+    if (P.jump_kind) X += jump_draw(P, C, rng, caphits);
+  } else {
+    const float dt = C.dt;
+    for (int k = 0; k < n; ++k) {
+      const float G = inv_normal_bits(draw(rng));
+      if (NF == 0) {
+        X += fmaf(C.gbm_vol, G, C.gbm_drift);
+      } else if (NF == 1) {
+        const FactorConst &f = C.f[0];
+        const float vn = evolve<S1>(va, rng, f, P, 0, caphits, fallbacks);
+        const float root = sqrt_approx(f.C3 * (va + vn));
+        X += fmaf(root, G, fmaf(f.C2, vn, fmaf(f.C1, va, f.C0)));
+        va = vn;
+      } else {
+        const FactorConst &f0 = C.f[0];
+        const FactorConst &f1 = C.f[1];
+        const float van = evolve<S1>(va, rng, f0, P, 0, caphits, fallbacks);
+        const float vbn = evolve<S2>(vb, rng, f1, P, 1, caphits, fallbacks);
+        const float root = sqrt_approx(fmaf(f0.C3, va + van, f1.C3 * (vb + vbn)));
+        const float drift =
+            fmaf(f1.C2, vbn, fmaf(f1.C1, vb, fmaf(f0.C2, van, fmaf(f0.C1, va, f0.C0))));
+        X += fmaf(root, G, drift);
+        va = van;
+        vb = vbn;
+      }
+      if (PD) {
+        if (P.jump_kind) X += jump_draw(P, C, rng, caphits);
+        const float t = (float)(k + 1) * dt;
+        switch (trk) {
+          case TRK_GEO_ASIAN: acc += X; break;
+          case TRK_ARITH_ASIAN: acc += __expf(X); break;
+          case TRK_LOOKBACK:
+            mn = fminf(mn, X);
+            mx = fmaxf(mx, X);
+            break;
+          case TRK_BARRIER_UP:
+            if (tu < 0.0f && X >= P.b_log[1]) tu = t;
+            if (tb < 0.0f && X >= P.b_log[0]) tb = t;
+            if (td < 0.0f && X >= P.b_log[2]) td = t;
+            break;
+          case TRK_BARRIER_DOWN:
+            if (td < 0.0f && X <= P.b_log[2]) td = t;
+            if (tb < 0.0f && X <= P.b_log[0]) tb = t;
+            if (tu < 0.0f && X <= P.b_log[1]) tu = t;
+            break;
+          default: break;
+        }
+      }
+    }
+    if (!PD && NF > 0 && P.jump_kind) X += jump_draw(P, C, rng, caphits);
+  }
+  out[0] = X;
+  if (PD) {
+    switch (trk) {
+      case TRK_GEO_ASIAN: out[1] = C.dt * (acc - 0.5f * X); break;
+      case TRK_ARITH_ASIAN: out[1] = C.dt * (0.5f + acc - 0.5f * __expf(X)); break;
+      case TRK_LOOKBACK:
+        out[1] = mn;
+        out[2] = mx;
+        break;
+      case TRK_BARRIER_UP:
+      case TRK_BARRIER_DOWN:
+        out[1] = tb;
+        out[2] = tu;
+        out[3] = td;
+        break;
+      default: break;
+    }
+  }
+}
+
+template <int NF, int S1, int S2, bool PD>
+__global__ void __launch_bounds__(kSimBlock) simulate_kernel(const __grid_constant__ SimParams P) {
+  const unsigned int s = blockIdx.x * kSimBlock + threadIdx.x;
+  const unsigned int S = P.n_streams;
+  if (s >= S) return;
+  Xo rng;
+  rng.a = P.states[s];
+  rng.b = P.states[(size_t)S + s];
+  rng.c = P.states[2 * (size_t)S + s];
+  rng.d = P.states[3 * (size_t)S + s];
+  unsigned int caphits = 0, fallbacks = 0;
+  const int F = P.n_fields;
+  for (unsigned long long i = P.path_begin + s; i < P.path_end; i += S) {
+    const Xo start = rng;
+    const size_t col = (size_t)(i - P.rec_offset);
+    for (int sc = 0; sc < P.n_sc; ++sc) {
+      Xo r = start;
+      float f[kMaxFields];
+      sim_path<NF, S1, S2, PD>(P, P.sc[sc], r, f, caphits, fallbacks);
+      float *dst = P.records + (size_t)sc * F * P.rec_stride + col;
+      dst[0] = f[0];
+      if (PD) {
+        if (F > 1) dst[P.rec_stride] = f[1];
+        if (F > 2) dst[2 * P.rec_stride] = f[2];
+        if (F > 3) dst[3 * P.rec_stride] = f[3];
+      }
+      if (sc == 0) rng = r;
+    }
+  }
+  P.states[s] = rng.a;
+  P.states[(size_t)S + s] = rng.b;
+  P.states[2 * (size_t)S + s] = rng.c;
+  P.states[3 * (size_t)S + s] = rng.d;
+  if (caphits) atomicAdd(P.status, caphits);
+  if (fallbacks) atomicAdd(P.status + 1, fallbacks);
+}
+
+}  // namespace dev
+
+// Host launcher: dispatches to the compiled instantiation (defined in sim_*.cu).
+cudaError_t launch_simulate(const SimParams &P, int s1, int s2, bool path_dep,
+                            cudaStream_t stream);
+
+}  // namespace myql

@@ -1,0 +1,229 @@
+// tables.cu -- device set-up kernels: xoshiro stream seeding (jump-ahead) and
+// the FP64 build of the SchemeNCI chi-squared tables; plus numerics probes.
+#include "chi2_fp64.cuh"
+#include "device_numerics.cuh"
+#include "engine_types.h"
+
+namespace myql {
+
+__constant__ unsigned long long c_jump[64][4];
+
+namespace dev {
+
+__device__ __forceinline__ void xo_transition(Xo &s) {
+  const unsigned long long t = s.b << 17;
+  s.c ^= s.a;
+  s.d ^= s.b;
+  s.b ^= s.c;
+  s.a ^= s.d;
+  s.c ^= t;
+  s.d = rotl64(s.d, 45);
+}
+
+// State advanced by 2^(128+i) steps (Vigna's jump loop with polynomial i).
+__device__ void jump_apply(Xo &s, int i) {
+  unsigned long long a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+  for (int w = 0; w < 4; ++w) {
+    const unsigned long long poly = c_jump[i][w];
+    for (int b = 0; b < 64; ++b) {
+      if ((poly >> b) & 1ull) {
+        a0 ^= s.a;
+        a1 ^= s.b;
+        a2 ^= s.c;
+        a3 ^= s.d;
+      }
+      xo_transition(s);
+    }
+  }
+  s.a = a0;
+  s.b = a1;
+  s.c = a2;
+  s.d = a3;
+}
+
+__device__ Xo splitmix_seed(unsigned long long x) {
+  Xo s;
+  unsigned long long v[4];
+  for (int i = 0; i < 4; ++i) {
+    unsigned long long z = (x += 0x9e3779b97f4a7c15ull);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    v[i] = z ^ (z >> 31);
+  }
+  s.a = v[0];
+  s.b = v[1];
+  s.c = v[2];
+  s.d = v[3];
+  return s;
+}
+
+// Block b produces streams first + 128 b + t: thread 0 jumps the seeded state
+// to the block's first stream (one polynomial per set bit of its index), then
+// a doubling tree fills the other 127 states with one jump each.
+constexpr int kSeedBlock = 128;
+__global__ void __launch_bounds__(kSeedBlock) seed_streams_kernel(unsigned long long seed,
+                                                                  unsigned long long first,
+                                                                  unsigned long long n,
+                                                                  unsigned long long *out) {
+  __shared__ Xo sh[kSeedBlock];
+  const unsigned long long base = first + (unsigned long long)blockIdx.x * kSeedBlock;
+  if (threadIdx.x == 0) {
+    Xo s = splitmix_seed(seed);
+    for (int i = 0; i < 64; ++i)
+      if ((base >> i) & 1ull) jump_apply(s, i);
+    sh[0] = s;
+  }
+  __syncthreads();
+  for (int r = 0; (1 << r) < kSeedBlock; ++r) {
+    const int span = 1 << r;
+    if ((int)threadIdx.x < span) {
+      Xo s = sh[threadIdx.x];
+      jump_apply(s, r);
+      sh[threadIdx.x + span] = s;
+    }
+    __syncthreads();
+  }
+  const unsigned long long k = (unsigned long long)blockIdx.x * kSeedBlock + threadIdx.x;
+  if (k < n) {
+    const Xo s = sh[threadIdx.x];
+    out[k] = s.a;
+    out[n + k] = s.b;
+    out[2 * n + k] = s.c;
+    out[3 * n + k] = s.d;
+  }
+}
+
+__global__ void rng_draws_kernel(const unsigned long long *states, unsigned long long n,
+                                 unsigned long long count, unsigned long long *out) {
+  const unsigned long long k = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  Xo s{states[k], states[n + k], states[2 * n + k], states[3 * n + k]};
+  for (unsigned long long i = 0; i < count; ++i) out[k * count + i] = xo_next(s);
+}
+
+// ---- SchemeNCI table build (FP64) -----------------------------------------
+__global__ void nci_nodes_main_kernel(double d, int rows, double dx, double *y) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)rows * kNciGrid) return;
+  const int k = (int)(idx / kNciGrid), i = (int)(idx % kNciGrid);
+  const double nu = d + 2.0 * k;
+  const double p = i * dx;
+  double v = 0.0;
+  if (i > 0) v = p <= 0.5 ? chi2_quantile(nu, p, false) : chi2_quantile(nu, 1.0 - p, true);
+  y[idx] = v;
+}
+
+__global__ void nci_nodes_tail_kernel(double d, int rows, double w0, double dw, double *y,
+                                      double *m) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)rows * kNciTail) return;
+  const int k = (int)(idx / kNciTail), j = (int)(idx % kNciTail);
+  const double nu = d + 2.0 * k;
+  const double w = w0 + j * dw;
+  const double q = exp(-w);
+  const double v = chi2_quantile(nu, q, true);
+  y[idx] = v;
+  m[idx] = exp(-w - chi2_logpdf(nu, v));  // dy/dw = q / f(y)
+}
+
+// Monotone cubic Hermite cells with the reference's harmonic-mean slopes
+// (VolSchemes.hpp:292-310), stored as monomial coefficients in t.
+__device__ __forceinline__ double nci_slope(const double *yr, int i, double inv_dx) {
+  if (i == 0) return (yr[1] - yr[0]) * inv_dx;
+  if (i == kNciGrid - 1) return (yr[i] - yr[i - 1]) * inv_dx;
+  const double d1 = (yr[i] - yr[i - 1]) * inv_dx;
+  const double d2 = (yr[i + 1] - yr[i]) * inv_dx;
+  return d1 * d2 > 0.0 ? 2.0 * d1 * d2 / (d1 + d2) : 0.0;
+}
+
+__device__ __forceinline__ float4 hermite_cell(double y0, double y1, double hm0, double hm1) {
+  return make_float4((float)y0, (float)hm0, (float)(3.0 * (y1 - y0) - (2.0 * hm0 + hm1)),
+                     (float)(2.0 * (y0 - y1) + (hm0 + hm1)));
+}
+
+__global__ void nci_cells_main_kernel(int rows, const double *y, double dx, float4 *cells) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)rows * (kNciGrid - 1)) return;
+  const int k = (int)(idx / (kNciGrid - 1)), i = (int)(idx % (kNciGrid - 1));
+  const double *yr = y + (size_t)k * kNciGrid;
+  const double inv_dx = 1.0 / dx;
+  const double m0 = nci_slope(yr, i, inv_dx), m1 = nci_slope(yr, i + 1, inv_dx);
+  cells[idx] = hermite_cell(yr[i], yr[i + 1], dx * m0, dx * m1);
+}
+
+__global__ void nci_cells_tail_kernel(int rows, const double *y, const double *m, double dw,
+                                      float4 *cells) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)rows * (kNciTail - 1)) return;
+  const int k = (int)(idx / (kNciTail - 1)), j = (int)(idx % (kNciTail - 1));
+  const size_t o = (size_t)k * kNciTail + j;
+  cells[idx] = hermite_cell(y[o], y[o + 1], dw * m[o], dw * m[o + 1]);
+}
+
+// ---- probes --------------------------------------------------------------
+__global__ void chi2_probe_kernel(const double *dof, const double *p, double *out, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = p[i] <= 0.5 ? chi2_quantile(dof[i], p[i], false) : chi2_quantile(dof[i], 1.0 - p[i], true);
+}
+
+__global__ void sampler_probe_kernel(int kind, const unsigned long long *x, const double *lam,
+                                     float *out, size_t n, unsigned int cap, unsigned int *status) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  unsigned int hits = 0;
+  if (kind == 0)
+    out[i] = inv_normal_bits(x[i]);
+  else
+    out[i] = (float)poisson_inv((float)lam[i], x[i], cap, hits);
+  if (hits) atomicAdd(status, hits);
+}
+
+}  // namespace dev
+
+cudaError_t upload_jump_polys(const unsigned long long polys[64][4]) {
+  return cudaMemcpyToSymbol(c_jump, polys, sizeof(unsigned long long) * 64 * 4);
+}
+
+cudaError_t launch_seed_streams(unsigned long long seed, unsigned long long first,
+                                unsigned long long n, unsigned long long *out,
+                                cudaStream_t stream) {
+  const unsigned int blocks = (unsigned int)((n + dev::kSeedBlock - 1) / dev::kSeedBlock);
+  dev::seed_streams_kernel<<<blocks, dev::kSeedBlock, 0, stream>>>(seed, first, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rng_draws(const unsigned long long *states, unsigned long long n,
+                             unsigned long long count, unsigned long long *out,
+                             cudaStream_t stream) {
+  dev::rng_draws_kernel<<<(unsigned int)((n + 127) / 128), 128, 0, stream>>>(states, n, count, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_nci_build(double d, int rows, double *tmp_main, double *tmp_ty, double *tmp_tm,
+                             float4 *cells_main, float4 *cells_tail, double w0, double dw,
+                             cudaStream_t stream) {
+  const double dx = kNciUmax / (kNciGrid - 1);
+  const long long nm = (long long)rows * kNciGrid, nt = (long long)rows * kNciTail;
+  dev::nci_nodes_main_kernel<<<(unsigned int)((nm + 127) / 128), 128, 0, stream>>>(d, rows, dx, tmp_main);
+  dev::nci_nodes_tail_kernel<<<(unsigned int)((nt + 127) / 128), 128, 0, stream>>>(d, rows, w0, dw, tmp_ty, tmp_tm);
+  const long long cm = (long long)rows * (kNciGrid - 1), ct = (long long)rows * (kNciTail - 1);
+  dev::nci_cells_main_kernel<<<(unsigned int)((cm + 255) / 256), 256, 0, stream>>>(rows, tmp_main, dx, cells_main);
+  dev::nci_cells_tail_kernel<<<(unsigned int)((ct + 255) / 256), 256, 0, stream>>>(rows, tmp_ty, tmp_tm, dw, cells_tail);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_chi2_probe(const double *dof, const double *p, double *out, size_t n,
+                              cudaStream_t stream) {
+  dev::chi2_probe_kernel<<<(unsigned int)((n + 127) / 128), 128, 0, stream>>>(dof, p, out, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sampler_probe(int kind, const unsigned long long *x, const double *lam,
+                                 float *out, size_t n, unsigned int cap, unsigned int *status,
+                                 cudaStream_t stream) {
+  dev::sampler_probe_kernel<<<(unsigned int)((n + 127) / 128), 128, 0, stream>>>(kind, x, lam, out, n, cap, status);
+  return cudaGetLastError();
+}
+
+}  // namespace myql

@@ -196,6 +196,16 @@ int myql_abi_version(void);
  * to provoke MYQL_ERR_LOOP_CAP without touching the GPU's health. */
 myql_status myql_ctx_set_loop_cap(myql_ctx *ctx, uint32_t max_loop_iters);
 
+/* Upper bound on the per-path record scratch of one launch (bytes; 0 = the
+ * 2 GiB default).  Larger requests are simulated in chunks of whole stream
+ * rounds; results do not depend on the chunking. */
+myql_status myql_ctx_set_records_limit(myql_ctx *ctx, uint64_t bytes);
+
+/* Host-side validation of a job, without a device: the checks myql_mc_price
+ * runs before any launch (MYQL_ERR_NV_CONDITION for SchemeNV with
+ * sigma^2 > 4 kappa theta, as VolSchemes.hpp:40-41 throws). */
+myql_status myql_validate_job(const myql_mc_job *job);
+
 /* --- pricing entry points ------------------------------------------------ */
 
 /* One pricing request: replaces MonteCarloPricer::calculate (MonteCarloPricer.hpp:95).

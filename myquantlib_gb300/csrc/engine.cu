@@ -743,6 +743,20 @@ myql_status myql_ctx_set_loop_cap(myql_ctx *ctx, uint32_t cap) {
   return MYQL_OK;
 }
 
+myql_status myql_ctx_set_records_limit(myql_ctx *ctx, uint64_t bytes) {
+  if (!ctx) return set_error(MYQL_ERR_INVALID_ARG, "null context");
+  ctx->records_cap_bytes = bytes ? bytes : (2ull << 30);
+  return MYQL_OK;
+}
+
+myql_status myql_validate_job(const myql_mc_job *job) {
+  if (!job) return set_error(MYQL_ERR_INVALID_ARG, "null job");
+  myql_status s = validate_job(*job);
+  if (s != MYQL_OK) return s;
+  Plan pl;
+  return make_plan(*job, pl);
+}
+
 myql_status myql_mc_price(myql_ctx *ctx, const myql_mc_job *job, double *out,
                           myql_mc_stats *stats) {
   myql_status s = ctx_check(ctx);

@@ -431,6 +431,9 @@ class Engine:
     def set_loop_cap(self, cap: int):
         _abi.check(self.lib.myql_ctx_set_loop_cap(self.handle, cap))
 
+    def set_records_limit(self, nbytes: int):
+        _abi.check(self.lib.myql_ctx_set_records_limit(self.handle, nbytes))
+
     def price(self, job: "_Job") -> tuple[np.ndarray, _abi.McStatsC]:
         out = np.zeros(2 * _abi.Q_COUNT * job.n_strikes, dtype=np.float64)
         st = _abi.McStatsC()
@@ -579,6 +582,12 @@ def make_job(model, stepper: ASVJStepper | None, instrument: _Instrument, mode: 
     c.n_streams = cfg.n_streams
     job.S0, job.r, job.q = S0, r, q
     return _Job(job, strikes)
+
+
+def validate(job: _Job) -> None:
+    """Host-side checks of the engine (no device needed); raises MyqlError."""
+    lib = _abi.load()
+    _abi.check(lib.myql_validate_job(C.byref(job.c)))
 
 
 def result_from_raw(raw: np.ndarray, mode: GreekMode, is_strip: bool, stats=None) -> MonteCarloResult:

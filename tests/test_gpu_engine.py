@@ -1,0 +1,170 @@
+"""GPU tests of the engine's building blocks and edge cases (through the C ABI):
+bit-exact jump-ahead streams, the device samplers against the oracle, the FP64
+chi-squared tables against scipy, size edge cases, determinism, chunking and
+host-side fault injection (loop caps), which faults no GPU."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+from scipy import stats
+
+import jobspec
+import myquantlib_gb300 as m
+import pyrng
+from myquantlib_gb300 import _abi
+
+pytestmark = pytest.mark.gpu
+GOLDEN = Path(__file__).resolve().parent / "golden"
+KAT = json.loads((GOLDEN / "rng_kat.json").read_text())
+MC_SPECS = {s["name"]: s for s in json.loads((GOLDEN / "reference_mc.json").read_text())}
+
+
+def test_stream_states_bit_exact(engine):
+    got = engine.stream_states(42, 0, 4)
+    assert [[int(x) for x in row] for row in got] == KAT["seed42_stream_states_0_3"]
+    for seed, first, n in [(7, 0, 300), (2**63 + 11, 129, 3), (123456789, 1000, 2)]:
+        got = engine.stream_states(seed, first, n)
+        for k in ([0, 1, n - 1] if n > 3 else range(n)):
+            assert [int(x) for x in got[k]] == pyrng.stream_state(seed, first + k), (seed, first, k)
+
+
+def test_stream_draws_bit_exact(engine):
+    got = engine.draws(42, 0, 2, 3)
+    assert [int(x) for x in got[0]] == KAT["seed42_first3"]
+    s = pyrng.stream_state(42, 1)
+    want = []
+    for _ in range(3):
+        o, s = pyrng.next_out(s)
+        want.append(o)
+    assert [int(x) for x in got[1]] == want
+
+
+def test_device_inverse_normal(engine, oracle_lib):
+    lib = oracle_lib.restatement()
+    rng = np.random.default_rng(3)
+    x = rng.integers(0, 2**64, 20000, dtype=np.uint64)
+    x = np.concatenate([x, np.array([1, 2**10, 2**40, 2**63, 2**64 - 2**11, 2**63 + 1], dtype=np.uint64)])
+    got = engine.sampler(0, x).astype(np.float64)
+    want = np.array([lib.myql_oracle_normcdfinv(lib.myql_oracle_uniform_of(int(v))) for v in x])
+    assert np.max(np.abs(got - want) / np.maximum(1.0, np.abs(want))) < 2e-6
+
+
+def test_device_inverse_poisson(engine, oracle_lib):
+    lib = oracle_lib.restatement()
+    rng = np.random.default_rng(5)
+    n = 40000
+    lam = np.concatenate([rng.uniform(0, 4, n // 4), rng.uniform(4, 30, n // 4),
+                          rng.uniform(30, 800, n // 4), rng.lognormal(0, 2, n // 4)])
+    x = rng.integers(0, 2**64, n, dtype=np.uint64)
+    got = engine.sampler(1, x, lam).astype(np.float64)
+    want = np.array([lib.myql_oracle_poissinvcdf(l, lib.myql_oracle_uniform_of(int(v))) for l, v in zip(lam, x)])
+    mism = got != want
+    assert np.mean(mism) < 2e-4, np.mean(mism)
+    assert np.all(np.abs(got - want) <= 1)
+
+
+def test_device_chi2_quantile(engine):
+    rng = np.random.default_rng(9)
+    dof = np.concatenate([[0.494] * 6, rng.uniform(0.05, 2500, 200)])
+    p = np.concatenate([[1e-4, 0.001, 0.5, 0.9, 0.999, 1 - 1e-12], rng.uniform(0, 0.999, 200)])
+    got = engine.chi2_quantile(dof, p)
+    want = stats.chi2.ppf(p, dof)
+    assert np.max(np.abs(got - want) / want) < 1e-9
+
+
+def base_spec():
+    return jobspec.with_config(MC_SPECS["c1_heston_nv_call"], paths=50000, steps=50)
+
+
+def test_deterministic_and_chunking_invariant(engine):
+    job = jobspec.make_job(base_spec())
+    a, _ = engine.price(job)
+    b, _ = engine.price(job)
+    assert np.array_equal(a, b)
+    engine.set_records_limit(1 << 14)  # forces many chunks of whole stream rounds
+    try:
+        c, st = engine.price(job)
+    finally:
+        engine.set_records_limit(0)
+    assert np.allclose(a, c, rtol=1e-12, atol=0)
+    assert st.kernel_launches > 4
+
+
+@pytest.mark.parametrize("paths,streams", [(1, 0), (3, 0), (1000, 4096), (131073, 0), (5000, 7)])
+def test_path_count_edges(engine, oracle_lib, paths, streams):
+    spec = jobspec.with_config(MC_SPECS["heston_nv_put_full"], paths=paths, streams=streams, steps=20)
+    job = jobspec.make_job(spec)
+    raw, st = engine.price(job)
+    want, _ = oracle_lib.mc_price(job, oracle_lib.LAYOUT_STREAMS, 8)
+    assert st.paths == paths
+    assert np.all(np.isfinite(raw))
+    np.testing.assert_allclose(raw[0], want[0], rtol=2e-4, atol=1e-5)
+
+
+def test_large_strip(engine, oracle_lib):
+    spec = jobspec.with_config(MC_SPECS["c2_bates_nci_strip_essential"], paths=4096, streams=512)
+    spec["instrument"]["K"] = list(np.linspace(50.0, 150.0, 1000))
+    job = jobspec.make_job(spec)
+    raw, _ = engine.price(job)
+    want, _ = oracle_lib.mc_price(job, oracle_lib.LAYOUT_STREAMS, 8)
+    se = np.maximum(raw[1::2], 1e-12)
+    assert np.max(np.abs(raw[0::2] - want[0::2]) / se) < 0.35
+
+
+def test_day0_barrier_breach_prices_zero(engine):
+    raw, _ = engine.price(jobspec.make_job(MC_SPECS["bs_downout_put_day0_breach"]))
+    assert raw[0, 0] == 0.0 and raw[1, 0] == 0.0
+
+
+def test_loop_cap_fault_injection_keeps_context_usable(engine):
+    """A capped device loop reports MYQL_ERR_LOOP_CAP (no trap, no hang) and the
+    context keeps working: the next call returns the normal result."""
+    spec = jobspec.with_config(MC_SPECS["heston_exact_call"], paths=20000)
+    job = jobspec.make_job(spec)
+    good, _ = engine.price(job)
+    engine.set_loop_cap(1)
+    try:
+        with pytest.raises(_abi.MyqlError) as e:
+            engine.price(job)
+        assert e.value.status == _abi.ERR_LOOP_CAP
+    finally:
+        engine.set_loop_cap(0)
+    again, _ = engine.price(job)
+    assert np.array_equal(good, again)
+
+
+def test_nv_condition_status_through_engine(engine):
+    model = m.HestonModel(m.HestonParams(1.0, 0.01, 0.5, -0.7, 0.04))
+    pr = m.MonteCarloPricer(model, m.HestonStepper(m.SchemeNV), m.GreekMode.NONE,
+                            m.MonteCarloConfig(num_paths=1000), engine=engine)
+    with pytest.raises(_abi.MyqlError) as e:
+        pr.calculate(100.0, 0.02, 0.0, m.EuropeanOption(100.0, 1.0))
+    assert e.value.status == _abi.ERR_NV_CONDITION
+
+
+def test_barrier_in_plus_out_equals_european(engine):
+    """barrier_test.cpp:97-98: with common random numbers, in + out = vanilla exactly."""
+    h = m.HestonModel(m.HestonParams(1.5, 0.04, 0.3, -0.7, 0.04))
+    cfg = m.MonteCarloConfig(num_paths=1 << 16, time_steps=252, seed=7)
+    st = m.HestonStepper(m.SchemeNV)
+    vin = m.MonteCarloPricer(h, st, m.GreekMode.NONE, cfg, engine).calculate(100.0, 0.02, 0.0, m.UpAndInCall(100.0, 120.0, 1.0))
+    vout = m.MonteCarloPricer(h, st, m.GreekMode.NONE, cfg, engine).calculate(100.0, 0.02, 0.0, m.UpAndOutCall(100.0, 120.0, 1.0))
+    # the European leg must use the same stream consumption: a path-dependent tracker
+    # that never knocks (barrier far away) reproduces the vanilla payoff path by path
+    veur = m.MonteCarloPricer(h, st, m.GreekMode.NONE, cfg, engine).calculate(100.0, 0.02, 0.0, m.UpAndOutCall(100.0, 1e9, 1.0))
+    # per-batch FP32 sums: in + out and the vanilla agree to FP32 summation rounding
+    assert abs((vin.price + vout.price) - veur.price) < 2e-6 * veur.price
+
+
+def test_arith_asian_one_step_equals_half_european(engine):
+    """asian_test.cpp:75-77: a one-step arithmetic Asian (trapezoid of S0 and S_T)
+    equals 1/2 of a European call struck at 2K - S0."""
+    h = m.HestonModel(m.HestonParams(1.5, 0.04, 0.3, -0.7, 0.04))
+    cfg = m.MonteCarloConfig(num_paths=1 << 18, time_steps=1, seed=11)
+    a = m.MonteCarloPricer(h, m.HestonStepper(m.SchemeNV), m.GreekMode.NONE, cfg, engine).calculate(
+        100.0, 0.02, 0.0, m.AsianOption(m.TrackerArithAsian, m.PayoffVanilla(), True, 100.0, 1.0))
+    e = m.MonteCarloPricer(h, m.HestonStepper(m.SchemeNV), m.GreekMode.NONE, cfg, engine).calculate(
+        100.0, 0.02, 0.0, m.EuropeanOption(100.0, 1.0))
+    # same path: avg = (S0 + S_T)/2, payoff = max(S_T - (2K - S0), 0)/2 = max(S_T - K,0)/2 at K=S0
+    assert abs(a.price - 0.5 * e.price) < 1e-4 * e.price

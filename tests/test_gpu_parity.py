@@ -1,0 +1,174 @@
+"""GPU parity of the Monte Carlo hot path (calls through the C ABI).
+
+Three layers, from tightest to loosest:
+ 1. path-by-path replay: the GPU and the FP64 oracle draw the same xoshiro
+    streams (stream k = seed jumped k times, path i on stream i mod S), so each
+    path's terminal state must agree to FP32 accuracy, and prices/Greeks must
+    agree far inside one standard error;
+ 2. the reference's own estimator (OpenMP thread layout, seed + t*999983):
+    independent samples, agreement within 4 combined standard errors;
+ 3. the reference's FP64 Fourier oracle (tests/golden/reference_fourier.json):
+    |z| < 4 for price and Greeks, the reference's own ERROR threshold
+    (mc_full_greek_verifier.cpp:62-84).
+"""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import jobspec
+import myquantlib_gb300 as m
+from myquantlib_gb300 import _abi
+
+pytestmark = pytest.mark.gpu
+GOLDEN = Path(__file__).resolve().parent / "golden"
+MC_SPECS = {s["name"]: s for s in json.loads((GOLDEN / "reference_mc.json").read_text())}
+FOURIER = {s["name"]: s for s in json.loads((GOLDEN / "reference_fourier.json").read_text())}
+
+# ---------------------------------------------------------------- 1. replay
+REPLAY = [
+    ("c1_heston_nv_call", 16384, 1024),
+    ("heston_nv_put_full", 4096, 512),
+    ("heston_exact_call", 8192, 1024),
+    ("heston_nci_call", 8192, 1024),
+    ("c2_bates_nci_full_k100_t1", 2048, 512),
+    ("c2_bates_nci_strip_essential", 4096, 512),
+    ("c3_bateskou_nci_asian", 4096, 512),
+    ("c3_bateskou_nci_upout", 4096, 512),
+    ("c3_dheston_nci_asian", 4096, 512),
+    ("c4_dbates_nv_nci_asian", 2048, 512),
+    ("c5_heston_nv_downout_put", 4096, 512),
+    ("heston_lookback_float_call", 4096, 512),
+    ("heston_lookback_inflight", 4096, 512),
+    ("bs_geo_asian_inflight", 4096, 512),
+    ("heston_arith_asian_inflight", 4096, 512),
+    ("heston_cash_digital_essential", 8192, 1024),
+    ("heston_asset_digital_put_full", 4096, 512),
+    ("dbateskou_nv_full", 2048, 512),
+    ("bs_call_oneshot", 8192, 1024),
+]
+
+
+def views_from_gpu(spec, job, g):
+    """GPU records -> (S_T, second value, hit times) per scenario, FP64."""
+    S0 = job.c.S0
+    X = g[:, 0, :].astype(np.float64)
+    ST = S0 * np.exp(X)
+    kind = spec["instrument"]["kind"]
+    ins = job.c.instrument
+    n = job.c.config.time_steps
+    T = ins.maturity
+    c = job.c.config
+    dts = np.full(g.shape[0], T / n)
+    if g.shape[0] >= 5:  # Full: T-bumped scenarios 3, 4
+        dts[3] = (T + c.t_bump) / n
+        dts[4] = (T - c.t_bump) / n
+    second = None
+    if kind == "asian_geo":
+        Tt = n * dts + ins.t_elapsed
+        c0 = (ins.past_avg_log * ins.t_elapsed + np.log(S0) * n * dts) / Tt - np.log(S0)
+        second = S0 * np.exp(c0[:, None] + g[:, 1, :] / Tt[:, None])
+    elif kind == "asian_arith":
+        Tt = n * dts + ins.t_elapsed
+        second = S0 * (ins.past_avg_S * ins.t_elapsed / (S0 * Tt))[:, None] + S0 * g[:, 1, :] / Tt[:, None]
+    elif kind == "lookback":
+        second = S0 * np.exp(g[:, 1, :])
+    hits = g[:, 1:4, :] if kind == "barrier" else None
+    return ST, second, hits
+
+
+@pytest.mark.parametrize("name,paths,streams", REPLAY, ids=[r[0] for r in REPLAY])
+def test_path_replay_against_oracle(engine, oracle_lib, name, paths, streams):
+    spec = jobspec.with_config(MC_SPECS[name], paths=paths, streams=streams, seed=20261203)
+    job = jobspec.make_job(spec)
+    g = engine.paths(job)                                  # (scenarios, fields, paths) FP32
+    raw, st = engine.price(job)
+    want, rec = oracle_lib.mc_price(job, oracle_lib.LAYOUT_STREAMS, 8, records=True)
+    nsc = g.shape[0]
+    ST, second, hits = views_from_gpu(spec, job, g)
+    rel = np.abs(ST - rec[:nsc, :, 0]) / rec[:nsc, :, 0]
+    # FP32 paths vs FP64 paths on identical random numbers
+    assert np.median(rel) < 1e-5, np.median(rel)
+    assert np.mean(rel > 1e-3) < 2e-3, np.mean(rel > 1e-3)  # discrete flips (Poisson boundaries)
+    if second is not None:
+        rel2 = np.abs(second - rec[:nsc, :, 1]) / np.abs(rec[:nsc, :, 1])
+        assert np.median(rel2) < 1e-5 and np.mean(rel2 > 1e-3) < 2e-3
+    if hits is not None:
+        ho = np.stack([rec[:nsc, :, 3], rec[:nsc, :, 4], rec[:nsc, :, 5]], axis=1)
+        assert np.mean(np.abs(hits - ho) > 1e-4) < 2e-3
+    # same paths -> estimates agree far inside one standard error
+    se = np.maximum(raw[1::2], want[1::2])
+    diff = np.abs(raw[0::2] - want[0::2])
+    ok = diff <= 0.35 * se + 1e-6 * np.abs(want[0::2]) + 1e-12
+    assert ok.all(), (np.array(_abi.Q_NAMES)[~ok.all(axis=1)], (diff / np.maximum(se, 1e-300))[~ok])
+    assert st.loop_cap_hits == 0
+
+
+# ---------------------------------------------------------------- 2. reference estimator
+STAT = [
+    ("c1_heston_nv_call", 1 << 18, 1 << 16),
+    ("heston_nv_put_full", 1 << 17, 1 << 14),
+    ("c2_bates_nci_strip_essential", 1 << 17, 1 << 14),
+    ("c3_bateskou_nci_upout", 1 << 17, 1 << 14),
+    ("c4_dbates_nv_nci_asian", 1 << 16, 1 << 13),
+    ("heston_lookback_float_call", 1 << 17, 1 << 14),
+    ("heston_cash_digital_essential", 1 << 18, 1 << 15),
+]
+
+
+@pytest.mark.parametrize("name,gpu_paths,ref_paths", STAT, ids=[s[0] for s in STAT])
+def test_within_4se_of_reference_estimator(engine, oracle_lib, name, gpu_paths, ref_paths):
+    spec = MC_SPECS[name]
+    gjob = jobspec.make_job(jobspec.with_config(spec, paths=gpu_paths))
+    raw, _ = engine.price(gjob)
+    rjob = jobspec.make_job(jobspec.with_config(spec, paths=ref_paths))
+    ref, _ = oracle_lib.mc_price(rjob, oracle_lib.LAYOUT_REFERENCE, 8)
+    se = np.sqrt(raw[1::2] ** 2 + ref[1::2] ** 2)
+    z = np.where(se > 0, (raw[0::2] - ref[0::2]) / np.maximum(se, 1e-300), 0.0)
+    zero = se == 0
+    assert np.all(np.abs(raw[0::2][zero] - ref[0::2][zero]) < 1e-9)
+    assert np.max(np.abs(z)) < 4.0, dict(zip(_abi.Q_NAMES, np.max(np.abs(z), axis=1)))
+
+
+# ---------------------------------------------------------------- 3. Fourier oracle
+FOURIER_CASES = [
+    ("c1_heston_call", "NV", "none", 1 << 22, 100, {}),
+    ("heston_put_k95_t05", "NV", "full", 1 << 20, 50, {}),
+    ("heston_vg_call", "NV", "full", 1 << 21, 100, {"t_bump": 1e-2}),
+    ("dheston_vg_call", "NV", "full", 1 << 20, 100, {"t_bump": 1e-2}),
+    ("bateskou_vg_call", "NV", "full", 1 << 20, 100, {"t_bump": 1e-2}),
+    ("dbateskou_vg_call", "NV", "full", 1 << 20, 100, {"t_bump": 1e-2}),
+    ("heston_cash_k105", "NV", "essential", 1 << 21, 100, {}),
+    ("heston_asset_put_k95", "NV", "essential", 1 << 21, 100, {}),
+    ("bs_call_k110_t2", None, "full", 1 << 20, 1, {}),
+    ("merton_call", None, "essential", 1 << 21, 1, {}),
+    ("kou_call", None, "essential", 1 << 21, 1, {}),
+    ("heston_nci_call_k100", "NCI", "essential", 1 << 20, 50, {}),
+    ("heston_nci_call_k100", "Exact", "none", 1 << 20, 50, {}),
+    ("c2_bates_call_k100.6349_t1.0", "NCI", "full", 1 << 20, 200, {}),
+    ("c2_bates_call_k60.0000_t0.25", "NCI", "essential", 1 << 20, 50, {}),
+    ("c2_bates_call_k140.0000_t4.0", "NCI", "essential", 1 << 19, 800, {}),
+]
+
+
+@pytest.mark.parametrize("name,scheme,mode,paths,steps,extra", FOURIER_CASES,
+                         ids=[f"{c[0]}-{c[1]}-{c[2]}" for c in FOURIER_CASES])
+def test_against_fourier_oracle(engine, name, scheme, mode, paths, steps, extra):
+    f = FOURIER[name]
+    spec = dict(f)
+    nf = len(f["model"].get("heston", []))
+    spec["schemes"] = [scheme] * nf
+    spec["mode"] = mode
+    spec["config"] = {"paths": paths, "steps": steps, **extra}
+    raw, _ = engine.price(jobspec.make_job(spec))
+    vals, ses = raw[0::2, 0], raw[1::2, 0]
+    four = np.array(f["fourier"])
+    n_active = {"none": 1, "essential": 3, "full": 10}[mode]
+    for q in range(n_active):
+        if q in (4, 8) and nf < 2:
+            continue
+        if ses[q] == 0:
+            continue
+        z = (vals[q] - four[q]) / ses[q]
+        assert abs(z) < 4.0, (_abi.Q_NAMES[q], vals[q], four[q], ses[q], z)

@@ -1,0 +1,343 @@
+#!/usr/bin/env python
+"""Headline benchmark of the GB300 Monte Carlo engine.
+
+Workload (the Bates strip of the baseline configurations): Bates model =
+Heston(kappa 2, theta 0.05, sigma 0.9 [Feller violated], rho -0.6, v0 0.05) +
+Merton jumps (lambda 0.5, mu -0.1, delta 0.15); SchemeNCI; European calls with
+64 strikes uniform on [60, 140] x 8 maturities {0.25, 0.5, 1, 1.5, 2, 2.5, 3, 4};
+200 steps per year; 2^22 paths; GreekMode::Full (CRN delta, gamma, vega, theta,
+rho, vanna, charm: 7 simulated scenarios per path); S0 100, r 0.02, q 0, seed 42.
+One step = pricing the whole strip = 8 pricing requests (one per maturity, as
+the reference prices one maturity per MonteCarloPricer::calculate call).
+
+Metric: paths*steps/s = simulated path-steps (all 7 scenarios) per second.
+  value -- device time of the 8 requests (CUDA events on the launching stream,
+           inputs resident, L2 flushed between steps)
+  e2e   -- the same through the C ABI (myql_mc_price) with pinned host strike
+           and result buffers, host<->device copies inside the timed region
+The reference arm (--impl reference) times the reference's Monte Carlo
+algorithm on the host cores: the FP64 C restatement of the reference (the
+reference's own headers need Boost and cannot be built on the GPU machine) at the
+reference's release flags, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+MATURITIES = [0.25, 0.5, 1.0, 1.5, 2.0, 2.5, 3.0, 4.0]
+STRIKES = list(60.0 + 80.0 * np.arange(64) / 63.0)
+PATHS = 1 << 22
+STEPS_PER_YEAR = 200
+SEED = 42
+N_SCENARIOS = 7
+# algorithmic work per simulated path-step of this workload (Bates, NCI):
+# inverse normal 42 ALU + 1 XU, Poisson inversion 58 ALU + 3 XU, NCI Hermite
+# lookup with its uniform 46 ALU, log-S update 7 ALU + 1 XU; one 16-byte table
+# gather
+ALU_PER_STEP, XU_PER_STEP, GATHER_BYTES = 153, 5, 16
+
+
+def workload_jobs(m, stream_offset: int = 0, paths: int = PATHS):
+    model = m.BatesModel(m.HestonParams(2.0, 0.05, 0.9, -0.6, 0.05), m.MertonParams(0.5, -0.1, 0.15))
+    jobs = []
+    for T in MATURITIES:
+        cfg = m.MonteCarloConfig(num_paths=paths, time_steps=int(round(STEPS_PER_YEAR * T)), seed=SEED,
+                                 stream_offset=stream_offset)
+        jobs.append(m.make_job(model, m.BatesStepper(m.SchemeNCI), m.EuropeanOption(STRIKES, T),
+                               m.GreekMode.FULL, cfg, 100.0, 0.02, 0.0))
+    return jobs
+
+
+def path_steps(paths: int = PATHS) -> tuple[int, int]:
+    base = sum(paths * int(round(STEPS_PER_YEAR * T)) for T in MATURITIES)
+    return base * N_SCENARIOS, base
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def read_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    return json.loads(p.read_text()) if p.exists() else {}
+
+
+def read_traffic() -> float | None:
+    p = ROOT / "profiles" / "simulate_kernel_bates_nci_full.json"
+    if p.exists():
+        return json.loads(p.read_text()).get("dram_bytes_per_launch_full_size")
+    return None
+
+
+def cpu_reference(args, scale_to_full: bool = True) -> dict:
+    """The reference's algorithm on the host cores (FP64 restatement, release flags),
+    timed on two bounded samples of the workload and extrapolated linearly in the
+    path count to the full request (the per-call NCI table builds are the intercept)."""
+    from oracle import oracle
+    import myquantlib_gb300 as m
+    oracle.build(ref=False)
+    cores = os.cpu_count() or 1
+    samples = []
+    for paths in (args.cpu_paths, 2 * args.cpu_paths):
+        jobs = workload_jobs(m, paths=paths)
+        t0 = time.perf_counter()
+        for j in jobs:
+            oracle.mc_price(j, oracle.LAYOUT_REFERENCE, cores, fast=True)
+        samples.append((paths, time.perf_counter() - t0))
+    (p1, t1), (p2, t2) = samples
+    slope = (t2 - t1) / (p2 - p1)
+    intercept = max(t1 - slope * p1, 0.0)
+    full_time = intercept + slope * PATHS
+    sim, _ = path_steps(PATHS)
+    rate = sim / full_time
+    return {"value": rate, "unit": "paths*steps/s", "cores": cores, "kind": "port",
+            "sample": (f"whole workload (8 maturities x 64 strikes, Full Greeks) at {p1} and {p2} "
+                       f"paths ({t1:.1f} s, {t2:.1f} s on {cores} threads), extrapolated linearly in "
+                       f"the path count to 2^22 paths ({full_time:.0f} s)")}
+
+
+def run_reference(args) -> dict:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return {}
+    times = []
+    res = None
+    for _ in range(args.warmup + args.steps):
+        res = cpu_reference(args)
+        times.append(res)
+    vals = [r["value"] for r in times[args.warmup:]]
+    v = statistics.median(vals)
+    cpu = dict(times[-1])
+    cpu["value"] = v
+    return {"metric": "paths*steps/s", "value": v, "unit": "paths*steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference", "cpu_baseline": cpu,
+            "e2e": {"value": v, "unit": "paths*steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "config": workload_config(args)}
+
+
+def workload_config(args) -> dict:
+    sim, base = path_steps()
+    return {"workload": "Bates SchemeNCI European call strip, Full CRN Greeks (configuration 2)",
+            "strikes": 64, "maturities": MATURITIES, "paths": PATHS, "steps_per_year": STEPS_PER_YEAR,
+            "scenarios_per_path": N_SCENARIOS, "simulated_path_steps_per_step": sim,
+            "base_path_steps_per_step": base, "l2": "flushed between steps (256 MiB write)",
+            "parallelism": f"replicas x{args.gpus} (disjoint xoshiro stream ranges)"}
+
+
+def run_engine(args) -> dict:
+    import torch
+    import myquantlib_gb300 as m
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    eng = m.Engine(local)
+    streams_per_rank = 131072
+    jobs = workload_jobs(m, stream_offset=rank * streams_per_rank)
+    nk = len(STRIKES)
+    stream = torch.cuda.Stream(device=local)
+    outs = [torch.empty(2 * 10 * nk, dtype=torch.float64, device=f"cuda:{local}") for _ in jobs]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def step_device():
+        for j, o in zip(jobs, outs):
+            m._abi.check(eng.lib.myql_mc_price_async(eng.handle, m.pricers.C.byref(j.c), o.data_ptr(),
+                                                     stream.cuda_stream))
+
+    # warm-up (also builds the NCI table and the stream table once)
+    launches_per_step = 0
+    for w in range(max(args.warmup, 1)):
+        tot = 0
+        for j in jobs:
+            _, st = eng.price(j)
+            tot += st.kernel_launches
+        launches_per_step = tot
+    with torch.cuda.stream(stream):
+        step_device()
+    torch.cuda.synchronize()
+
+    # ---- device-timed region
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                ev[k][0].record(stream)
+                step_device()
+                ev[k][1].record(stream)
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    dev_ms = sum(a.elapsed_time(b) for a, b in ev)
+
+    # ---- end-to-end through the C ABI: pinned host strikes in, pinned results out
+    pin_k = [torch.tensor(STRIKES, dtype=torch.float64).pin_memory() for _ in jobs]
+    pin_o = [torch.empty(2 * 10 * nk, dtype=torch.float64).pin_memory() for _ in jobs]
+    for j, pk in zip(jobs, pin_k):
+        j.c.instrument.strikes = m.pricers.C.cast(pk.data_ptr(), m.pricers.C.POINTER(m.pricers.C.c_double))
+    stats = []
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for j, po in zip(jobs, pin_o):
+            st = m._abi.McStatsC()
+            m._abi.check(eng.lib.myql_mc_price(eng.handle, m.pricers.C.byref(j.c),
+                                               m.pricers.C.cast(po.data_ptr(), m.pricers.C.POINTER(m.pricers.C.c_double)),
+                                               m.pricers.C.byref(st)))
+            stats.append((st.simulate_ms, st.payoff_ms, st.device_ms, st.kernel_launches))
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+
+    sim, base = path_steps()
+    t_dev = dev_ms / 1e3
+    if dist:
+        import torch as _t
+        buf = _t.tensor([t_dev, e2e_s], device=f"cuda:{local}", dtype=_t.float64)
+        dist.all_reduce(buf, op=dist.ReduceOp.MAX)
+        t_dev, e2e_s = float(buf[0]), float(buf[1])
+    value = world * sim * args.steps / t_dev
+    e2e = world * sim * args.steps / e2e_s
+    if rank != 0:
+        return {}
+
+    # ---- roofline of the dominant kernel (simulate), from its own CUDA events
+    sim_ms = sum(s[0] for s in stats) / args.steps
+    pay_ms = sum(s[1] for s in stats) / args.steps
+    alu_peak = eng.peak(0)
+    xu_peak = eng.peak(1)
+    alu_ach = ALU_PER_STEP * sim / (sim_ms / 1e3)
+    xu_ach = XU_PER_STEP * sim / (sim_ms / 1e3)
+    alu_frac, xu_frac = alu_ach / alu_peak, xu_ach / xu_peak
+    bound = "alu" if alu_frac >= xu_frac else "xu"
+    roof = {"bound": bound, "kernel": "simulate_kernel<1,NCI,-,European>",
+            "achieved": (alu_ach if bound == "alu" else xu_ach) / 1e9,
+            "peak": (alu_peak if bound == "alu" else xu_peak) / 1e9, "unit": "Gop/s",
+            "frac": max(alu_frac, xu_frac),
+            "peak_source": "measured by myql_probe_peak (FP32-FMA / MUFU microbenchmark on this GPU)",
+            "alu": {"achieved": alu_ach / 1e9, "peak": alu_peak / 1e9, "frac": alu_frac, "ops_per_path_step": ALU_PER_STEP},
+            "xu": {"achieved": xu_ach / 1e9, "peak": xu_peak / 1e9, "frac": xu_frac, "ops_per_path_step": XU_PER_STEP},
+            "simulate_ms_per_step": sim_ms, "payoff_ms_per_step": pay_ms,
+            "traffic": read_traffic(),
+            "hbm": {"achieved": GATHER_BYTES * sim / (sim_ms / 1e3) / 1e9,
+                    "peak": read_peaks().get("hbm_gbs"), "unit": "GB/s",
+                    "note": "table gathers are L2-resident; HBM is not the bound"}}
+    line = {"metric": "paths*steps/s", "value": value, "unit": "paths*steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": workload_config(args),
+            "e2e": {"value": e2e, "unit": "paths*steps/s", "h2d_bytes_per_step": 8 * nk * len(jobs),
+                    "d2h_bytes_per_step": 8 * 2 * 10 * nk * len(jobs)},
+            "gpu_launches": launches_per_step * args.steps, "roofline": roof, "clocks": clk.summary()}
+    if world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_reference(args)
+    return line
+
+
+def run_ncu_case() -> None:
+    """A small case of the same kernels for an ncu capture (a few hundred MB on the device)."""
+    import myquantlib_gb300 as m
+    eng = m.Engine(0)
+    job = workload_jobs(m, paths=1 << 18)[MATURITIES.index(1.0)]
+    for _ in range(2):
+        eng.price(job)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
+    ap.add_argument("--cpu-paths", type=int, default=8192, help="paths of the smaller CPU-baseline sample")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--ncu-case", action="store_true",
+                    help="profiling case: one maturity (T=1), 2^18 paths, two requests, no timing")
+    args = ap.parse_args()
+    if args.ncu_case:
+        run_ncu_case()
+        return
+    line = run_reference(args) if args.impl == "reference" else run_engine(args)
+    if line:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -140,6 +140,8 @@ typedef struct myql_mc_config {
   int32_t scheme[2];  /* myql_scheme per variance factor (the Stepper's VolScheme1/2) */
   int32_t greek_mode; /* myql_greek_mode (the pricer's GreekMode template argument)   */
   uint64_t n_streams; /* xoshiro streams (0 = default 131072, capped at num_paths)    */
+  uint64_t stream_offset; /* index of the first stream: replicas or ranks that take
+                             disjoint stream ranges draw independent paths          */
 } myql_mc_config;
 
 typedef struct myql_mc_job {
@@ -180,6 +182,8 @@ typedef struct myql_mc_stats {
   uint32_t table_fallbacks;    /* NCI draws outside the chi-squared table        */
   uint32_t kernel_launches;    /* kernels launched by this call                  */
   double device_ms;            /* device time of the call (CUDA events)          */
+  double simulate_ms;          /* of which: path-simulation kernels              */
+  double payoff_ms;            /* of which: payoff / Greek reduction kernels     */
 } myql_mc_stats;
 
 /* --- context ------------------------------------------------------------- */
@@ -287,6 +291,12 @@ myql_status myql_chi2_quantile(myql_ctx *ctx, const double *dof, const double *p
  * of x.  out: n floats. */
 myql_status myql_probe_sampler(myql_ctx *ctx, int kind, const uint64_t *x,
                                const double *lambda, float *out, size_t n);
+
+/* Measured issue-rate ceilings of this GPU for the compute roofline of the
+ * path kernels: kind 0 = FP32 FMA lane operations per second, kind 1 = MUFU
+ * (special-function) operations per second.  Runs a short dependent-chain
+ * microbenchmark on every SM. */
+myql_status myql_probe_peak(myql_ctx *ctx, int kind, double *ops_per_second);
 
 #ifdef __cplusplus
 }

@@ -53,7 +53,7 @@ class McConfigC(C.Structure):
     _fields_ = [("num_paths", C.c_uint64), ("time_steps", C.c_uint64), ("seed", C.c_uint64),
                 ("fd_bump", C.c_double), ("vol_bump", C.c_double), ("t_bump", C.c_double),
                 ("r_bump", C.c_double), ("scheme", C.c_int32 * 2), ("greek_mode", C.c_int32),
-                ("n_streams", C.c_uint64)]
+                ("n_streams", C.c_uint64), ("stream_offset", C.c_uint64)]
 
 
 class McJobC(C.Structure):
@@ -64,7 +64,8 @@ class McJobC(C.Structure):
 class McStatsC(C.Structure):
     _fields_ = [("paths", C.c_uint64), ("path_steps", C.c_uint64), ("scenarios", C.c_uint32),
                 ("loop_cap_hits", C.c_uint32), ("table_fallbacks", C.c_uint32),
-                ("kernel_launches", C.c_uint32), ("device_ms", C.c_double)]
+                ("kernel_launches", C.c_uint32), ("device_ms", C.c_double),
+                ("simulate_ms", C.c_double), ("payoff_ms", C.c_double)]
 
 
 class MlmcConfigC(C.Structure):
@@ -114,6 +115,7 @@ _SIGS = {
                                      C.POINTER(C.c_double), C.c_size_t]),
     "myql_probe_sampler": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_uint64),
                                      C.POINTER(C.c_double), C.POINTER(C.c_float), C.c_size_t]),
+    "myql_probe_peak": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
 }
 
 _lib = None

@@ -32,6 +32,7 @@ cudaError_t launch_nci_build(double d, int rows, double *tmp_main, double *tmp_t
                              cudaStream_t stream);
 cudaError_t launch_chi2_probe(const double *dof, const double *p, double *out, size_t n,
                               cudaStream_t stream);
+cudaError_t run_peak_probe(int kind, int sm_count, cudaStream_t stream, double *ops_per_s);
 cudaError_t launch_sampler_probe(int kind, const unsigned long long *x, const double *lam,
                                  float *out, size_t n, unsigned int cap, unsigned int *status,
                                  cudaStream_t stream);
@@ -506,16 +507,18 @@ static myql_status ctx_check(myql_ctx *ctx) {
 
 namespace myql {
 
-// Stream states of (seed, first = 0, n) in ctx->st_cached; copied to st_work.
-myql_status ensure_streams(CtxBase *ctx, uint64_t seed, uint64_t n) {
-  if (!(ctx->st_valid && ctx->st_seed == seed && ctx->st_n == n)) {
+// Stream states of (seed, first, n) in ctx->st_cached (kept for the next call
+// with the same seed and range); copied to st_work, which the kernels advance.
+myql_status ensure_streams(CtxBase *ctx, uint64_t seed, uint64_t first, uint64_t n) {
+  if (!(ctx->st_valid && ctx->st_seed == seed && ctx->st_first == first && ctx->st_n == n)) {
     cudaError_t e = ctx->st_cached.ensure(n * 32);
     if (e != cudaSuccess) return cuda_status(e, "stream table");
-    e = launch_seed_streams(seed, 0, n, (unsigned long long *)ctx->st_cached.p, ctx->stream);
+    e = launch_seed_streams(seed, first, n, (unsigned long long *)ctx->st_cached.p, ctx->stream);
     if (e != cudaSuccess) return cuda_status(e, "seed_streams launch");
     ctx->launches++;
     ctx->st_valid = true;
     ctx->st_seed = seed;
+    ctx->st_first = first;
     ctx->st_n = n;
   }
   cudaError_t e = ctx->st_work.ensure(n * 32);
@@ -585,7 +588,7 @@ myql_status run_plan(CtxBase *ctx, const myql_mc_job &job, Plan &pl, double *out
   cudaStream_t st = ctx->stream;
   SimParams &P = pl.sim;
   PayoffParams &Q = pl.pay;
-  myql_status s = ensure_streams(ctx, job.config.seed, pl.S);
+  myql_status s = ensure_streams(ctx, job.config.seed, job.config.stream_offset, pl.S);
   if (s != MYQL_OK) return s;
   P.states = (unsigned long long *)ctx->st_work.p;
   P.loop_cap = ctx->loop_cap;
@@ -633,14 +636,22 @@ myql_status run_plan(CtxBase *ctx, const myql_mc_job &job, Plan &pl, double *out
     P.path_begin = b;
     P.path_end = en;
     P.rec_offset = b;
+    cudaEvent_t sa = ctx->phase_event(), sb = ctx->phase_event();
+    cudaEventRecord(sa, st);
     e = launch_simulate(P, pl.s1, pl.s2, pl.path_dep, st);
+    cudaEventRecord(sb, st);
+    ctx->ev_tags.push_back(0);
     if (e != cudaSuccess) return cuda_status(e, "simulate launch");
     ctx->launches++;
     if (keep_records) continue;
     Q.n_paths = en - b;
     Q.tile0 = tiles_done;
     const uint64_t nt = (en - b + tile - 1) / tile;
+    cudaEvent_t pa = ctx->phase_event(), pb = ctx->phase_event();
+    cudaEventRecord(pa, st);
     e = launch_payoff(Q, nt, st);
+    cudaEventRecord(pb, st);
+    ctx->ev_tags.push_back(1);
     if (e != cudaSuccess) return cuda_status(e, "payoff launch");
     ctx->launches++;
     tiles_done += nt;
@@ -658,6 +669,16 @@ myql_status run_plan(CtxBase *ctx, const myql_mc_job &job, Plan &pl, double *out
   if (e != cudaSuccess) return cuda_status(e, "finalize launch");
   ctx->launches++;
   return MYQL_OK;
+}
+
+// Sums the event-timed phases of the last call (after the stream has completed).
+void phase_times(CtxBase *ctx, double *sim_ms, double *pay_ms) {
+  *sim_ms = *pay_ms = 0.0;
+  for (size_t i = 0; i < ctx->ev_tags.size(); ++i) {
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, ctx->ev_pool[2 * i], ctx->ev_pool[2 * i + 1]) == cudaSuccess)
+      (ctx->ev_tags[i] == 0 ? *sim_ms : *pay_ms) += ms;
+  }
 }
 
 myql_status read_status(CtxBase *ctx, myql_mc_stats *stats) {
@@ -771,6 +792,7 @@ myql_status myql_mc_price(myql_ctx *ctx, const myql_mc_job *job, double *out,
   cudaError_t e = ctx->out.ensure(nout * sizeof(double));
   if (e != cudaSuccess) return cuda_status(e, "output buffer");
   ctx->launches = 0;
+  ctx->phase_reset();
   e = cudaEventRecord(ctx->ev0, ctx->stream);
   if (e != cudaSuccess) return cuda_status(e, "event");
   s = run_plan(ctx, *job, pl, (double *)ctx->out.p, false);
@@ -790,6 +812,7 @@ myql_status myql_mc_price(myql_ctx *ctx, const myql_mc_job *job, double *out,
   st->scenarios = (uint32_t)pl.n_sc;
   st->path_steps = pl.M * (uint64_t)pl.n_sc * (uint64_t)pl.steps;
   st->kernel_launches = ctx->launches;
+  phase_times(ctx, &st->simulate_ms, &st->payoff_ms);
   return read_status(ctx, st);
 }
 
@@ -807,6 +830,7 @@ myql_status myql_mc_price_async(myql_ctx *ctx, const myql_mc_job *job, double *o
   cudaStream_t own = ctx->stream;
   if (user) ctx->stream = user;
   ctx->launches = 0;
+  ctx->phase_reset();
   s = run_plan(ctx, *job, pl, out_dev, false);
   ctx->stream = own;
   return s;
@@ -829,6 +853,7 @@ myql_status myql_mc_paths(myql_ctx *ctx, const myql_mc_job *job, float *records,
   if (records_len < need)
     return set_error(MYQL_ERR_INVALID_ARG, "records buffer holds %zu floats, need %zu", records_len, need);
   ctx->launches = 0;
+  ctx->phase_reset();
   s = run_plan(ctx, *job, pl, nullptr, true);
   if (s != MYQL_OK) return s;
   cudaError_t e = cudaMemcpyAsync(records, ctx->records.p, need * sizeof(float),
@@ -913,6 +938,13 @@ myql_status myql_probe_sampler(myql_ctx *ctx, int kind, const uint64_t *x, const
   if (e == cudaSuccess) e = cudaMemcpyAsync(out, ctx->probe_c.p, n * 4, cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   return cuda_status(e, "sampler probe");
+}
+
+myql_status myql_probe_peak(myql_ctx *ctx, int kind, double *ops_per_second) {
+  myql_status s = ctx_check(ctx);
+  if (s != MYQL_OK) return s;
+  if (!ops_per_second || kind < 0 || kind > 1) return set_error(MYQL_ERR_INVALID_ARG, "bad peak probe arguments");
+  return cuda_status(run_peak_probe(kind, ctx->sm_count, ctx->stream, ops_per_second), "peak probe");
 }
 
 }  // extern "C"

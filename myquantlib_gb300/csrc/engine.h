@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <map>
 #include <string>
+#include <vector>
 
 #include "engine_types.h"
 #include "myql_gpu.h"
@@ -42,13 +43,28 @@ struct CtxBase {
   uint64_t records_cap_bytes = 2ull << 30;  // per-path record scratch per chunk
   // xoshiro stream-state table of the last (seed, n)
   bool st_valid = false;
-  uint64_t st_seed = 0, st_n = 0;
+  uint64_t st_seed = 0, st_first = 0, st_n = 0;
   DevBuf st_cached, st_work;
   std::map<uint64_t, NciEntry> nci;  // keyed by the bits of d = 4 kappa theta / sigma^2
   DevBuf records, partials, out, status, strikes;
   DevBuf probe_a, probe_b, probe_c;
   DevBuf aux_a, aux_b, aux_c, aux_d;  // batch / MLMC / control-variate work buffers
+  // event pairs around the phase launches of the current call (tag 0 = simulate, 1 = payoff)
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<int> ev_tags;
+  size_t ev_used = 0;
+  void phase_reset() { ev_used = 0; ev_tags.clear(); }
+  cudaEvent_t phase_event() {
+    if (ev_used == ev_pool.size()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      ev_pool.push_back(e);
+    }
+    return ev_pool[ev_used++];
+  }
   void release_all() {
+    for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
+    ev_pool.clear();
     st_cached.release();
     st_work.release();
     nci.clear();

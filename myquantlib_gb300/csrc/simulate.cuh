@@ -144,8 +144,8 @@ __device__ __forceinline__ void sim_path(const SimParams &P, const ScenarioConst
         const float van = evolve<S1>(va, rng, f0, P, 0, caphits, fallbacks);
         const float vbn = evolve<S2>(vb, rng, f1, P, 1, caphits, fallbacks);
         const float root = sqrt_approx(fmaf(f0.C3, va + van, f1.C3 * (vb + vbn)));
-        const float drift =
-            fmaf(f1.C2, vbn, fmaf(f1.C1, vb, fmaf(f0.C2, van, fmaf(f0.C1, va, f0.C0))));
+        const float drift = fmaf(f1.C2, vbn, fmaf(f1.C1, vb, fmaf(f0.C2, van,
+                                 fmaf(f0.C1, va, f0.C0 + f1.C0))));
         X += fmaf(root, G, drift);
         va = van;
         vb = vbn;

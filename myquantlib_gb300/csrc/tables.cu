@@ -4,6 +4,8 @@
 #include "device_numerics.cuh"
 #include "engine_types.h"
 
+#include <algorithm>
+
 namespace myql {
 
 __constant__ unsigned long long c_jump[64][4];
@@ -226,4 +228,75 @@ cudaError_t launch_sampler_probe(int kind, const unsigned long long *x, const do
   return cudaGetLastError();
 }
 
+}  // namespace myql
+
+// ---- issue-rate ceilings (compute roofline denominators) -------------------
+namespace myql {
+namespace dev {
+constexpr int kPeakIters = 4096;
+
+// 8 independent FMA chains per thread: the FP32 pipe's sustained lane rate.
+__global__ void __launch_bounds__(256) fma_peak_kernel(float *sink, float seed) {
+  float a0 = seed + threadIdx.x, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3;
+  float a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6, a7 = a0 + 7;
+  const float m = 0.999999f, c = 1e-7f;
+#pragma unroll 16
+  for (int i = 0; i < kPeakIters; ++i) {
+    a0 = fmaf(a0, m, c); a1 = fmaf(a1, m, c); a2 = fmaf(a2, m, c); a3 = fmaf(a3, m, c);
+    a4 = fmaf(a4, m, c); a5 = fmaf(a5, m, c); a6 = fmaf(a6, m, c); a7 = fmaf(a7, m, c);
+  }
+  const float s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  if (s == 12345.678f) sink[blockIdx.x] = s;
+}
+
+// 8 independent ex2.approx chains per thread: the MUFU rate.
+__global__ void __launch_bounds__(256) mufu_peak_kernel(float *sink, float seed) {
+  float a[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) a[j] = -1e-3f * (seed + threadIdx.x + j);
+#pragma unroll 8
+  for (int i = 0; i < kPeakIters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      float r;
+      asm volatile("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a[j]));
+      a[j] = -r;
+    }
+  }
+  float s = 0.0f;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s += a[j];
+  if (s == 12345.678f) sink[blockIdx.x] = s;
+}
+}  // namespace dev
+
+cudaError_t run_peak_probe(int kind, int sm_count, cudaStream_t stream, double *ops_per_s) {
+  float *sink = nullptr;
+  cudaEvent_t e0, e1;
+  cudaError_t e = cudaMalloc(&sink, 65536 * sizeof(float));
+  if (e != cudaSuccess) return e;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int blocks = sm_count * 8;
+  double best = 0.0;
+  for (int rep = 0; rep < 4 && e == cudaSuccess; ++rep) {
+    cudaEventRecord(e0, stream);
+    if (kind == 0)
+      dev::fma_peak_kernel<<<blocks, 256, 0, stream>>>(sink, 1.0f + rep);
+    else
+      dev::mufu_peak_kernel<<<blocks, 256, 0, stream>>>(sink, 1.0f + rep);
+    cudaEventRecord(e1, stream);
+    e = cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const double ops = (double)blocks * 256.0 * dev::kPeakIters * 8.0;
+    if (rep > 0 && ms > 0.0f) best = std::max(best, ops / (ms * 1e-3));
+  }
+  if (e == cudaSuccess) e = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(sink);
+  *ops_per_s = best;
+  return e;
+}
 }  // namespace myql

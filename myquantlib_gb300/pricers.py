@@ -380,6 +380,7 @@ class MonteCarloConfig:  # MonteCarloPricer.hpp:16-26
     t_bump: float = 1e-4
     r_bump: float = 1e-4
     n_streams: int = 0  # xoshiro streams (0 = engine default)
+    stream_offset: int = 0  # first stream index (disjoint ranges = independent replicas)
 
 
 @dataclass
@@ -462,6 +463,12 @@ class Engine:
         _abi.check(self.lib.myql_rng_draws(self.handle, seed, first, n, count,
                                            out.ctypes.data_as(C.POINTER(C.c_uint64))))
         return out.reshape(n, count)
+
+    def peak(self, kind: int) -> float:
+        """Measured FP32-FMA (kind 0) or MUFU (kind 1) operations per second."""
+        v = C.c_double()
+        _abi.check(self.lib.myql_probe_peak(self.handle, kind, C.byref(v)))
+        return v.value
 
     def chi2_quantile(self, dof, p) -> np.ndarray:
         dof = np.ascontiguousarray(dof, dtype=np.float64)
@@ -580,6 +587,7 @@ def make_job(model, stepper: ASVJStepper | None, instrument: _Instrument, mode: 
     c.scheme[1] = stepper.VolScheme2.code
     c.greek_mode = int(mode)
     c.n_streams = cfg.n_streams
+    c.stream_offset = cfg.stream_offset
     job.S0, job.r, job.q = S0, r, q
     return _Job(job, strikes)
 

@@ -34,8 +34,8 @@ static inline double oracle_norm_inv(double p) {
   static const double d[4] = {7.784695709041462e-03, 3.224671290700398e-01,
                               2.445134137142996e+00, 3.754408661907416e+00};
   double x;
-  if (p <= 0.0) return -INFINITY;
-  if (p >= 1.0) return INFINITY;
+  if (p <= 0.0) return -40.0;
+  if (p >= 1.0) return 40.0;
   if (p > 0.02425 && p < 0.97575) {
     const double q = p - 0.5, r = q * q;
     x = (((((a[0] * r + a[1]) * r + a[2]) * r + a[3]) * r + a[4]) * r + a[5]) * q /
@@ -100,8 +100,8 @@ static inline oracle_gamma_eval oracle_gamma(double a, double x, double lga) {
 /* Quantile of chi-squared(nu) at lower-tail probability p (upper == 0) or
  * upper-tail probability p (upper != 0). */
 static inline double oracle_chi2_quantile_tail(double nu, double p, int upper) {
-  if (p <= 0.0) return upper ? INFINITY : 0.0;
-  if (p >= 1.0) return upper ? 0.0 : INFINITY;
+  if (p <= 0.0) return upper ? 1e300 : 0.0;
+  if (p >= 1.0) return upper ? 0.0 : 1e300;
   const double a = 0.5 * nu, lga = lgamma(a), lp = log(p);
   const double z = upper ? -oracle_norm_inv(p) : oracle_norm_inv(p);
   const double h = 1.0 / (9.0 * a);
@@ -114,10 +114,13 @@ static inline double oracle_chi2_quantile_tail(double nu, double p, int upper) {
   } else {
     u = upper ? log(a + 1.0) : u_small;
   }
-  double lo = -INFINITY, hi = INFINITY;
+  /* bracket kept with flags (not infinities), so the iteration is also exact
+     when compiled with -ffast-math */
+  double lo = 0.0, hi = 0.0;
+  int have_lo = 0, have_hi = 0;
   for (int it = 0; it < 300; ++it) {
     const double x = exp(u);
-    if (x <= 0.0) return 0.0;
+    if (!(x > 0.0)) return 0.0;
     const oracle_gamma_eval g = oracle_gamma(a, x, lga);
     double G, dG;
     if (!upper) {
@@ -127,11 +130,18 @@ static inline double oracle_chi2_quantile_tail(double nu, double p, int upper) {
       G = lp - g.logQ;
       dG = g.xpdf_Q;
     }
-    if (G < 0.0) lo = u; else hi = u;
+    if (G < 0.0) {
+      lo = u;
+      have_lo = 1;
+    } else {
+      hi = u;
+      have_hi = 1;
+    }
     double un = u - G / dG;
-    if (!(un > lo && un < hi)) {
-      if (isinf(lo)) un = u - 2.0;
-      else if (isinf(hi)) un = u + 2.0;
+    const int inside = (!have_lo || un > lo) && (!have_hi || un < hi) && un == un;
+    if (!inside) {
+      if (!have_lo) un = u - 2.0;
+      else if (!have_hi) un = u + 2.0;
       else un = 0.5 * (lo + hi);
     }
     if (fabs(un - u) < 1e-14 * fmax(1.0, fabs(u))) {

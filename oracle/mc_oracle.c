@@ -915,14 +915,16 @@ static void plan_build(plan_t *P, const myql_mc_job *job, nci_ws nci[MAXSC][2]) 
   }
   P->n_sc = n;
   for (int s = 0; s < n; ++s) {
+    /* the rho steppers reuse the base workspace (MonteCarloPricer.hpp:294-295) */
+    const int rho_sc = s == 5 || s == 6;
     for (int f = 0; f < P->nf; ++f)
-      if (c->scheme[f] == MYQL_SCHEME_NCI) {
+      if (c->scheme[f] == MYQL_SCHEME_NCI && !rho_sc) {
         myql_heston_params hp = m->heston[f];
         hp.v0 = v0[s][f];
         nci_build(&nci[s][f], &hp, dts[s]);
       }
     P->st[s].path_dep = pd;
-    stepper_init(&P->st[s], job, vol[s], v0[s], dts[s], rs[s], Ts[s], nci[s]);
+    stepper_init(&P->st[s], job, vol[s], v0[s], dts[s], rs[s], Ts[s], rho_sc ? nci[0] : nci[s]);
     P->st[s].path_dep = pd;
     stepper_jumps(&P->st[s], m, pd ? dts[s] : Ts[s]);
   }

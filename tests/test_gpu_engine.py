@@ -74,7 +74,7 @@ def test_device_chi2_quantile(engine):
 
 
 def base_spec():
-    return jobspec.with_config(MC_SPECS["c1_heston_nv_call"], paths=50000, steps=50)
+    return jobspec.with_config(MC_SPECS["c1_heston_nv_call"], paths=50000, steps=50, streams=1024)
 
 
 def test_deterministic_and_chunking_invariant(engine):
@@ -108,8 +108,9 @@ def test_large_strip(engine, oracle_lib):
     job = jobspec.make_job(spec)
     raw, _ = engine.price(job)
     want, _ = oracle_lib.mc_price(job, oracle_lib.LAYOUT_STREAMS, 8)
-    se = np.maximum(raw[1::2], 1e-12)
-    assert np.max(np.abs(raw[0::2] - want[0::2]) / se) < 0.35
+    se = np.maximum(raw[1::2], want[1::2])
+    floor = 1e-7 * float(np.max(np.abs(want[0])))
+    assert np.all(np.abs(raw[0::2] - want[0::2]) <= 0.35 * se + floor)
 
 
 def test_day0_barrier_breach_prices_zero(engine):

@@ -89,20 +89,7 @@ static void compute_polys() {
   std::memcpy(g_polys, tmp, sizeof tmp);
 }
 
-// ---------------------------------------------------------------------------
-// Job planning: everything the launches need, computed in FP64 on the host.
-struct Plan {
-  int nf = 0, s1 = 0, s2 = 0, tracker = 0, n_fields = 1, n_sc = 1, mode = 0;
-  bool path_dep = false;
-  uint64_t M = 0, S = 0;
-  int steps = 0;
-  double T = 0, df = 1;
-  SimParams sim;
-  PayoffParams pay;
-  int active_mask = 1;
-};
-
-static int tracker_of(const myql_instrument &in) {
+int tracker_of(const myql_instrument &in) {
   switch (in.kind) {
     case MYQL_INSTR_EUROPEAN: return TRK_EUROPEAN;
     case MYQL_INSTR_ASIAN_GEO: return TRK_GEO_ASIAN;
@@ -188,13 +175,13 @@ myql_status validate_job(const myql_mc_job &job) {
   return MYQL_OK;
 }
 
-static double expected_avg_variance(const myql_heston_params &h, double T) {
+double expected_avg_variance(const myql_heston_params &h, double T) {
   if (std::fabs(h.kappa * T) > 1e-8)
     return h.theta + (h.v0 - h.theta) * (1.0 - std::exp(-h.kappa * T)) / (h.kappa * T);
   return h.v0;
 }
 
-static double jump_variance(const myql_model &m) {
+double jump_variance(const myql_model &m) {
   if (m.jump == MYQL_JUMP_MERTON)
     return m.jump_lambda * (m.merton_mu * m.merton_mu + m.merton_delta * m.merton_delta);
   if (m.jump == MYQL_JUMP_KOU)
@@ -210,7 +197,7 @@ struct ScDef {
   double dt, T, r;
 };
 
-static void fill_factor(FactorConst &fc, const myql_heston_params &h, double v0, int scheme,
+void fill_factor(FactorConst &fc, const myql_heston_params &h, double v0, int scheme,
                         double r_part, double dt) {
   const double k = h.kappa, th = h.theta, s = h.sigma, rho = h.rho;
   fc.v0 = (float)v0;
@@ -255,7 +242,7 @@ static int nci_nmax_ref(const myql_heston_params &p, double dt) {
 // Rows to tabulate: the reference's n_max, extended so that Poisson indices
 // reached from variances far in the CIR tail (stationary Gamma quantile near
 // 1 - 1e-8, or v0 if larger) are looked up rather than approximated.
-static int nci_rows_wanted(const myql_heston_params &p, double dt_min) {
+int nci_rows_wanted(const myql_heston_params &p, double dt_min) {
   const double shape = 2.0 * p.kappa * p.theta / (p.sigma * p.sigma);
   const double scale = p.sigma * p.sigma / (2.0 * p.kappa);
   const double v_hi = std::max(2.0 * p.v0, scale * (shape + 6.0 * std::sqrt(shape) + 25.0));
@@ -267,7 +254,7 @@ static int nci_rows_wanted(const myql_heston_params &p, double dt_min) {
   return (int)std::min(rows, 1024.0);
 }
 
-static unsigned long long u999_threshold() {
+unsigned long long u999_threshold() {
   // smallest x with double(x) * 2^-64 >= 0.999
   const double lim = kNciUmax * 18446744073709551616.0;
   unsigned long long x = (unsigned long long)lim;

@@ -86,4 +86,31 @@ struct CtxBase {
 myql_status set_error(myql_status st, const char *fmt, ...);
 myql_status cuda_status(cudaError_t e, const char *what);
 
+// Job planning: everything the launches need, computed in FP64 on the host.
+struct Plan {
+  int nf = 0, s1 = 0, s2 = 0, tracker = 0, n_fields = 1, n_sc = 1, mode = 0;
+  bool path_dep = false;
+  uint64_t M = 0, S = 0;
+  int steps = 0;
+  double T = 0, df = 1;
+  SimParams sim;
+  PayoffParams pay;
+  int active_mask = 1;
+};
+
+
+// planning helpers (engine.cu)
+int tracker_of(const myql_instrument &in);
+myql_status validate_job(const myql_mc_job &job);
+myql_status make_plan(const myql_mc_job &job, Plan &pl);
+void fill_factor(FactorConst &fc, const myql_heston_params &h, double v0, int scheme, double r_part,
+                 double dt);
+unsigned long long u999_threshold();
+double expected_avg_variance(const myql_heston_params &h, double T);
+double jump_variance(const myql_model &m);
+int nci_rows_wanted(const myql_heston_params &p, double dt_min);
+myql_status ensure_streams(CtxBase *ctx, uint64_t seed, uint64_t first, uint64_t n);
+myql_status ensure_nci(CtxBase *ctx, const myql_heston_params &p, double dt_min, NciTable &tab);
+myql_status read_status(CtxBase *ctx, myql_mc_stats *stats);
+
 }  // namespace myql

@@ -1123,3 +1123,442 @@ double myql_oracle_chi2_quantile(double nu, double p) { return oracle_chi2_quant
 double myql_oracle_uniform_of(uint64_t x) {
   return (double)x * 5.421010862427522170037264e-20;
 }
+
+/* ================================================================== MLMC
+ * Restatement of MultiLevelMonteCarloPricer::calculate / evaluate_level
+ * (pricers/mlmc/MultiLevelMonteCarloPricer.hpp:46-341) and
+ * CoupledASVJStepper::multi_step_coupled (models/asvj/core/CoupledASVJStepper.hpp:170-517).
+ */
+
+/* one fine/coarse pair of the coupled stepper; sf/sc prepared with dt_fine/dt_coarse */
+static void coupled_path(const stepper_t *sf, const stepper_t *sc, int trk, const tcfg_t *c, double S0,
+                         int n_coarse, xo_t *r, state_t *stf, state_t *stc) {
+  memset(stf, 0, sizeof *stf);
+  memset(stc, 0, sizeof *stc);
+  const double lS0 = log(S0);
+  const double dtf = sf->dt, dtc = sc->dt;
+  /* start_path for both (tracker init with their own dt) */
+  state_t *sts[2] = {stf, stc};
+  const double dts[2] = {dtf, dtc};
+  for (int w = 0; w < 2; ++w) {
+    state_t *st = sts[w];
+    st->logS = lS0;
+    switch (trk) {
+      case TRK_GEO: st->sumLogS = c->past_avg_log * c->t_elapsed + 0.5 * st->logS * dts[w]; break;
+      case TRK_ARITH:
+        st->sumLogS = c->past_avg_log * c->t_elapsed + 0.5 * st->logS * dts[w];
+        st->sumS = c->past_avg_S * c->t_elapsed + 0.5 * exp(st->logS) * dts[w];
+        break;
+      case TRK_LB:
+        st->minLogS = (c->hist_min_logS < 1e300) ? c->hist_min_logS : st->logS;
+        st->maxLogS = (c->hist_max_logS > -1e300) ? c->hist_max_logS : st->logS;
+        break;
+      case TRK_BUP:
+        if (st->logS >= c->b_base) st->hit_base = 1;
+        if (st->logS >= c->b_up) st->hit_up = 1;
+        if (st->logS >= c->b_dn) st->hit_dn = 1;
+        break;
+      case TRK_BDN:
+        if (st->logS <= c->b_base) st->hit_base = 1;
+        if (st->logS <= c->b_up) st->hit_up = 1;
+        if (st->logS <= c->b_dn) st->hit_dn = 1;
+        break;
+      default: break;
+    }
+  }
+  const int pd = trk != TRK_EUR;
+  const int nf = sf->nf;
+  double lf = lS0, lc = lS0;
+  const double total_time = n_coarse * (2.0 * dtf);
+  if (nf == 0 && !pd) {
+    const double G = normcdfinv_as241(uni(r));
+    lf += sf->gbm_drift_dt * (n_coarse * 2) + sf->gbm_vol_dt * sqrt((double)(n_coarse * 2)) * G;
+    lc += sc->gbm_drift_dt * n_coarse + sc->gbm_vol_dt * sqrt((double)n_coarse) * G;
+    const double J = log_jump(sf, r);
+    lf += J;
+    lc += J;
+  } else {
+    if (!pd && nf > 0) {
+      const double J = log_jump(sf, r);
+      lf += J;
+      lc += J;
+    }
+    double vf[2] = {nf >= 1 ? sf->f[0].v0 : 0.0, nf >= 2 ? sf->f[1].v0 : 0.0};
+    double vc[2] = {nf >= 1 ? sc->f[0].v0 : 0.0, nf >= 2 ? sc->f[1].v0 : 0.0};
+    for (int k = 0; k < n_coarse; ++k) {
+      const double G1 = normcdfinv_as241(uni(r));
+      const double G2 = normcdfinv_as241(uni(r));
+      double Gc = (G1 + G2) / 1.4142135623730951;
+      double j1 = 0.0, j2 = 0.0;
+      if (nf == 0) {
+        Gc = (G1 + G2) / 1.4142135623730951;
+        lc += sc->gbm_drift_dt + sc->gbm_vol_dt * Gc;
+        lf += sf->gbm_drift_dt + sf->gbm_vol_dt * G1;
+        if (pd) {
+          j1 = log_jump(sf, r);
+          lf += j1;
+        }
+        stf->logS = lf;
+        if (pd) tracker_update(stf, trk, c, dtf);
+        lf += sf->gbm_drift_dt + sf->gbm_vol_dt * G2;
+        if (pd) {
+          j2 = log_jump(sf, r);
+          lf += j2;
+        }
+        stf->logS = lf;
+        if (pd) {
+          tracker_update(stf, trk, c, dtf);
+          lc += j1 + j2;
+          stc->logS = lc;
+          tracker_update(stc, trk, c, dtc);
+        }
+      } else {
+        double Z1[2] = {0.0, 0.0}, Z2[2] = {0.0, 0.0}, mid[2] = {0.0, 0.0}, nxt[2] = {0.0, 0.0};
+        for (int i = 0; i < nf; ++i) {
+          if (sf->f[i].scheme == MYQL_SCHEME_NV) {
+            Z1[i] = normcdfinv_as241(uni(r));
+            const double root = sqrt(sf->f[i].W[0] * vf[i] + sf->f[i].W[1]) + sf->f[i].W[2] * Z1[i];
+            mid[i] = sf->f[i].W[0] * (root * root) + sf->f[i].W[1];
+          } else {
+            mid[i] = evolve(&sf->f[i], vf[i], r);
+          }
+        }
+        double r1;
+        if (nf == 1) {
+          const double *C = sf->f[0].C;
+          r1 = sqrt(C[3] * (vf[0] + mid[0]));
+          lf += C[0] + C[1] * vf[0] + C[2] * mid[0] + r1 * G1;
+        } else {
+          const double *Ca = sf->f[0].C, *Cb = sf->f[1].C;
+          r1 = sqrt(Ca[3] * (vf[0] + mid[0]) + Cb[3] * (vf[1] + mid[1]));
+          lf += Ca[0] + Ca[1] * vf[0] + Ca[2] * mid[0] + Cb[0] + Cb[1] * vf[1] + Cb[2] * mid[1] + r1 * G1;
+        }
+        if (pd) {
+          j1 = log_jump(sf, r);
+          lf += j1;
+        }
+        stf->logS = lf;
+        if (pd) tracker_update(stf, trk, c, dtf);
+        for (int i = 0; i < nf; ++i) {
+          if (sf->f[i].scheme == MYQL_SCHEME_NV) {
+            Z2[i] = normcdfinv_as241(uni(r));
+            const double root = sqrt(sf->f[i].W[0] * mid[i] + sf->f[i].W[1]) + sf->f[i].W[2] * Z2[i];
+            nxt[i] = sf->f[i].W[0] * (root * root) + sf->f[i].W[1];
+          } else {
+            nxt[i] = evolve(&sf->f[i], mid[i], r);
+          }
+        }
+        double r2;
+        if (nf == 1) {
+          const double *C = sf->f[0].C;
+          r2 = sqrt(C[3] * (mid[0] + nxt[0]));
+          lf += C[0] + C[1] * mid[0] + C[2] * nxt[0] + r2 * G2;
+        } else {
+          const double *Ca = sf->f[0].C, *Cb = sf->f[1].C;
+          r2 = sqrt(Ca[3] * (mid[0] + nxt[0]) + Cb[3] * (mid[1] + nxt[1]));
+          lf += Ca[0] + Ca[1] * mid[0] + Ca[2] * nxt[0] + Cb[0] + Cb[1] * mid[1] + Cb[2] * nxt[1] + r2 * G2;
+        }
+        if (pd) {
+          j2 = log_jump(sf, r);
+          lf += j2;
+        }
+        stf->logS = lf;
+        if (pd) tracker_update(stf, trk, c, dtf);
+        double cn[2] = {0.0, 0.0};
+        for (int i = 0; i < nf; ++i) {
+          if (sc->f[i].scheme == MYQL_SCHEME_NV) {
+            const double Zc = (Z1[i] + Z2[i]) / 1.4142135623730951;
+            const double root = sqrt(sc->f[i].W[0] * vc[i] + sc->f[i].W[1]) + sc->f[i].W[2] * Zc;
+            cn[i] = sc->f[i].W[0] * (root * root) + sc->f[i].W[1];
+          } else {
+            cn[i] = nxt[i];
+          }
+        }
+        if (r1 + r2 > 1e-15) Gc = (r1 * G1 + r2 * G2) / hypot(r1, r2);
+        if (nf == 1) {
+          const double *C = sc->f[0].C;
+          const double rc = sqrt(C[3] * (vc[0] + cn[0]));
+          lc += C[0] + C[1] * vc[0] + C[2] * cn[0] + rc * Gc;
+        } else {
+          const double *Ca = sc->f[0].C, *Cb = sc->f[1].C;
+          const double rc = sqrt(Ca[3] * (vc[0] + cn[0]) + Cb[3] * (vc[1] + cn[1]));
+          lc += Ca[0] + Ca[1] * vc[0] + Ca[2] * cn[0] + Cb[0] + Cb[1] * vc[1] + Cb[2] * cn[1] + rc * Gc;
+        }
+        for (int i = 0; i < nf; ++i) {
+          vf[i] = nxt[i];
+          vc[i] = cn[i];
+        }
+        if (pd) {
+          lc += j1 + j2;
+          stc->logS = lc;
+          tracker_update(stc, trk, c, dtc);
+        }
+      }
+      if (!pd) stc->logS = lc;
+    }
+  }
+  /* finalize both */
+  for (int w = 0; w < 2; ++w) {
+    state_t *st = sts[w];
+    st->logS = w == 0 ? lf : lc;
+    switch (trk) {
+      case TRK_GEO:
+        st->sumLogS -= 0.5 * st->logS * dts[w];
+        st->sumLogS = exp(st->sumLogS / (total_time + c->t_elapsed));
+        break;
+      case TRK_ARITH:
+        st->sumLogS -= 0.5 * st->logS * dts[w];
+        st->sumS -= 0.5 * exp(st->logS) * dts[w];
+        st->sumLogS = exp(st->sumLogS / (total_time + c->t_elapsed));
+        st->sumS = st->sumS / (total_time + c->t_elapsed);
+        break;
+      case TRK_LB:
+        st->minLogS = exp(st->minLogS);
+        st->maxLogS = exp(st->maxLogS);
+        break;
+      default: break;
+    }
+    st->logS = exp(st->logS);
+  }
+}
+
+/* one stepper of the job at step dt (total_time = T) */
+static void make_stepper(stepper_t *s, const myql_mc_job *job, int pd, double dt, double T, nci_ws nci[2]) {
+  const double v0[2] = {job->model.heston[0].v0, job->model.heston[1].v0};
+  stepper_init(s, job, job->model.vol, v0, dt, job->r, T, nci);
+  s->path_dep = pd;
+  stepper_jumps(s, &job->model, pd ? dt : T);
+}
+
+typedef struct {
+  int layout, n_threads;
+  uint64_t S;          /* streams layout: pool size */
+  xo_t *pool;          /* n_threads (reference) or S (streams) persistent states */
+} mlmc_rng;
+
+/* evaluate_level: adds sum and sum of squares of P_fine - P_coarse over dN paths */
+static void mlmc_eval(const plan_t *P, const myql_mc_job *job, uint64_t base_steps, int l, uint64_t dN,
+                      mlmc_rng *R, double *sum, double *sum_sq) {
+  const double T = P->T;
+  const int pd = P->trk != TRK_EUR;
+  nci_ws nci[2];
+  memset(nci, 0, sizeof nci);
+  stepper_t sf, sc;
+  int n_coarse;
+  if (l == 0) {
+    const double dt = T / (double)base_steps;
+    for (int f = 0; f < P->nf; ++f)
+      if (job->config.scheme[f] == MYQL_SCHEME_NCI) nci_build(&nci[f], &job->model.heston[f], dt);
+    make_stepper(&sf, job, pd, dt, T, nci);
+    sf.n_steps = (int)base_steps;
+    n_coarse = (int)base_steps;
+  } else {
+    const uint64_t fine = base_steps * (1ull << l);
+    const double dtf = T / (double)fine;
+    for (int f = 0; f < P->nf; ++f)
+      if (job->config.scheme[f] == MYQL_SCHEME_NCI) nci_build(&nci[f], &job->model.heston[f], dtf);
+    make_stepper(&sf, job, pd, dtf, T, nci);
+    make_stepper(&sc, job, pd, dtf * 2.0, T, nci);
+    n_coarse = (int)(fine / 2);
+  }
+  const double K = job->instrument.strikes[0];
+  const int T_threads = R->layout == MYQL_ORACLE_LAYOUT_REFERENCE ? R->n_threads : R->n_threads;
+  double *ts = (double *)calloc((size_t)T_threads, sizeof(double));
+  double *tq = (double *)calloc((size_t)T_threads, sizeof(double));
+  if (R->layout == MYQL_ORACLE_LAYOUT_REFERENCE) {
+#pragma omp parallel num_threads(R->n_threads)
+    {
+#ifdef _OPENMP
+      const int tid = omp_get_thread_num(), nt = omp_get_num_threads();
+#else
+      const int tid = 0, nt = 1;
+#endif
+      xo_t *rng = &R->pool[tid];
+      const uint64_t q = dN / (uint64_t)nt, rem = dN % (uint64_t)nt;
+      const uint64_t b = (uint64_t)tid < rem ? (q + 1) * tid : q * tid + rem;
+      const uint64_t e = b + ((uint64_t)tid < rem ? q + 1 : q);
+      state_t a, c;
+      double pf[3], pc[3];
+      for (uint64_t i = b; i < e; ++i) {
+        double d;
+        if (l == 0) {
+          run_path(&sf, P->trk, &P->tcfg, P->S0, rng, &a);
+          payoff_triplet(&P->in, &a, P->S0, P->h, K, pf);
+          d = pf[0];
+        } else {
+          coupled_path(&sf, &sc, P->trk, &P->tcfg, P->S0, n_coarse, rng, &a, &c);
+          payoff_triplet(&P->in, &a, P->S0, P->h, K, pf);
+          payoff_triplet(&P->in, &c, P->S0, P->h, K, pc);
+          d = pf[0] - pc[0];
+        }
+        ts[tid] += d;
+        tq[tid] += d * d;
+      }
+    }
+  } else {
+    const uint64_t U = R->S < dN ? R->S : dN;
+#pragma omp parallel for schedule(static) num_threads(R->n_threads)
+    for (uint64_t s = 0; s < U; ++s) {
+#ifdef _OPENMP
+      const int tid = omp_get_thread_num();
+#else
+      const int tid = 0;
+#endif
+      xo_t *rng = &R->pool[s];
+      state_t a, c;
+      double pf[3], pc[3];
+      for (uint64_t i = s; i < dN; i += U) {
+        double d;
+        if (l == 0) {
+          run_path(&sf, P->trk, &P->tcfg, P->S0, rng, &a);
+          payoff_triplet(&P->in, &a, P->S0, P->h, K, pf);
+          d = pf[0];
+        } else {
+          coupled_path(&sf, &sc, P->trk, &P->tcfg, P->S0, n_coarse, rng, &a, &c);
+          payoff_triplet(&P->in, &a, P->S0, P->h, K, pf);
+          payoff_triplet(&P->in, &c, P->S0, P->h, K, pc);
+          d = pf[0] - pc[0];
+        }
+        ts[tid] += d;
+        tq[tid] += d * d;
+      }
+    }
+  }
+  for (int t = 0; t < T_threads; ++t) {
+    *sum += ts[t];
+    *sum_sq += tq[t];
+  }
+  free(ts);
+  free(tq);
+  for (int f = 0; f < 2; ++f) {
+    free(nci[f].y);
+    free(nci[f].m);
+  }
+}
+
+/* MultiLevelMonteCarloPricer::calculate; returns 0 */
+int myql_oracle_mlmc_price(const myql_mc_job *job_in, const myql_mlmc_config *cfg, int layout,
+                           int n_threads, myql_mlmc_result *res) {
+  if (!job_in || !cfg || !res || n_threads < 1) return -1;
+  myql_mc_job job = *job_in;
+  job.config.time_steps = cfg->base_steps;
+  job.config.fd_bump = cfg->fd_bump;
+  nci_ws nci_unused[MAXSC][2];
+  memset(nci_unused, 0, sizeof nci_unused);
+  /* the plan's tracker/payoff data (no NCI tables needed here: schemes set to NV temporarily) */
+  myql_mc_job jp = job;
+  jp.config.greek_mode = job.config.greek_mode;
+  int saved[2] = {jp.config.scheme[0], jp.config.scheme[1]};
+  jp.config.scheme[0] = jp.config.scheme[1] = MYQL_SCHEME_EXACT;
+  plan_t *P = (plan_t *)calloc(1, sizeof(plan_t));
+  plan_build(P, &jp, nci_unused);
+  (void)saved;
+  const double T = P->T, df = exp(-job.r * T);
+  const size_t L_max = cfg->L_max;
+  mlmc_rng R;
+  R.layout = layout;
+  R.n_threads = n_threads;
+  R.S = cfg->n_streams ? cfg->n_streams : 131072ull;
+  if (layout == MYQL_ORACLE_LAYOUT_REFERENCE) {
+    R.pool = (xo_t *)malloc(sizeof(xo_t) * n_threads);
+    for (int t = 0; t < n_threads; ++t) xo_seed(&R.pool[t], cfg->seed + (uint64_t)t * 999983ull);
+  } else {
+    R.pool = (xo_t *)malloc(sizeof(xo_t) * R.S);
+    xo_seed(&R.pool[0], cfg->seed);
+    for (uint64_t k = 1; k < R.S; ++k) {
+      R.pool[k] = R.pool[k - 1];
+      xo_jump(&R.pool[k]);
+    }
+  }
+  size_t L = cfg->L_min;
+  uint64_t N_l[32] = {0};
+  double sum_dP[32] = {0}, sum_sq_dP[32] = {0}, V_l[32] = {0}, cost_l[32] = {0};
+  for (size_t l = 0; l <= L_max; ++l) cost_l[l] = (double)(cfg->base_steps * (1ull << l));
+  double alpha = cfg->alpha, beta = cfg->beta;
+  int converged = 0;
+  while (!converged) {
+    for (size_t l = 0; l <= L; ++l) {
+      double sum_sqrt_VC_pilot = 0.0;
+      for (size_t k = 0; k <= L; ++k) sum_sqrt_VC_pilot += sqrt(V_l[k] * cost_l[k]);
+      uint64_t optimal_N = 0;
+      if (V_l[l] > 1e-18)
+        optimal_N = (uint64_t)ceil(2.0 * pow(cfg->epsilon, -2.0) * sqrt(V_l[l] / cost_l[l]) * sum_sqrt_VC_pilot);
+      uint64_t pilot_N = cfg->N0 / (1ull << l);
+      if (pilot_N < 20) pilot_N = 20;
+      const uint64_t target_N = pilot_N > optimal_N ? pilot_N : optimal_N;
+      if (N_l[l] < target_N) {
+        const uint64_t dN = target_N - N_l[l];
+        mlmc_eval(P, &job, cfg->base_steps, (int)l, dN, &R, &sum_dP[l], &sum_sq_dP[l]);
+        N_l[l] += dN;
+        if (N_l[l] > 1) {
+          const double mean = sum_dP[l] / N_l[l];
+          const double v = (sum_sq_dP[l] / N_l[l]) - (mean * mean);
+          V_l[l] = v > 1e-18 ? v : 1e-18;
+        }
+      }
+    }
+    if (cfg->adaptive_rates && L >= 2) {
+      double est[2];
+      for (int which = 0; which < 2; ++which) {
+        double sum_l = 0, sum_logV = 0, sum_l_logV = 0, sum_l2 = 0;
+        int count = 0;
+        const size_t start_l = L - 2;
+        for (size_t l = start_l; l <= L; ++l) {
+          const double val = which == 0 ? fabs(sum_dP[l] / N_l[l]) : V_l[l];
+          if (val > 1e-16) {
+            const double y = log(val), x = (double)(l - start_l);
+            sum_l += x;
+            sum_logV += y;
+            sum_l_logV += x * y;
+            sum_l2 += x * x;
+            count++;
+          }
+        }
+        est[which] = count < 2 ? -1.0
+                               : -((count * sum_l_logV - sum_l * sum_logV) / (count * sum_l2 - sum_l * sum_l)) / log(2.0);
+      }
+      if (est[0] > 0.3) alpha = est[0] < 2.0 ? est[0] : 2.0;
+      if (est[1] > 0.3) beta = est[1] < 2.0 ? est[1] : 2.0;
+    }
+    double sum_sqrt_VC = 0.0;
+    for (size_t l = 0; l <= L; ++l) sum_sqrt_VC += sqrt(V_l[l] * cost_l[l]);
+    int needs_more = 0;
+    for (size_t l = 0; l <= L; ++l) {
+      const uint64_t optimal_N = (uint64_t)ceil(2.0 * pow(cfg->epsilon, -2.0) * sqrt(V_l[l] / cost_l[l]) * sum_sqrt_VC);
+      if (optimal_N > N_l[l]) needs_more = 1;
+    }
+    if (needs_more) continue;
+    const double diff_mean_L = fabs(sum_dP[L] / N_l[L]);
+    double effective = diff_mean_L;
+    if (L > 0) {
+      const double prev = 0.5 * fabs(sum_dP[L - 1] / N_l[L - 1]);
+      effective = diff_mean_L > prev ? diff_mean_L : prev;
+    }
+    const double bias = effective / (pow(2.0, alpha) - 1.0);
+    if (bias > cfg->epsilon / 1.4142135623730951) {
+      if (L < L_max) L++;
+      else converged = 1;
+    } else {
+      converged = 1;
+    }
+  }
+  memset(res, 0, sizeof *res);
+  res->alpha_estimated = alpha;
+  res->beta_estimated = beta;
+  res->n_levels = (uint32_t)(L + 1);
+  double var_total = 0.0;
+  for (size_t l = 0; l <= L; ++l) {
+    res->paths_per_level[l] = N_l[l];
+    const uint64_t spp = (l == 0) ? cfg->base_steps : (cfg->base_steps * (1ull << l) * 3 / 2);
+    res->total_steps += N_l[l] * spp;
+    const double mean = sum_dP[l] / N_l[l];
+    res->mean_diffs[l] = mean * df;
+    res->var_diffs[l] = V_l[l] * df * df;
+    res->price += mean * df;
+    var_total += V_l[l] / N_l[l];
+  }
+  res->price_std_err = sqrt(var_total) * df;
+  free(R.pool);
+  free(P);
+  return 0;
+}

@@ -60,6 +60,8 @@ def restatement(fast: bool = False) -> C.CDLL:
     lib.myql_oracle_poissinvcdf.restype = C.c_double
     lib.myql_oracle_poissinvcdf.argtypes = [C.c_double, C.c_double]
     lib.myql_oracle_chi2_quantile.argtypes = [C.c_double, C.c_double]
+    lib.myql_oracle_mlmc_price.restype = C.c_int
+    lib.myql_oracle_mlmc_price.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
     lib.myql_oracle_uniform_of.restype = C.c_double
     lib.myql_oracle_uniform_of.argtypes = [C.c_uint64]
     return lib
@@ -73,6 +75,8 @@ def reference(fast: bool = False) -> C.CDLL:
     lib = _load("_ref/libmyql_ref_fast.so" if fast else "_ref/libmyql_ref.so")
     lib.myql_ref_mc_price.restype = C.c_int
     lib.myql_ref_mc_price.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double)]
+    lib.myql_ref_mlmc_price.restype = C.c_int
+    lib.myql_ref_mlmc_price.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
     lib.myql_ref_fourier.restype = C.c_int
     lib.myql_ref_fourier.argtypes = [C.c_void_p, C.c_double, C.POINTER(C.c_double)]
     return lib
@@ -129,3 +133,24 @@ def stream_states(seed: int, first: int, n: int) -> np.ndarray:
     out = np.zeros(4 * n, dtype=np.uint64)
     lib.myql_oracle_stream_states(seed, first, n, out.ctypes.data_as(C.POINTER(C.c_uint64)))
     return out.reshape(n, 4)
+
+
+def mlmc_price(job, cfg, layout: int = LAYOUT_REFERENCE, n_threads: int = 1, fast: bool = False):
+    """Restatement of MultiLevelMonteCarloPricer::calculate -> MlmcResultC."""
+    from myquantlib_gb300 import _abi
+    res = _abi.MlmcResultC()
+    if restatement(fast).myql_oracle_mlmc_price(C.byref(job.c), C.byref(cfg), layout, n_threads, C.byref(res)) != 0:
+        raise RuntimeError("oracle MLMC failed")
+    return res
+
+
+def ref_mlmc_price(job, cfg, n_threads: int = 1):
+    """The reference's own MultiLevelMonteCarloPricer (None when not instantiated)."""
+    from myquantlib_gb300 import _abi
+    res = _abi.MlmcResultC()
+    st = reference().myql_ref_mlmc_price(C.byref(job.c), C.byref(cfg), n_threads, C.byref(res))
+    if st == -2:
+        return None
+    if st != 0:
+        raise RuntimeError(f"reference MLMC failed ({st})")
+    return res

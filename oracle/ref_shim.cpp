@@ -21,6 +21,8 @@
 #include <myql/models/asvj/core/ASVJmodel.hpp>
 #include <myql/models/asvj/core/ASVJstepper.hpp>
 #include <myql/pricers/fourier/FourierPricer.hpp>
+#include <myql/models/asvj/core/CoupledASVJStepper.hpp>
+#include <myql/pricers/mlmc/MultiLevelMonteCarloPricer.hpp>
 #include <myql/pricers/montecarlo/MonteCarloPricer.hpp>
 
 #include "myql_gpu.h"
@@ -176,9 +178,90 @@ int exotic_any(const Model &model, const myql_mc_job &j, double *out) {
   }
 }
 
+MLMCConfig mlmc_cfg_of(const myql_mlmc_config &c) {
+  MLMCConfig m;
+  m.epsilon = c.epsilon;
+  m.L_min = c.L_min;
+  m.L_max = c.L_max;
+  m.N0 = c.N0;
+  m.base_steps = c.base_steps;
+  m.alpha = c.alpha;
+  m.beta = c.beta;
+  m.adaptive_rates = c.adaptive_rates != 0;
+  m.seed = c.seed;
+  m.fd_bump = c.fd_bump;
+  return m;
+}
+
+template <class Model, class Coupled, class Instr>
+int run_mlmc(const Model &model, const Instr &ins, const myql_mc_job &j, const myql_mlmc_config &c,
+             myql_mlmc_result *res) {
+  MultiLevelMonteCarloPricer<Model, Coupled, Instr, GreekMode::None> pricer(model, mlmc_cfg_of(c));
+  const auto r = pricer.calculate(j.S0, j.r, j.q, ins);
+  std::memset(res, 0, sizeof *res);
+  res->price = r.price;
+  res->price_std_err = r.price_std_err;
+  res->total_steps = r.total_steps;
+  res->n_levels = (uint32_t)r.paths_per_level.size();
+  for (size_t l = 0; l < r.paths_per_level.size() && l < MYQL_MLMC_MAX_LEVELS; ++l) {
+    res->paths_per_level[l] = r.paths_per_level[l];
+    res->mean_diffs[l] = r.mean_diffs[l];
+    res->var_diffs[l] = r.var_diffs[l];
+  }
+  res->alpha_estimated = r.alpha_estimated;
+  res->beta_estimated = r.beta_estimated;
+  return 0;
+}
+
 }  // namespace
 
 extern "C" {
+
+// The reference's MultiLevelMonteCarloPricer (GreekMode::None) for the
+// instantiated combinations; -2 otherwise.
+int myql_ref_mlmc_price(const myql_mc_job *jp, const myql_mlmc_config *cp, int n_threads,
+                        myql_mlmc_result *res) {
+  if (!jp || !cp || !res) return -1;
+  omp_set_num_threads(n_threads > 0 ? n_threads : 1);
+  const myql_mc_job &j = *jp;
+  const auto &m = j.model;
+  const auto &in = j.instrument;
+  const double K = in.strikes[0], T = in.maturity;
+  const bool call = in.option_type == MYQL_CALL;
+  if (in.payoff != MYQL_PAYOFF_VANILLA || in.is_strip) return -2;
+  if (is(j, 1, MYQL_SCHEME_NV, 0, MYQL_JUMP_NONE)) {
+    HestonModel model(hp(m.heston[0]));
+    if (in.kind == MYQL_INSTR_BARRIER && !in.barrier_up && in.barrier_action == MYQL_BARRIER_OUT && !call &&
+        in.rebate_timing == MYQL_REBATE_NONE) {
+      DownAndOutPut<> opt(K, in.barrier, T, in.barrier_rate, in.rebate);
+      return run_mlmc<HestonModel, CoupledHestonStepper<SchemeNV, TrackerBarrier<false>>, decltype(opt)>(model, opt, j, *cp, res);
+    }
+    if (in.kind == MYQL_INSTR_EUROPEAN && call) {
+      EuropeanOption<CallV> opt(K, T);
+      return run_mlmc<HestonModel, CoupledHestonStepper<SchemeNV, TrackerEuropean>, decltype(opt)>(model, opt, j, *cp, res);
+    }
+    return -2;
+  }
+  if (is(j, 1, MYQL_SCHEME_NCI, 0, MYQL_JUMP_MERTON) && in.kind == MYQL_INSTR_EUROPEAN && call) {
+    BatesModel model(hp(m.heston[0]), mp(m));
+    EuropeanOption<CallV> opt(K, T);
+    return run_mlmc<BatesModel, CoupledBatesStepper<SchemeNCI, TrackerEuropean>, decltype(opt)>(model, opt, j, *cp, res);
+  }
+  if (is(j, 0, 0, 0, MYQL_JUMP_NONE) && in.kind == MYQL_INSTR_ASIAN_ARITH && call && in.fixed_strike) {
+    BlackScholesModel model(m.vol);
+    AsianOption<TrackerArithAsian, CallV, true> opt(K, T);
+    return run_mlmc<BlackScholesModel, CoupledBlackScholesStepper<TrackerArithAsian>, decltype(opt)>(model, opt, j, *cp, res);
+  }
+  if (is(j, 2, MYQL_SCHEME_NV, MYQL_SCHEME_EXACT, MYQL_JUMP_KOU) && in.kind == MYQL_INSTR_LOOKBACK && call &&
+      !in.fixed_strike) {
+    DoubleBatesKouModel model(hp(m.heston[0]), hp(m.heston[1]), kp(m));
+    LookbackOption<CallV, false> opt(K, T);
+    return run_mlmc<DoubleBatesKouModel, CoupledDoubleBatesKouStepper<SchemeNV, SchemeExact, TrackerLookback>,
+                    decltype(opt)>(model, opt, j, *cp, res);
+  }
+  return -2;
+}
+
 
 // Prices one job with the reference's MonteCarloPricer on n_threads OpenMP
 // threads.  Returns 0, or -2 when the combination is not instantiated here.

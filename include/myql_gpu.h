@@ -224,6 +224,28 @@ myql_status myql_mc_price(myql_ctx *ctx, const myql_mc_job *job, double *out,
 myql_status myql_mc_price_async(myql_ctx *ctx, const myql_mc_job *job,
                                 double *out_dev, void *stream);
 
+/* Pricing without allocating device memory.  No counterpart in the reference
+ * (its pricer allocates freely on the host).  For callers that must not
+ * allocate GPU memory while they price -- their device memory belongs to their
+ * own pool or to another framework's allocator, or allocation is forbidden
+ * after start-up.  All scratch lives in one fixed device array of
+ * MYQL_NOALLOC_SCRATCH_BYTES inside the library, which every GPU that loads the
+ * library holds until the process exits; requests that need more (roughly
+ * paths * fields * 4 + streams * 32 + strikes * 8 bytes plus tile partials)
+ * return MYQL_ERR_TOO_LARGE.  Scope: GreekMode None and Essential, schemes NV
+ * and Exact (NCI needs its chi-squared tables).  No context is needed: the
+ * first call on each device does a one-time set-up on that device (it looks
+ * up the array's device address and uploads the stream-jump polynomials), so
+ * make that first call before any stream capture.  The call enqueues on
+ * `stream` (cudaStream_t as void*, NULL = legacy default stream) and returns
+ * once the stream has finished the request; out_dev is a device buffer of
+ * MYQL_OUT_DOUBLES(n_strikes) doubles.  Every call shares the one array, so
+ * calls that overlap on the GPU (other streams, other host threads) race:
+ * serialize them. */
+#define MYQL_NOALLOC_SCRATCH_BYTES (32 << 20)
+myql_status myql_mc_price_noalloc(int device, const myql_mc_job *job, double *out_dev,
+                                  void *stream);
+
 /* Many uneven requests in one persistent launch: replaces a loop of
  * dispatcher::price_mc calls (PricingDispatch.hpp:93-126).
  * outs[j] is the host output buffer of job j (MYQL_OUT_DOUBLES of its strikes). */

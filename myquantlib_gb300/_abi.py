@@ -101,6 +101,7 @@ _SIGS = {
     "myql_mc_price": (C.c_int, [C.c_void_p, C.POINTER(McJobC), C.POINTER(C.c_double),
                                 C.POINTER(McStatsC)]),
     "myql_mc_price_async": (C.c_int, [C.c_void_p, C.POINTER(McJobC), C.c_void_p, C.c_void_p]),
+    "myql_mc_price_noalloc": (C.c_int, [C.c_int, C.POINTER(McJobC), C.c_void_p, C.c_void_p]),
     "myql_mc_price_batch": (C.c_int, [C.c_void_p, C.POINTER(McJobC), C.c_size_t,
                                       C.POINTER(C.POINTER(C.c_double)), C.POINTER(McStatsC)]),
     "myql_mc_paths": (C.c_int, [C.c_void_p, C.POINTER(McJobC), C.POINTER(C.c_float), C.c_size_t,

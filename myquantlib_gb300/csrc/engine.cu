@@ -89,6 +89,13 @@ static void compute_polys() {
   std::memcpy(g_polys, tmp, sizeof tmp);
 }
 
+// The jump polynomials for callers outside this file (nullptr if the derived
+// polynomial failed its check against the published jump()).
+const unsigned long long (*jump_polynomials())[4] {
+  std::call_once(g_poly_once, compute_polys);
+  return g_polys_ok ? g_polys : nullptr;
+}
+
 int tracker_of(const myql_instrument &in) {
   switch (in.kind) {
     case MYQL_INSTR_EUROPEAN: return TRK_EUROPEAN;

@@ -291,6 +291,13 @@ myql_status myql_mlmc_price(myql_ctx *ctx, const myql_mc_job *job,
                             const myql_mlmc_config *mlmc,
                             myql_mlmc_result *result);
 
+/* One evaluate_level call of the MLMC pricer (MultiLevelMonteCarloPricer.hpp:244-341)
+ * from a freshly seeded stream pool: dN paths of level l (0 = base stepper,
+ * l > 0 = coupled fine/coarse pair).  sums[0] = sum of P_l - P_(l-1),
+ * sums[1] = sum of squares (FP64).  Probe for per-level parity tests. */
+myql_status myql_mlmc_level(myql_ctx *ctx, const myql_mc_job *job, const myql_mlmc_config *mlmc,
+                            uint32_t level, uint64_t dN, double *sums);
+
 /* --- RNG streams (bit-exact against boost::random::xoshiro256pp) -------- */
 /* Writes the xoshiro256++ state of streams first..first+n-1 for `seed`:
  * stream k = state seeded by splitmix64(seed), advanced by k * 2^128 steps

@@ -83,8 +83,27 @@ void asian_consts(const myql_mc_job &job, const Plan &pl, double dt, int n_steps
 
 using namespace myql;
 
+static myql_status mlmc_run(myql_ctx *ctx_, const myql_mc_job *job_in, const myql_mlmc_config *cfg,
+                            myql_mlmc_result *res, int probe_level, uint64_t probe_dN,
+                            double *probe_sums);
+
 extern "C" myql_status myql_mlmc_price(myql_ctx *ctx_, const myql_mc_job *job_in,
                                        const myql_mlmc_config *cfg, myql_mlmc_result *res) {
+  if (!res) return set_error(MYQL_ERR_INVALID_ARG, "null result");
+  return mlmc_run(ctx_, job_in, cfg, res, -1, 0, nullptr);
+}
+
+extern "C" myql_status myql_mlmc_level(myql_ctx *ctx_, const myql_mc_job *job, const myql_mlmc_config *cfg,
+                                       uint32_t level, uint64_t dN, double *sums) {
+  if (!sums || dN == 0) return set_error(MYQL_ERR_INVALID_ARG, "need dN > 0 and an output");
+  if (cfg && level > cfg->L_max) return set_error(MYQL_ERR_INVALID_ARG, "level above L_max");
+  myql_mlmc_result unused;
+  return mlmc_run(ctx_, job, cfg, &unused, (int)level, dN, sums);
+}
+
+static myql_status mlmc_run(myql_ctx *ctx_, const myql_mc_job *job_in, const myql_mlmc_config *cfg,
+                            myql_mlmc_result *res, int probe_level, uint64_t probe_dN,
+                            double *probe_sums) {
   CtxBase *ctx = reinterpret_cast<CtxBase *>(ctx_);
   if (!ctx || !job_in || !cfg || !res) return set_error(MYQL_ERR_INVALID_ARG, "null argument");
   cudaError_t e = cudaSetDevice(ctx->device);
@@ -190,6 +209,12 @@ extern "C" myql_status myql_mlmc_price(myql_ctx *ctx_, const myql_mc_job *job_in
     return MYQL_OK;
   };
 
+  if (probe_level >= 0) {
+    probe_sums[0] = probe_sums[1] = 0.0;
+    s = evaluate_level((size_t)probe_level, probe_dN, probe_sums[0], probe_sums[1]);
+    if (s != MYQL_OK) return s;
+    return read_status(ctx, nullptr);
+  }
   // ---- Giles' adaptive controller (MultiLevelMonteCarloPricer.hpp:64-211)
   size_t L = cfg->L_min;
   std::vector<uint64_t> N_l(L_max + 1, 0);

@@ -1562,3 +1562,39 @@ int myql_oracle_mlmc_price(const myql_mc_job *job_in, const myql_mlmc_config *cf
   free(P);
   return 0;
 }
+
+/* One evaluate_level call from a freshly seeded pool (probe for the tests). */
+int myql_oracle_mlmc_level(const myql_mc_job *job_in, const myql_mlmc_config *cfg, int layout,
+                           int n_threads, uint32_t level, uint64_t dN, double *sums) {
+  if (!job_in || !cfg || !sums || n_threads < 1) return -1;
+  myql_mc_job job = *job_in;
+  job.config.time_steps = cfg->base_steps;
+  job.config.fd_bump = cfg->fd_bump;
+  nci_ws nci_unused[MAXSC][2];
+  memset(nci_unused, 0, sizeof nci_unused);
+  myql_mc_job jp = job;
+  jp.config.scheme[0] = jp.config.scheme[1] = MYQL_SCHEME_EXACT;
+  plan_t *P = (plan_t *)calloc(1, sizeof(plan_t));
+  plan_build(P, &jp, nci_unused);
+  mlmc_rng R;
+  R.layout = layout;
+  R.n_threads = n_threads;
+  R.S = cfg->n_streams ? cfg->n_streams : 131072ull;
+  if (layout == MYQL_ORACLE_LAYOUT_REFERENCE) {
+    R.pool = (xo_t *)malloc(sizeof(xo_t) * n_threads);
+    for (int t = 0; t < n_threads; ++t) xo_seed(&R.pool[t], cfg->seed + (uint64_t)t * 999983ull);
+  } else {
+    const uint64_t U = R.S < dN ? R.S : dN;
+    R.pool = (xo_t *)malloc(sizeof(xo_t) * R.S);
+    xo_seed(&R.pool[0], cfg->seed);
+    for (uint64_t k = 1; k < U; ++k) {
+      R.pool[k] = R.pool[k - 1];
+      xo_jump(&R.pool[k]);
+    }
+  }
+  sums[0] = sums[1] = 0.0;
+  mlmc_eval(P, &job, cfg->base_steps, (int)level, dN, &R, &sums[0], &sums[1]);
+  free(R.pool);
+  free(P);
+  return 0;
+}

@@ -62,6 +62,9 @@ def restatement(fast: bool = False) -> C.CDLL:
     lib.myql_oracle_chi2_quantile.argtypes = [C.c_double, C.c_double]
     lib.myql_oracle_mlmc_price.restype = C.c_int
     lib.myql_oracle_mlmc_price.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+    lib.myql_oracle_mlmc_level.restype = C.c_int
+    lib.myql_oracle_mlmc_level.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_uint32,
+                                           C.c_uint64, C.POINTER(C.c_double)]
     lib.myql_oracle_uniform_of.restype = C.c_double
     lib.myql_oracle_uniform_of.argtypes = [C.c_uint64]
     return lib
@@ -154,3 +157,12 @@ def ref_mlmc_price(job, cfg, n_threads: int = 1):
     if st != 0:
         raise RuntimeError(f"reference MLMC failed ({st})")
     return res
+
+
+def mlmc_level(job, cfg, level: int, dN: int, layout: int = LAYOUT_STREAMS, n_threads: int = 1):
+    """One evaluate_level call of the restatement -> (sum, sum of squares)."""
+    out = np.zeros(2)
+    if restatement().myql_oracle_mlmc_level(C.byref(job.c), C.byref(cfg), layout, n_threads, level, dN,
+                                            _dptr(out)) != 0:
+        raise RuntimeError("oracle MLMC level failed")
+    return out

@@ -10,3 +10,4 @@ from .pricers import (  # noqa: F401
     result_from_raw, stepper_for,
 )
 from . import _abi  # noqa: F401
+from . import dispatch  # noqa: F401

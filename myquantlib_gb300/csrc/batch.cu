@@ -1,8 +1,288 @@
-// batch.cu -- many pricing requests in one launch sequence (placeholder until
-// the persistent work-queue kernel lands).
+// batch.cu -- host side of myql_mc_price_batch: many uneven requests in one
+// persistent launch (the work the reference's runtime dispatcher does one
+// request at a time, PricingDispatch.hpp:93-126).
+//
+// Per call: plan every job (the same constants as myql_mc_price), seed one
+// stream table per distinct seed, cut every job into items of 128 streams,
+// order the items by cost (longest first), then
+//   H2D(job descriptors, items)  ->  persistent batch_kernel  ->  per-job finalize  ->  D2H
+// captured once as a CUDA graph per batch shape and replayed afterwards (only
+// the pinned staging buffers change between calls).  The persistent grid size
+// is chosen by a small autotuner on the first batch of a shape and cached.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <vector>
+
+#include "batch.cuh"
 #include "engine.h"
 
-extern "C" myql_status myql_mc_price_batch(myql_ctx *, const myql_mc_job *, size_t,
-                                           double *const *, myql_mc_stats *) {
-  return myql::set_error(MYQL_ERR_UNSUPPORTED, "batched pricing is not built yet");
+namespace myql {
+namespace {
+
+struct PinnedBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaHostAlloc(&p, bytes, cudaHostAllocDefault);
+    if (e == cudaSuccess) cap = bytes;
+    return e;
+  }
+  ~PinnedBuf() {
+    if (p) cudaFreeHost(p);
+  }
+};
+
+struct BatchState {
+  PinnedBuf h_jobs, h_items, h_slots, h_out;
+  DevBuf d_jobs, d_items, d_slots, d_partials, d_out, d_counter;
+  std::map<uint64_t, DevBuf> seed_tables;  // seed -> [4][kDefaultStreams] states
+  cudaGraphExec_t graph = nullptr;
+  uint64_t graph_key = 0;
+  std::map<uint64_t, unsigned int> tuned_blocks;  // shape signature -> persistent grid
+  ~BatchState() {
+    if (graph) cudaGraphExecDestroy(graph);
+  }
+};
+
+std::map<const CtxBase *, BatchState> g_batch;  // one batch state per context
+
+uint64_t mix(uint64_t h, uint64_t v) { return (h ^ v) * 0x100000001b3ull + (h >> 29); }
+
+}  // namespace
+
+cudaError_t launch_seed_streams(unsigned long long seed, unsigned long long first,
+                                unsigned long long n, unsigned long long *out, cudaStream_t stream);
+
+}  // namespace myql
+
+using namespace myql;
+
+extern "C" myql_status myql_mc_price_batch(myql_ctx *ctx_, const myql_mc_job *jobs, size_t n_jobs,
+                                           double *const *outs, myql_mc_stats *stats) {
+  CtxBase *ctx = reinterpret_cast<CtxBase *>(ctx_);
+  if (!ctx || !jobs || !outs || n_jobs == 0) return set_error(MYQL_ERR_INVALID_ARG, "null batch argument");
+  if (n_jobs > (1u << 24)) return set_error(MYQL_ERR_TOO_LARGE, "at most 2^24 jobs per batch");
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return cuda_status(e, "cudaSetDevice");
+  BatchState &B = g_batch[ctx];
+  cudaStream_t st = ctx->stream;
+
+  // ---- plan every job
+  std::vector<Plan> plans(n_jobs);
+  uint64_t total_items = 0, path_steps = 0, paths = 0;
+  std::map<uint64_t, uint64_t> seed_need;  // seed -> streams needed (offset + S)
+  for (size_t j = 0; j < n_jobs; ++j) {
+    const myql_mc_job &job = jobs[j];
+    if (!outs[j]) return set_error(MYQL_ERR_INVALID_ARG, "job %zu: null output", j);
+    myql_status s = validate_job(job);
+    if (s != MYQL_OK) return set_error(s, "job %zu: %s", j, g_err_message());
+    if (job.instrument.is_strip || job.instrument.n_strikes != 1 || job.config.greek_mode == MYQL_GREEKS_FULL)
+      return set_error(MYQL_ERR_UNSUPPORTED,
+                       "job %zu: batches take scalar instruments with GreekMode None or Essential", j);
+    s = make_plan(job, plans[j]);
+    if (s != MYQL_OK) return s;
+    const uint64_t need = job.config.stream_offset + plans[j].S;
+    if (need > kDefaultStreams * 64ull) return set_error(MYQL_ERR_TOO_LARGE, "job %zu: stream range too large", j);
+    uint64_t &cur = seed_need[job.config.seed];
+    cur = std::max(cur, need);
+    total_items += (plans[j].S + kBatchItemStreams - 1) / kBatchItemStreams;
+    path_steps += plans[j].M * (uint64_t)plans[j].steps;
+    paths += plans[j].M;
+  }
+  if (seed_need.size() > 256) return set_error(MYQL_ERR_TOO_LARGE, "at most 256 distinct seeds per batch");
+
+  // ---- stream tables, one per seed (kept across calls)
+  std::map<uint64_t, std::pair<const unsigned long long *, uint64_t>> tables;
+  ctx->launches = 0;
+  for (auto &kv : seed_need) {
+    DevBuf &tb = B.seed_tables[kv.first];
+    const uint64_t n = std::max<uint64_t>(kv.second, kDefaultStreams);
+    if (tb.cap < n * 32) {
+      e = tb.ensure(n * 32);
+      if (e == cudaSuccess) e = launch_seed_streams(kv.first, 0, n, (unsigned long long *)tb.p, st);
+      if (e != cudaSuccess) return cuda_status(e, "batch seed table");
+      ctx->launches++;
+    }
+    tables[kv.first] = {(const unsigned long long *)tb.p, tb.cap / 32};
+  }
+  e = ctx->status.ensure(16);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ctx->status.p, 0, 16, st);
+  if (e != cudaSuccess) return cuda_status(e, "status");
+
+  // ---- host staging: jobs, items, slots
+  e = B.h_jobs.ensure(n_jobs * sizeof(BatchJob));
+  if (e == cudaSuccess) e = B.h_items.ensure(total_items * sizeof(BatchItem));
+  if (e == cudaSuccess) e = B.h_slots.ensure(total_items * sizeof(unsigned int));
+  if (e == cudaSuccess) e = B.h_out.ensure(n_jobs * 2 * kQ * sizeof(double));
+  if (e == cudaSuccess) e = B.d_jobs.ensure(n_jobs * sizeof(BatchJob));
+  if (e == cudaSuccess) e = B.d_items.ensure(total_items * sizeof(BatchItem));
+  if (e == cudaSuccess) e = B.d_slots.ensure(total_items * sizeof(unsigned int));
+  if (e == cudaSuccess) e = B.d_partials.ensure(total_items * kBatchQ * 2 * sizeof(double));
+  if (e == cudaSuccess) e = B.d_out.ensure(n_jobs * 2 * kQ * sizeof(double));
+  if (e == cudaSuccess) e = B.d_counter.ensure(256);
+  if (e == cudaSuccess) e = ctx->strikes.ensure(n_jobs * sizeof(double));
+  if (e != cudaSuccess) return cuda_status(e, "batch buffers");
+  BatchJob *hj = (BatchJob *)B.h_jobs.p;
+  BatchItem *hi = (BatchItem *)B.h_items.p;
+  unsigned int *hs = (unsigned int *)B.h_slots.p;
+  std::vector<double> strikes(n_jobs);
+  std::vector<double> cost(total_items);
+  uint64_t item = 0;
+  uint64_t signature = 0;
+  // NCI tables: a later job may grow (reallocate) a table an earlier job of the
+  // same dimension d already points at, so build everything first and take the
+  // pointers in a second pass.
+  for (int pass = 0; pass < 2; ++pass)
+    for (size_t j = 0; j < n_jobs; ++j)
+      for (int f = 0; f < plans[j].nf; ++f)
+        if (jobs[j].config.scheme[f] == MYQL_SCHEME_NCI) {
+          myql_status s = ensure_nci(ctx, jobs[j].model.heston[f], plans[j].sim.sc[0].dt, plans[j].sim.nci[f]);
+          if (s != MYQL_OK) return s;
+        }
+  for (size_t j = 0; j < n_jobs; ++j) {
+    const myql_mc_job &job = jobs[j];
+    Plan &pl = plans[j];
+    BatchJob &J = hj[j];
+    std::memset(&J, 0, sizeof J);
+    J.sim = pl.sim;
+    J.pay = pl.pay;
+    const auto &tb = tables[job.config.seed];
+    J.sim.states = const_cast<unsigned long long *>(tb.first);
+    J.sim.status = (unsigned int *)ctx->status.p;
+    J.sim.loop_cap = ctx->loop_cap;
+    J.state_stride = tb.second;
+    J.stream_base = job.config.stream_offset;
+    strikes[j] = job.instrument.strikes[0];
+    J.pay.strikes = (const double *)ctx->strikes.p + j;
+    J.klass = batch_class(pl.nf, pl.s1, pl.s2);
+    J.mode = pl.mode;
+    J.df = pl.df;
+    J.first_item = item;
+    J.n_items = (pl.S + kBatchItemStreams - 1) / kBatchItemStreams;
+    const double per_stream = (double)((pl.M + pl.S - 1) / pl.S) * pl.steps *
+                              (1.0 + pl.nf + (pl.s1 >= 2 ? 1.5 : 0.0) + (pl.s2 >= 2 ? 1.5 : 0.0));
+    for (uint64_t k = 0; k < J.n_items; ++k, ++item) {
+      hi[item].job = (unsigned int)j;
+      hi[item].stream0 = (unsigned int)(k * kBatchItemStreams);
+      cost[item] = per_stream;
+    }
+    signature = mix(signature, (uint64_t)J.klass * 1315423911ull + pl.steps);
+  }
+  // longest items first; slot = item index in job order (finalize sums slots in order)
+  std::vector<uint64_t> order(total_items);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](uint64_t a, uint64_t b) { return cost[a] > cost[b]; });
+  {
+    std::vector<BatchItem> tmp(hi, hi + total_items);
+    for (uint64_t k = 0; k < total_items; ++k) {
+      hi[k] = tmp[order[k]];
+      hs[k] = (unsigned int)order[k];
+    }
+  }
+  e = cudaMemcpyAsync(ctx->strikes.p, strikes.data(), n_jobs * sizeof(double), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_status(e, "batch strikes");
+
+  BatchParams P;
+  P.jobs = (const BatchJob *)B.d_jobs.p;
+  P.items = (const BatchItem *)B.d_items.p;
+  P.item_slot = (const unsigned int *)B.d_slots.p;
+  P.n_items = total_items;
+  P.counter = (unsigned int *)B.d_counter.p;
+  P.partials = (double *)B.d_partials.p;
+
+  // ---- autotune the persistent grid once per batch shape
+  const int occ = batch_blocks_per_sm();
+  signature = mix(signature, n_jobs);
+  unsigned int blocks = (unsigned int)(occ * ctx->sm_count);
+  auto tuned = B.tuned_blocks.find(signature);
+  if (tuned != B.tuned_blocks.end()) {
+    blocks = tuned->second;
+  } else if (total_items > (uint64_t)8 * occ * ctx->sm_count) {
+    // candidates on the leading (most expensive) items of this batch
+    const unsigned int cands[3] = {(unsigned int)(occ * ctx->sm_count),
+                                   (unsigned int)std::max(1, occ / 2) * (unsigned int)ctx->sm_count,
+                                   (unsigned int)ctx->sm_count};
+    BatchParams T = P;
+    T.n_items = std::min<uint64_t>(total_items, (uint64_t)4 * occ * ctx->sm_count);
+    e = cudaMemcpyAsync(B.d_jobs.p, hj, n_jobs * sizeof(BatchJob), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(B.d_items.p, hi, T.n_items * sizeof(BatchItem), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(B.d_slots.p, hs, T.n_items * sizeof(unsigned int), cudaMemcpyHostToDevice, st);
+    float best = 1e30f;
+    for (int c = 0; c < 3 && e == cudaSuccess; ++c) {
+      e = cudaMemsetAsync(B.d_counter.p, 0, 4, st);
+      if (e == cudaSuccess) e = cudaEventRecord(ctx->ev0, st);
+      if (e == cudaSuccess) e = launch_batch(T, cands[c], st);
+      if (e == cudaSuccess) e = cudaEventRecord(ctx->ev1, st);
+      if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev1);
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+      ctx->launches++;
+      if (ms < best) {
+        best = ms;
+        blocks = cands[c];
+      }
+    }
+    if (e != cudaSuccess) return cuda_status(e, "batch autotune");
+    B.tuned_blocks[signature] = blocks;
+  }
+
+  // ---- the batch itself, through a CUDA graph per shape
+  uint64_t key = mix(mix(signature, total_items), blocks);
+  for (const void *ptr : {B.h_jobs.p, B.h_items.p, B.h_slots.p, B.h_out.p, B.d_jobs.p, B.d_items.p, B.d_slots.p,
+                          B.d_partials.p, B.d_out.p, B.d_counter.p})
+    key = mix(key, (uint64_t)(uintptr_t)ptr);
+  if (!B.graph || B.graph_key != key) {
+    if (B.graph) cudaGraphExecDestroy(B.graph);
+    B.graph = nullptr;
+    cudaGraph_t g = nullptr;
+    e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(B.d_jobs.p, B.h_jobs.p, n_jobs * sizeof(BatchJob), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(B.d_items.p, B.h_items.p, total_items * sizeof(BatchItem), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(B.d_slots.p, B.h_slots.p, total_items * sizeof(unsigned int), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.d_counter.p, 0, 4, st);
+    if (e == cudaSuccess) e = launch_batch(P, blocks, st);
+    if (e == cudaSuccess)
+      e = launch_batch_finalize((const BatchJob *)B.d_jobs.p, (unsigned int)n_jobs, (const double *)B.d_partials.p,
+                                (double *)B.d_out.p, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(B.h_out.p, B.d_out.p, n_jobs * 2 * kQ * sizeof(double), cudaMemcpyDeviceToHost, st);
+    cudaError_t e2 = cudaStreamEndCapture(st, &g);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&B.graph, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      B.graph = nullptr;
+      return cuda_status(e, "batch graph capture");
+    }
+    B.graph_key = key;
+  }
+  e = cudaEventRecord(ctx->ev0, st);
+  if (e == cudaSuccess) e = cudaGraphLaunch(B.graph, st);
+  if (e == cudaSuccess) e = cudaEventRecord(ctx->ev1, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_status(e, "batch run");
+  ctx->launches += 2;
+  const double *ho = (const double *)B.h_out.p;
+  for (size_t j = 0; j < n_jobs; ++j) {
+    // [quantity][value, se] -> the myql_mc_price layout [2q + (0|1)][strike]
+    std::memcpy(outs[j], ho + j * 2 * kQ, 2 * kQ * sizeof(double));
+  }
+  if (stats) {
+    std::memset(stats, 0, sizeof *stats);
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    stats->device_ms = ms;
+    stats->simulate_ms = ms;
+    stats->paths = paths;
+    stats->path_steps = path_steps;
+    stats->scenarios = 1;
+    stats->kernel_launches = ctx->launches;
+  }
+  return read_status(ctx, stats);
 }

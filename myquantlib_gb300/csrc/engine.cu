@@ -39,6 +39,8 @@ cudaError_t launch_sampler_probe(int kind, const unsigned long long *x, const do
 
 thread_local std::string g_err;
 
+const char *g_err_message() { return g_err.c_str(); }
+
 myql_status set_error(myql_status st, const char *fmt, ...) {
   char buf[512];
   va_list ap;

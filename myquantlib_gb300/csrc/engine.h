@@ -85,6 +85,7 @@ struct CtxBase {
 
 myql_status set_error(myql_status st, const char *fmt, ...);
 myql_status cuda_status(cudaError_t e, const char *what);
+const char *g_err_message();  // the calling thread's last error text
 
 // Job planning: everything the launches need, computed in FP64 on the host.
 struct Plan {

@@ -441,6 +441,16 @@ class Engine:
         _abi.check(self.lib.myql_mc_price(self.handle, C.byref(job.c), _ptr(out), C.byref(st)))
         return out.reshape(2 * _abi.Q_COUNT, job.n_strikes), st
 
+    def price_batch(self, jobs: list["_Job"]) -> tuple[list[np.ndarray], _abi.McStatsC]:
+        """All jobs in one persistent launch (scalar instruments, GreekMode NONE/ESSENTIAL)."""
+        n = len(jobs)
+        arr = (_abi.McJobC * n)(*[j.c for j in jobs])
+        outs = [np.zeros(2 * _abi.Q_COUNT, dtype=np.float64) for _ in jobs]
+        ptrs = (C.POINTER(C.c_double) * n)(*[_ptr(o) for o in outs])
+        st = _abi.McStatsC()
+        _abi.check(self.lib.myql_mc_price_batch(self.handle, arr, n, ptrs, C.byref(st)))
+        return [o.reshape(2 * _abi.Q_COUNT, 1) for o in outs], st
+
     def paths(self, job: "_Job") -> np.ndarray:
         nsc, nf = C.c_uint32(), C.c_uint32()
         _abi.check(self.lib.myql_mc_paths(self.handle, C.byref(job.c), None, 0, C.byref(nsc),

@@ -129,9 +129,13 @@ def read_peaks() -> dict:
 
 
 def read_traffic() -> float | None:
-    p = ROOT / "profiles" / "simulate_kernel_bates_nci_full.json"
+    """DRAM bytes (read + write) of one full-size simulate_kernel launch (T = 1, 2^22 paths),
+    from the ncu summary committed under profiles/ (a `dram_bytes_per_launch: N` line)."""
+    p = ROOT / "profiles" / "simulate_kernel_bates_nci_traffic.md"
     if p.exists():
-        return json.loads(p.read_text()).get("dram_bytes_per_launch_full_size")
+        for line in p.read_text().splitlines():
+            if line.startswith("dram_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
     return None
 
 
@@ -311,11 +315,69 @@ def run_engine(args) -> dict:
     return line
 
 
-def run_ncu_case() -> None:
-    """A small case of the same kernels for an ncu capture (a few hundred MB on the device)."""
+def run_batch(args) -> dict:
+    """Batched uneven requests (4096 jobs, myquantlib_gb300.workloads.uneven_requests) in one
+    persistent launch per step.  value: path-steps / device time of the batch graph (descriptor
+    upload, persistent kernel, finalize, result download); e2e: the same over the wall-clock of
+    the whole myql_mc_price_batch call (host planning included)."""
+    import torch
+    import myquantlib_gb300 as m
+    from myquantlib_gb300 import workloads
+
+    if int(os.environ.get("RANK", "0")) != 0:
+        return {}
+    eng = m.Engine(0)
+    rq = workloads.uneven_requests(args.batch_jobs)
+    jobs = [m.make_job(r.model, m.stepper_for(r.model, r.instrument, r.scheme), r.instrument, r.mode, r.cfg,
+                       r.S0, r.r, r.q) for r in rq]
+    total = workloads.path_steps(rq)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda:0")
+    launches = 0
+    for _ in range(max(args.warmup, 1)):
+        _, st = eng.price_batch(jobs)
+        launches = st.kernel_launches
+    dev_ms, wall = [], []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            _, st = eng.price_batch(jobs)
+            wall.append(time.perf_counter() - t0)
+            dev_ms.append(st.device_ms)
+    value = total * args.steps / (sum(dev_ms) / 1e3)
+    e2e = total * args.steps / sum(wall)
+    line = {"metric": "paths*steps/s", "value": value, "unit": "paths*steps/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sum(dev_ms) / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": f"{len(jobs)} uneven requests (Heston / Bates-Kou / Double Heston, "
+                                   "arithmetic Asian or up-and-out call, SchemeExact) in one persistent launch",
+                       "jobs": len(jobs), "path_steps_per_step": total, "l2": "flushed between steps"},
+            "e2e": {"value": e2e, "unit": "paths*steps/s", "h2d_bytes_per_step": None,
+                    "d2h_bytes_per_step": 8 * 20 * len(jobs)},
+            "gpu_launches": launches * args.steps, "clocks": clk.summary()}
+    if not args.no_cpu:
+        from oracle import oracle
+        oracle.build(ref=False)
+        cores = os.cpu_count() or 1
+        n_s = 32
+        t0 = time.perf_counter()
+        for j in jobs[:n_s]:
+            oracle.mc_price(j, oracle.LAYOUT_REFERENCE, cores, fast=True)
+        t = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": workloads.path_steps(rq[:n_s]) / t, "unit": "paths*steps/s",
+                                "cores": cores, "kind": "port",
+                                "sample": f"the first {n_s} requests at full size, one after another ({t:.1f} s)"}
+    return line
+
+
+def run_ncu_case(full: bool = False) -> None:
+    """One maturity (T = 1) of the workload, priced twice, for an ncu capture: 2^18 paths (a few
+    hundred MB on the device), or the full 2^22 paths for one-pass metrics."""
     import myquantlib_gb300 as m
     eng = m.Engine(0)
-    job = workload_jobs(m, paths=1 << 18)[MATURITIES.index(1.0)]
+    job = workload_jobs(m, paths=PATHS if full else 1 << 18)[MATURITIES.index(1.0)]
     for _ in range(2):
         eng.price(job)
 
@@ -328,13 +390,21 @@ def main():
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
     ap.add_argument("--cpu-paths", type=int, default=8192, help="paths of the smaller CPU-baseline sample")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--workload", choices=["strip", "batch"], default="strip",
+                    help="strip: the Bates Full-Greeks strip (headline); batch: uneven requests in one launch")
+    ap.add_argument("--batch-jobs", type=int, default=4096)
     ap.add_argument("--ncu-case", action="store_true",
                     help="profiling case: one maturity (T=1), 2^18 paths, two requests, no timing")
+    ap.add_argument("--ncu-full", action="store_true",
+                    help="profiling case at the full 2^22 paths (for one-pass metrics only)")
     args = ap.parse_args()
-    if args.ncu_case:
-        run_ncu_case()
+    if args.ncu_case or args.ncu_full:
+        run_ncu_case(full=args.ncu_full)
         return
-    line = run_reference(args) if args.impl == "reference" else run_engine(args)
+    if args.impl == "reference":
+        line = run_reference(args)
+    else:
+        line = run_batch(args) if args.workload == "batch" else run_engine(args)
     if line:
         print(json.dumps(line), flush=True)
 

@@ -39,7 +39,7 @@ struct PinnedBuf {
   }
 };
 
-struct BatchState {
+struct BatchState : ExtState {
   PinnedBuf h_jobs, h_items, h_slots, h_out;
   DevBuf d_jobs, d_items, d_slots, d_partials, d_out, d_counter;
   std::map<uint64_t, DevBuf> seed_tables;  // seed -> [4][kDefaultStreams] states
@@ -50,8 +50,6 @@ struct BatchState {
     if (graph) cudaGraphExecDestroy(graph);
   }
 };
-
-std::map<const CtxBase *, BatchState> g_batch;  // one batch state per context
 
 uint64_t mix(uint64_t h, uint64_t v) { return (h ^ v) * 0x100000001b3ull + (h >> 29); }
 
@@ -71,7 +69,8 @@ extern "C" myql_status myql_mc_price_batch(myql_ctx *ctx_, const myql_mc_job *jo
   if (n_jobs > (1u << 24)) return set_error(MYQL_ERR_TOO_LARGE, "at most 2^24 jobs per batch");
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e != cudaSuccess) return cuda_status(e, "cudaSetDevice");
-  BatchState &B = g_batch[ctx];
+  if (!ctx->batch) ctx->batch.reset(new BatchState);
+  BatchState &B = *static_cast<BatchState *>(ctx->batch.get());
   cudaStream_t st = ctx->stream;
 
   // ---- plan every job
@@ -96,14 +95,23 @@ extern "C" myql_status myql_mc_price_batch(myql_ctx *ctx_, const myql_mc_job *jo
     path_steps += plans[j].M * (uint64_t)plans[j].steps;
     paths += plans[j].M;
   }
-  if (seed_need.size() > 256) return set_error(MYQL_ERR_TOO_LARGE, "at most 256 distinct seeds per batch");
-
-  // ---- stream tables, one per seed (kept across calls)
+  // ---- stream tables, one per seed (kept across calls; 32 bytes per stream)
+  uint64_t table_bytes = 0;
+  for (auto &kv : seed_need) table_bytes += ((kv.second + 1023) & ~1023ull) * 32;
+  if (table_bytes > (8ull << 30))
+    return set_error(MYQL_ERR_TOO_LARGE, "stream tables of the batch's seeds exceed 8 GiB");
+  {
+    uint64_t cached = 0;
+    for (auto &kv : B.seed_tables) cached += kv.second.cap;
+    if (cached > (2ull << 30))  // drop the tables this batch does not use
+      for (auto it = B.seed_tables.begin(); it != B.seed_tables.end();)
+        it = seed_need.count(it->first) ? std::next(it) : B.seed_tables.erase(it);
+  }
   std::map<uint64_t, std::pair<const unsigned long long *, uint64_t>> tables;
   ctx->launches = 0;
   for (auto &kv : seed_need) {
     DevBuf &tb = B.seed_tables[kv.first];
-    const uint64_t n = std::max<uint64_t>(kv.second, kDefaultStreams);
+    const uint64_t n = (kv.second + 1023) & ~1023ull;
     if (tb.cap < n * 32) {
       e = tb.ensure(n * 32);
       if (e == cudaSuccess) e = launch_seed_streams(kv.first, 0, n, (unsigned long long *)tb.p, st);

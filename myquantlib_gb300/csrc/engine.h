@@ -4,6 +4,7 @@
 
 #include <cstdint>
 #include <map>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -33,6 +34,11 @@ struct NciEntry {
   DevBuf main, tail;
 };
 
+// Per-context state owned by another subsystem (batch queue, control variates).
+struct ExtState {
+  virtual ~ExtState() = default;
+};
+
 struct CtxBase {
   int device = 0;
   int sm_count = 0;
@@ -49,6 +55,7 @@ struct CtxBase {
   DevBuf records, partials, out, status, strikes;
   DevBuf probe_a, probe_b, probe_c;
   DevBuf aux_a, aux_b, aux_c, aux_d;  // batch / MLMC / control-variate work buffers
+  std::unique_ptr<ExtState> batch, cv;  // released with the context
   // event pairs around the phase launches of the current call (tag 0 = simulate, 1 = payoff)
   std::vector<cudaEvent_t> ev_pool;
   std::vector<int> ev_tags;
@@ -63,6 +70,8 @@ struct CtxBase {
     return ev_pool[ev_used++];
   }
   void release_all() {
+    batch.reset();
+    cv.reset();
     for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
     ev_pool.clear();
     st_cached.release();

@@ -6,7 +6,8 @@ v0, theta ~ U[0.01, 0.1], kappa ~ U[0.5, 4], sigma ~ U[0.1, 1],
 rho ~ U[-0.9, 0]; Kou lambda ~ U[0, 1], p = 0.4, eta1 = 10, eta2 = 5;
 paths = round(2^U[14, 20]), steps = round(2^U[4, 9]); instrument an
 arithmetic-Asian call or an up-and-out call with B = 1.3 S0 (50/50),
-K ~ U[80, 120], T = 1, S0 = 100, r = 0.02, q = 0.
+K ~ U[80, 120], T = 1, S0 = 100, r = 0.02, q = 0, seed 42 for every request
+(MonteCarloConfig's default, MonteCarloPricer.hpp:16-26).
 
 Variance scheme: SchemeExact for every factor.  The dispatcher's default
 (SchemeNCI, StepperTraits.hpp:68) builds a chi-squared quantile table per
@@ -53,7 +54,7 @@ def uneven_requests(n_jobs: int = 4096, seed: int = UNEVEN_SEED, max_log2_paths:
             instr = _p.AsianOption(_p.TrackerArithAsian, _p.PayoffVanilla(_p.OptionType.Call), True, K, 1.0)
         else:
             instr = _p.UpAndOutCall(K, 130.0, 1.0)
-        cfg = _p.MonteCarloConfig(num_paths=paths, time_steps=steps, seed=42 + j)
+        cfg = _p.MonteCarloConfig(num_paths=paths, time_steps=steps)  # seed 42, the reference default
         out.append(_d.Request(model, instr, cfg, 100.0, 0.02, 0.0, mode=mode, scheme=scheme))
     return out
 

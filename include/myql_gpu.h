@@ -327,6 +327,65 @@ myql_status myql_probe_sampler(myql_ctx *ctx, int kind, const uint64_t *x,
  * microbenchmark on every SM. */
 myql_status myql_probe_peak(myql_ctx *ctx, int kind, double *ops_per_second);
 
+/* --- neural martingale control variate (no counterpart in the reference) --
+ * An MLP g(t/T, log(S/S0), v1, v2, average to date, 1) -> 128 -> 128 -> 128
+ * (SiLU) -> 1 with BF16 weights and FP32 accumulation on the tensor cores,
+ * trained on pilot paths of the same model (an independent seed) to minimise
+ * Var(Y - C), C = sum_j g(state at t_j) dM_j, where dM_j is the increment of
+ * the discounted asset S e^{-(r-q)t} over the j-th hedge interval, centred
+ * step by step under the discretisation scheme.  E[C] = 0 for any network, so
+ * the price estimator mean(Y - C) is unbiased; the plain estimator mean(Y) of
+ * the same paths is returned beside it.  Scalar European and Asian
+ * instruments; GreekMode is ignored (prices only). */
+#define MYQL_CV_PARAMS 35332 /* FP32 parameters: W1[128][16] b1 W2[128][128] b2 W3[128][128] b3 w4[128] b4 (+3 pad) */
+typedef struct myql_cv_config {
+  uint32_t hedge_every;  /* time steps per hedge interval (hedge times t_j = j * hedge_every * dt) */
+  uint32_t iterations;   /* Adam steps (<= 4096)                                                */
+  uint64_t pilot_paths;  /* training paths (rounded up to a multiple of 128)                    */
+  uint64_t batch_paths;  /* paths per Adam step                                                 */
+  double learning_rate;  /* peak Adam step size (cosine decay to 5 %)                           */
+  uint64_t seed;         /* network initialisation                                              */
+} myql_cv_config;
+
+typedef struct myql_cv_result {
+  double price, price_std_err;             /* control-variate estimator              */
+  double plain_price, plain_std_err;       /* plain Monte Carlo on the same paths    */
+  double variance_ratio;                   /* Var(Y) / Var(Y - C)                    */
+  double initial_loss, final_loss;         /* training: first / last minibatch loss  */
+  double train_ms, simulate_ms, mlp_ms, total_ms;
+  uint64_t paths;
+  uint32_t kernel_launches;
+} myql_cv_result;
+
+/* Pilot simulation + training; the network stays in the context.  res (may be
+ * NULL) reports the in-sample estimators on the pilot paths. */
+myql_status myql_cv_train(myql_ctx *ctx, const myql_mc_job *job, const myql_cv_config *cfg,
+                          myql_cv_result *res);
+/* Prices job (its own seed, paths and streams) with the context's network. */
+myql_status myql_cv_price(myql_ctx *ctx, const myql_mc_job *job, const myql_cv_config *cfg,
+                          myql_cv_result *res);
+/* Network parameters (MYQL_CV_PARAMS floats): fresh initialisation, read, write. */
+myql_status myql_cv_init(myql_ctx *ctx, uint64_t seed);
+myql_status myql_cv_get_params(myql_ctx *ctx, float *params, size_t n);
+myql_status myql_cv_set_params(myql_ctx *ctx, const float *params, size_t n);
+/* The MLP kernels on caller data (checks against a CPU MLP): rows are
+ * (path p, hedge j) at p * n_hedge + j; feats[row][6], dM[row], Y[path].
+ * forward: cv[p] = sum_j g_j dM_j and g[row] (g may be NULL).
+ * gradient: the gradient of L = mean_p (Y_p - cv_p - mean(Y - cv))^2 with
+ * respect to the parameter blob, and L. */
+myql_status myql_cv_forward(myql_ctx *ctx, const float *feats, const float *dM, uint64_t n_paths,
+                            uint32_t n_hedge, float *cv, float *g);
+myql_status myql_cv_gradient(myql_ctx *ctx, const float *feats, const float *dM, const float *Y,
+                             uint64_t n_paths, uint32_t n_hedge, float *grad, double *loss);
+
+/* One-tile tcgen05 GEMM D[128][N] = A[128][K] * B[N][K]^T with the operands
+ * rounded to BF16 and FP32 accumulation, through the shared-memory operand
+ * layouts and descriptors the control-variate MLP kernels use: mode 0 K = 16,
+ * N = 128; mode 1 K = 128, N = 128; mode 2 K = 128, N = 16; mode 3 K = 128,
+ * N = 128 with both operands stored MN-major.  A ([128][K]), B ([N][K]) and
+ * D ([128][N]) are row-major host arrays. */
+myql_status myql_probe_mma(myql_ctx *ctx, int32_t mode, const float *A, const float *B, float *D);
+
 #ifdef __cplusplus
 }
 #endif

@@ -84,6 +84,22 @@ class MlmcResultC(C.Structure):
                 ("device_ms", C.c_double)]
 
 
+CV_PARAMS = 35332
+
+
+class CvConfigC(C.Structure):
+    _fields_ = [("hedge_every", C.c_uint32), ("iterations", C.c_uint32), ("pilot_paths", C.c_uint64),
+                ("batch_paths", C.c_uint64), ("learning_rate", C.c_double), ("seed", C.c_uint64)]
+
+
+class CvResultC(C.Structure):
+    _fields_ = [("price", C.c_double), ("price_std_err", C.c_double), ("plain_price", C.c_double),
+                ("plain_std_err", C.c_double), ("variance_ratio", C.c_double), ("initial_loss", C.c_double),
+                ("final_loss", C.c_double), ("train_ms", C.c_double), ("simulate_ms", C.c_double),
+                ("mlp_ms", C.c_double), ("total_ms", C.c_double), ("paths", C.c_uint64),
+                ("kernel_launches", C.c_uint32)]
+
+
 class MyqlError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"[myql status {status}] {message}")
@@ -119,6 +135,17 @@ _SIGS = {
     "myql_probe_sampler": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_uint64),
                                      C.POINTER(C.c_double), C.POINTER(C.c_float), C.c_size_t]),
     "myql_probe_peak": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
+    "myql_cv_train": (C.c_int, [C.c_void_p, C.POINTER(McJobC), C.POINTER(CvConfigC), C.POINTER(CvResultC)]),
+    "myql_cv_price": (C.c_int, [C.c_void_p, C.POINTER(McJobC), C.POINTER(CvConfigC), C.POINTER(CvResultC)]),
+    "myql_cv_init": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "myql_cv_get_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_size_t]),
+    "myql_cv_set_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_size_t]),
+    "myql_cv_forward": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_uint64, C.c_uint32,
+                                  C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "myql_cv_gradient": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                   C.c_uint64, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_double)]),
+    "myql_probe_mma": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                 C.POINTER(C.c_float)]),
 }
 
 _lib = None

@@ -1,0 +1,167 @@
+// cv.cuh -- neural martingale control variate (no counterpart in the reference).
+//
+// A small MLP g(t, log S, v1, v2, running average) -> R is trained on pilot
+// paths of the engine itself and then used as the control
+//     C = sum_j g(state at t_j) * dM_j,
+// where dM_j is the martingale increment of the discounted asset
+// M_t = S_t e^{-(r-q) t} over the hedge interval [t_j, t_{j+1}).  Per step k
+// the increment is taken conditionally centred under the discrete scheme:
+//     dM_k = M_k e^{a_k} expm1(root G - root^2 / 2) + M_k' expm1(J_k),
+// with a_k = drift_k + root^2/2 - (r-q) dt, G independent of the variances and
+// E[e^{J}] = 1 (compensated jumps), so E[g_j dM_k] = 0 for any g_j that depends
+// on the path up to t_j: the estimator Y - C is unbiased whatever the network.
+//
+// Network: 16 input slots (6 used: t/T, x-scaled log-spot, scaled v1, v2, the
+// running average to date, 1) -> 128 -> 128 -> 128 (SiLU) -> 1, BF16 weights and
+// activations, FP32 accumulation on the tcgen05 tensor cores.
+//
+// Data layout (HBM): rows are (path, hedge time); a tile is 128 consecutive
+// paths at one hedge time, tiles ordered [path block][hedge time].  Feature
+// tiles are stored as the IMG16 shared-memory image (4 KB, moved by one bulk
+// copy); dM is FP32 [tile][128].
+#pragma once
+#include <cuda_bf16.h>
+
+#include "batch.cuh"
+#include "tc.cuh"
+
+namespace myql {
+
+constexpr int kCvHidden = 128;
+constexpr int kCvIn = 16;
+constexpr int kCvFeatures = 6;
+constexpr uint32_t kCvTileBytes = 128u * kCvIn * 2u;  // 4096
+
+// FP32 parameter blob: W1 [128][16], b1, W2 [128][128], b2, W3 [128][128], b3, w4 [128], b4
+constexpr int kPW1 = 0;
+constexpr int kPB1 = kPW1 + 128 * 16;
+constexpr int kPW2 = kPB1 + 128;
+constexpr int kPB2 = kPW2 + 128 * 128;
+constexpr int kPW3 = kPB2 + 128;
+constexpr int kPB3 = kPW3 + 128 * 128;
+constexpr int kPW4 = kPB3 + 128;
+constexpr int kPB4 = kPW4 + 128;
+constexpr int kPCount = kPB4 + 4;
+
+// Packed BF16 weight images: W1 IMG16 [128][16], W2 and W3 IMG128 [128][128],
+// W1 zero-padded to K = 64 as IMG128 [128][64] (backward kernel).
+constexpr uint32_t kImgW1 = 0, kImgW2 = 4096, kImgW3 = 4096 + 32768, kImgW1x64 = 4096 + 65536;
+constexpr uint32_t kImgBytes = kImgW1x64 + 16384;
+constexpr uint32_t kImgFwdBytes = kImgW1x64;  // W1, W2, W3
+// FP32 vectors beside the images: b1, b2, b3, w4 (128 each), b4
+constexpr int kVecB1 = 0, kVecB2 = 128, kVecB3 = 256, kVecW4 = 384, kVecB4 = 512, kVecCount = 516;
+
+constexpr unsigned long long kCvWaitNs = 2000000000ull;  // bounded waits: 2 s
+
+struct CvSimParams {
+  SimParams sim;        // one scenario (base), path-dependent stepping
+  PayoffParams pay;     // scalar instrument
+  double df;
+  uint8_t *feat;        // feature tiles of this launch's paths
+  float *dM;            // [tile][128]
+  float *Y;             // discounted payoff per path (launch-local index)
+  unsigned long long path_begin, path_end;
+  int hedge_every, n_hedge;
+  float rq_dt;          // (r - q) dt
+  float inv_T, x_scale, va_scale, vb_scale, S0;
+};
+
+struct CvMlpParams {
+  const uint8_t *feat;
+  const float *dM;
+  const uint8_t *img;   // packed weights (kImgBytes)
+  const float *vec;     // kVecCount floats
+  float *cv;            // per path: sum_j g_j dM_j
+  float *g_out;         // optional per-row g
+  const float *coef;    // backward: dL/dC per path
+  float *grad;          // backward: FP32 parameter-blob gradient (accumulated)
+  unsigned long long n_paths;
+  unsigned int n_pb, n_hedge;
+  unsigned int *status;  // [2] += 1 on a wait that ran out
+};
+
+namespace dev {
+
+// Path observer writing the features at hedge times and the centred
+// martingale increments of every hedge interval.
+struct CvHook {
+  static constexpr bool active = true;
+  const CvSimParams *P;
+  uint8_t *tile0;  // feature tile of hedge 0 for this path's block
+  float *dm0;      // dM entry of hedge 0 for this path
+  uint32_t lane;
+  int j, he, n;
+  float m, m_mid, acc, dt;
+
+  __device__ __forceinline__ void write_feat(int jj, float t, float X, float va, float vb, float avg) {
+    __nv_bfloat162 p0 = __floats2bfloat162_rn(t * P->inv_T, X * P->x_scale);
+    __nv_bfloat162 p1 = __floats2bfloat162_rn(va * P->va_scale, vb * P->vb_scale);
+    __nv_bfloat162 p2 = __floats2bfloat162_rn(avg, 1.0f);
+    uint4 c0;
+    c0.x = *reinterpret_cast<uint32_t *>(&p0);
+    c0.y = *reinterpret_cast<uint32_t *>(&p1);
+    c0.z = *reinterpret_cast<uint32_t *>(&p2);
+    c0.w = 0u;
+    uint8_t *tile = tile0 + (size_t)jj * kCvTileBytes;
+    *reinterpret_cast<uint4 *>(tile + tc::img16_offset(lane, 0)) = c0;
+    *reinterpret_cast<uint4 *>(tile + tc::img16_offset(lane, 8)) = make_uint4(0u, 0u, 0u, 0u);
+  }
+  __device__ __forceinline__ float average_to_date(int k, float X, float trk) const {
+    if (k == 0) return 0.0f;
+    if (P->sim.tracker == TRK_ARITH_ASIAN) return dt * (0.5f + trk - 0.5f * __expf(X)) * P->inv_T;
+    if (P->sim.tracker == TRK_GEO_ASIAN) return dt * (trk - 0.5f * X) * P->inv_T;
+    return 0.0f;
+  }
+  __device__ __forceinline__ void begin(float va, float vb) {
+    m = 1.0f;
+    acc = 0.0f;
+    j = 0;
+    write_feat(0, 0.0f, 0.0f, va, vb, 0.0f);
+  }
+  __device__ __forceinline__ void diffusion(float root, float G, float drift) {
+    const float half_var = 0.5f * root * root;
+    const float a = drift + half_var - P->rq_dt;
+    acc = fmaf(m * __expf(a), expm1f(fmaf(root, G, -half_var)), acc);
+    m_mid = m * __expf(fmaf(root, G, drift) - P->rq_dt);
+  }
+  __device__ __forceinline__ void jump(float J) { acc = fmaf(m_mid, expm1f(J), acc); }
+  __device__ __forceinline__ void step_end(int k, float X, float va, float vb, float trk) {
+    m = __expf(X - P->rq_dt * (float)k);
+    if (k < n && k % he == 0) {
+      dm0[(size_t)j * 128] = acc * P->S0;
+      acc = 0.0f;
+      ++j;
+      write_feat(j, (float)k * dt, X, va, vb, average_to_date(k, X, trk));
+    }
+  }
+  __device__ __forceinline__ void finish() { dm0[(size_t)j * 128] = acc * P->S0; }
+};
+
+// Terminal record -> the payoff pass's view of one path (base scenario).
+__device__ __forceinline__ PathView record_view(const PayoffParams &Q, const float (&r)[kMaxFields]) {
+  PathView v;
+  v.S = Q.S0 * __expf(r[0]);
+  v.Y = 0.0f;
+  v.hit[0] = v.hit[1] = v.hit[2] = -1.0f;
+  switch (Q.tracker) {
+    case TRK_GEO_ASIAN: v.Y = Q.S0 * __expf(fmaf(Q.avg_c1[0], r[1], Q.avg_c0[0])); break;
+    case TRK_ARITH_ASIAN: v.Y = Q.S0 * fmaf(Q.avg_c1[0], r[1], Q.avg_c0[0]); break;
+    default: break;
+  }
+  return v;
+}
+
+}  // namespace dev
+
+cudaError_t launch_cv_sim(const CvSimParams &P, int klass, cudaStream_t st);
+cudaError_t launch_cv_mlp(const CvMlpParams &P, unsigned int blocks, cudaStream_t st);
+cudaError_t launch_cv_bwd(const CvMlpParams &P, unsigned int blocks, cudaStream_t st);
+cudaError_t launch_cv_pack(const float *params, uint8_t *img, float *vec, cudaStream_t st);
+cudaError_t launch_cv_adam(float *params, float *m, float *v, const float *grad, float lr, float b1t, float b2t,
+                           cudaStream_t st);
+cudaError_t launch_cv_resid(const float *Y, const float *cv, unsigned long long n, float *coef, double *loss_out,
+                            cudaStream_t st);
+cudaError_t launch_cv_reduce(const float *Y, const float *cv, unsigned long long n, double *sums4,
+                             cudaStream_t st);
+
+}  // namespace myql

@@ -1,0 +1,613 @@
+// cv_mlp.cu -- the control variate's MLP on the tcgen05 tensor cores.
+//
+// cv_mlp_kernel (forward, persistent): weights stay in shared memory; feature
+// tiles of 128 rows stream in by bulk copy (double buffered); per tile three
+// MMA chains (K = 16, 128, 128) accumulate FP32 in TMEM, and the four warps
+// turn each accumulator row into SiLU activations (BF16, written back as the
+// next layer's A operand).  The output layer is a per-row FP32 dot product,
+// multiplied by the row's martingale increment and summed per path over the
+// hedge times.
+//
+// cv_bwd_kernel (training): per tile, the forward pass again (keeping h1, h2
+// in shared memory), then back-propagation of dL/dg = coef_path * dM_row:
+//   dz3 = dg * w4 * silu'(z3)
+//   dh2 = dz3 W3        (W3's image read MN-major)      dW3 += dz3^T h2 (MN-major operands)
+//   dz2 = dh2 * silu'(z2)  (z2 recomputed into spare TMEM)
+//   dh1 = dz2 W2                                        dW2 += dz2^T h1
+//   dz1 = dh1 * silu'(z1)  (z1 recomputed)              dW1 += dz1^T x
+// dW2, dW3 accumulate in TMEM over the block's tiles, dW1 in registers, the
+// bias and output-layer gradients through warp reductions; one FP32 atomic add
+// per parameter and block at the end.
+//
+// Every mbarrier wait is bounded; a wait that runs out sets status[2], makes
+// the whole block leave its tile loop, waits (bounded) for its own bulk
+// copies in flight and frees its TMEM.
+#include "cv.cuh"
+
+namespace myql {
+namespace dev {
+
+__device__ __forceinline__ uint8_t *align1024(uint8_t *p) {
+  const uint32_t a = tc::smem_u32(p);
+  return p + (((a + 1023u) & ~1023u) - a);
+}
+
+// z (TMEM, 128 columns of this thread's row) + bias -> SiLU -> BF16 IMG128 row of H
+__device__ __forceinline__ void epi_hidden(uint32_t tm_row, const float *bias, uint8_t *H, uint32_t row) {
+#pragma unroll 1
+  for (int c = 0; c < 4; ++c) {
+    float v[32];
+    tc::tmem_ld32(tm_row + (uint32_t)(c * 32), v);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      uint32_t w[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int k = c * 32 + q * 8 + 2 * e;
+        __nv_bfloat162 p = __floats2bfloat162_rn(tc::silu(v[q * 8 + 2 * e] + bias[k]),
+                                                 tc::silu(v[q * 8 + 2 * e + 1] + bias[k + 1]));
+        w[e] = *reinterpret_cast<uint32_t *>(&p);
+      }
+      *reinterpret_cast<uint4 *>(H + tc::img128_offset(row, (uint32_t)(c * 32 + q * 8), 128)) =
+          make_uint4(w[0], w[1], w[2], w[3]);
+    }
+  }
+}
+
+// output layer: g = b4 + sum_k silu(z3_k + b3_k) w4_k
+__device__ __forceinline__ float epi_out(uint32_t tm_row, const float *vec) {
+  float g = vec[kVecB4];
+#pragma unroll 1
+  for (int c = 0; c < 4; ++c) {
+    float v[32];
+    tc::tmem_ld32(tm_row + (uint32_t)(c * 32), v);
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+      const int k = c * 32 + i;
+      g = fmaf(tc::silu(v[i] + vec[kVecB3 + k]), vec[kVecW4 + k], g);
+    }
+  }
+  return g;
+}
+
+// D[128 x N] (TMEM) = A (IMG128, [128][K]) * B (IMG128, [N][K])^T, K = 128, both K-major
+__device__ __forceinline__ void mma_k128(uint32_t d, const uint8_t *A, const uint8_t *B, int N, uint32_t acc0) {
+  const uint32_t a = tc::smem_u32(A), b = tc::smem_u32(B);
+#pragma unroll
+  for (int kk = 0; kk < 8; ++kk) {
+    const uint32_t ao = (uint32_t)(kk >> 2) * 16384u + (uint32_t)(kk & 3) * 32u;
+    const uint32_t bo = (uint32_t)(kk >> 2) * (uint32_t)N * 128u + (uint32_t)(kk & 3) * 32u;
+    tc::mma_bf16(d, tc::desc_sw128(a + ao), tc::desc_sw128(b + bo), tc::idesc_bf16(128, N),
+                 (kk > 0 || acc0) ? 1u : 0u);
+  }
+}
+
+// D[128 x N] = A^T B over K = 128 rows where A ([128 rows][128]) and B ([128 rows][N])
+// are natural IMG128 row images read MN-major (lines along M / N, 8-row K groups)
+__device__ __forceinline__ void mma_tn_rows(uint32_t d, const uint8_t *A, const uint8_t *B, int N, uint32_t acc0) {
+  const uint32_t a = tc::smem_u32(A), b = tc::smem_u32(B);
+#pragma unroll
+  for (int kk = 0; kk < 8; ++kk) {
+    const uint32_t o = (uint32_t)kk * 2048u;
+    tc::mma_bf16(d, tc::desc_sw128_mn(a + o, 16384u), tc::desc_sw128_mn(b + o, 16384u),
+                 tc::idesc_bf16_mn(128, N, true, true), (kk > 0 || acc0) ? 1u : 0u);
+  }
+}
+
+// D[128 rows x N] = A (IMG128 [128 rows][K], K-major) * W where W's IMG128 image
+// [K rows][N] is read MN-major: the back-propagation product dz * W.
+__device__ __forceinline__ void mma_nn(uint32_t d, const uint8_t *A, const uint8_t *W, int N) {
+  const uint32_t a = tc::smem_u32(A), b = tc::smem_u32(W);
+#pragma unroll
+  for (int kk = 0; kk < 8; ++kk) {
+    const uint32_t ao = (uint32_t)(kk >> 2) * 16384u + (uint32_t)(kk & 3) * 32u;
+    tc::mma_bf16(d, tc::desc_sw128(a + ao), tc::desc_sw128_mn(b + (uint32_t)kk * 2048u, 16384u),
+                 tc::idesc_bf16_mn(128, N, false, true), kk > 0 ? 1u : 0u);
+  }
+}
+
+// all threads: bounded wait on a commit barrier, then agree on the outcome
+__device__ __forceinline__ bool block_wait(uint64_t *bar, uint32_t &phase) {
+  const bool ok = tc::mbar_wait(bar, phase & 1u, kCvWaitNs);
+  ++phase;
+  const int bad = __syncthreads_or(!ok);
+  tc::fence_after_sync();
+  return bad == 0;
+}
+__device__ __forceinline__ void block_sync_async() {
+  tc::fence_proxy_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+}
+
+// ------------------------------------------------------------------ forward
+__global__ void __launch_bounds__(128, 1) cv_mlp_kernel(const __grid_constant__ CvMlpParams P) {
+  extern __shared__ uint8_t dyn[];
+  __shared__ __align__(8) uint64_t bar_w, bar_x[2], bar_mma;
+  __shared__ uint32_t tmem_base;
+  __shared__ float vec[kVecCount];
+  uint8_t *sm = align1024(dyn);
+  uint8_t *sW1 = sm + kImgW1, *sW2 = sm + kImgW2, *sW3 = sm + kImgW3, *sH = sm + kImgFwdBytes;
+  uint8_t *sX = sH + 32768;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  for (int i = tid; i < kVecCount; i += 128) vec[i] = P.vec[i];
+  if (tid == 0) {
+    tc::mbar_init(&bar_w, 1);
+    tc::mbar_init(&bar_x[0], 1);
+    tc::mbar_init(&bar_x[1], 1);
+    tc::mbar_init(&bar_mma, 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(&tmem_base, 128);
+    tc::tmem_relinquish();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tm = tmem_base;
+  const uint32_t tm_row = tm + ((uint32_t)(warp * 32) << 16);
+  const unsigned int n_mine = P.n_pb > blockIdx.x ? (P.n_pb - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  const unsigned long long total = (unsigned long long)n_mine * P.n_hedge;
+  auto tile_of = [&](unsigned long long t) {
+    return ((unsigned long long)blockIdx.x + (t / P.n_hedge) * gridDim.x) * P.n_hedge + t % P.n_hedge;
+  };
+  int pending = -1;  // x buffer with a bulk copy in flight (thread 0) and its phase parity
+  uint32_t pending_parity = 0;
+  if (tid == 0) {
+    tc::mbar_arrive_expect_tx(&bar_w, kImgFwdBytes);
+    tc::bulk_g2s(sm, P.img, kImgFwdBytes, &bar_w);
+    if (total > 0) {
+      tc::mbar_arrive_expect_tx(&bar_x[0], kCvTileBytes);
+      tc::bulk_g2s(sX, P.feat + tile_of(0) * kCvTileBytes, kCvTileBytes, &bar_x[0]);
+      pending = 0;
+    }
+  }
+  bool ok = true;
+  if (tid == 0) ok = tc::mbar_wait(&bar_w, 0, kCvWaitNs);
+  bool err = __syncthreads_or(!ok) != 0;
+  uint32_t phase = 0;
+  float acc = 0.0f;
+  for (unsigned long long t = 0; t < total && !err; ++t) {
+    const unsigned long long tile = tile_of(t);
+    const unsigned int j = (unsigned int)(t % P.n_hedge);
+    if (tid == 0) {
+      if (t + 1 < total) {
+        const int nb = (int)((t + 1) & 1);
+        tc::mbar_arrive_expect_tx(&bar_x[nb], kCvTileBytes);
+        tc::bulk_g2s(sX + nb * kCvTileBytes, P.feat + tile_of(t + 1) * kCvTileBytes, kCvTileBytes, &bar_x[nb]);
+      }
+      ok = tc::mbar_wait(&bar_x[t & 1], (uint32_t)((t >> 1) & 1), kCvWaitNs);
+      pending = (t + 1 < total) ? (int)((t + 1) & 1) : -1;
+      pending_parity = (uint32_t)(((t + 1) >> 1) & 1);
+      if (ok) {
+        tc::fence_after_sync();
+        tc::mma_bf16(tm, tc::desc_img16(tc::smem_u32(sX + (t & 1) * kCvTileBytes)), tc::desc_img16(tc::smem_u32(sW1)),
+                     tc::idesc_bf16(128, 128), 0u);
+        tc::mma_commit(&bar_mma);
+      }
+    }
+    if (__syncthreads_or(!ok)) { err = true; break; }
+    if (!block_wait(&bar_mma, phase)) { err = true; break; }
+    epi_hidden(tm_row, vec + kVecB1, sH, (uint32_t)tid);
+    block_sync_async();
+    if (tid == 0) {
+      mma_k128(tm, sH, sW2, 128, 0u);
+      tc::mma_commit(&bar_mma);
+    }
+    if (!block_wait(&bar_mma, phase)) { err = true; break; }
+    epi_hidden(tm_row, vec + kVecB2, sH, (uint32_t)tid);
+    block_sync_async();
+    if (tid == 0) {
+      mma_k128(tm, sH, sW3, 128, 0u);
+      tc::mma_commit(&bar_mma);
+    }
+    if (!block_wait(&bar_mma, phase)) { err = true; break; }
+    const float g = epi_out(tm_row, vec);
+    const unsigned long long row = tile * 128ull + (unsigned long long)tid;
+    acc = fmaf(g, P.dM[row], acc);
+    if (P.g_out) P.g_out[row] = g;
+    if (j == P.n_hedge - 1) {
+      const unsigned long long pb = tile / P.n_hedge;
+      const unsigned long long path = pb * 128ull + (unsigned long long)tid;
+      if (path < P.n_paths) P.cv[path] = acc;
+      acc = 0.0f;
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+  }
+  if (err) {
+    if (tid == 0) {
+      atomicAdd(P.status + 2, 1u);
+      if (pending >= 0) tc::mbar_wait(&bar_x[pending], pending_parity, kCvWaitNs);
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_dealloc(tm, 128);
+}
+
+// ------------------------------------------------------------------ backward
+// column sums over the block's 128 rows of a per-row 32-vector; lane i of the
+// returned value holds the sum of column i (valid in every warp after the call
+// through `red`, [4][32] floats of shared memory)
+__device__ __forceinline__ float colsum32(const float (&v)[32], float *red, int warp, int lane) {
+  float mine = 0.0f;
+#pragma unroll
+  for (int i = 0; i < 32; ++i) {
+    float s = v[i];
+    s += __shfl_xor_sync(0xffffffffu, s, 16);
+    s += __shfl_xor_sync(0xffffffffu, s, 8);
+    s += __shfl_xor_sync(0xffffffffu, s, 4);
+    s += __shfl_xor_sync(0xffffffffu, s, 2);
+    s += __shfl_xor_sync(0xffffffffu, s, 1);
+    if (lane == i) mine = s;
+  }
+  red[warp * 32 + lane] = mine;
+  __syncthreads();
+  const float tot = red[lane] + red[32 + lane] + red[64 + lane] + red[96 + lane];
+  __syncthreads();
+  return tot;
+}
+
+__device__ __forceinline__ void store_bf16_chunk(uint8_t *img, uint32_t row, int k0, const float *x) {
+  uint32_t w[4];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    __nv_bfloat162 p = __floats2bfloat162_rn(x[2 * e], x[2 * e + 1]);
+    w[e] = *reinterpret_cast<uint32_t *>(&p);
+  }
+  *reinterpret_cast<uint4 *>(img + tc::img128_offset(row, (uint32_t)k0, 128)) = make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+__global__ void __launch_bounds__(128, 1) cv_bwd_kernel(const __grid_constant__ CvMlpParams P) {
+  extern __shared__ uint8_t dyn[];
+  __shared__ __align__(8) uint64_t bar_w, bar_mma;
+  __shared__ uint32_t tmem_base;
+  __shared__ float vec[kVecCount];
+  __shared__ float red[128];
+  uint8_t *sm = align1024(dyn);
+  // [W1x64 16K][W2 32K][W3 32K][X64 16K][H1 32K][H2 32K][D 32K]
+  uint8_t *sW1 = sm, *sW2 = sm + 16384, *sW3 = sm + 49152, *sX = sm + 81920, *sH1 = sm + 98304;
+  uint8_t *sH2 = sm + 131072, *sD = sm + 163840;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int i = tid; i < kVecCount; i += 128) vec[i] = P.vec[i];
+  // padding chunks of the x image stay zero
+  for (int c = 2; c < 8; ++c)
+    *reinterpret_cast<uint4 *>(sX + tc::img128_offset((uint32_t)tid, (uint32_t)(c * 8), 128)) = make_uint4(0, 0, 0, 0);
+  if (tid == 0) {
+    tc::mbar_init(&bar_w, 1);
+    tc::mbar_init(&bar_mma, 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(&tmem_base, 512);
+    tc::tmem_relinquish();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tm = tmem_base;
+  const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+  const uint32_t T0 = tm, T1 = tm + 128, TW3 = tm + 256, TW2 = tm + 384;
+  if (tid == 0) {
+    tc::mbar_arrive_expect_tx(&bar_w, 16384u + 65536u);
+    tc::bulk_g2s(sW1, P.img + kImgW1x64, 16384u, &bar_w);
+    tc::bulk_g2s(sW2, P.img + kImgW2, 65536u, &bar_w);  // W2 and W3 are adjacent
+  }
+  bool ok = true;
+  if (tid == 0) ok = tc::mbar_wait(&bar_w, 0, kCvWaitNs);
+  bool err = __syncthreads_or(!ok) != 0;
+  const unsigned int n_mine = P.n_pb > blockIdx.x ? (P.n_pb - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  const unsigned long long total = (unsigned long long)n_mine * P.n_hedge;
+  uint32_t phase = 0;
+  float dw1[64];
+#pragma unroll
+  for (int i = 0; i < 64; ++i) dw1[i] = 0.0f;
+  float gb1 = 0.0f, gb2 = 0.0f, gb3 = 0.0f, gw4 = 0.0f, gb4 = 0.0f;
+  for (unsigned long long t = 0; t < total && !err; ++t) {
+    const unsigned long long pb = (unsigned long long)blockIdx.x + (t / P.n_hedge) * gridDim.x;
+    const unsigned long long tile = pb * P.n_hedge + t % P.n_hedge;
+    const unsigned long long row = tile * 128ull + (unsigned long long)tid;
+    const unsigned long long path = pb * 128ull + (unsigned long long)tid;
+    const float dg = path < P.n_paths ? P.coef[path] * P.dM[row] : 0.0f;
+    {  // x row -> X64 image (features 0..15; 16..63 stay zero)
+      const uint8_t *ft = P.feat + tile * kCvTileBytes;
+      *reinterpret_cast<uint4 *>(sX + tc::img128_offset((uint32_t)tid, 0, 128)) =
+          *reinterpret_cast<const uint4 *>(ft + tc::img16_offset((uint32_t)tid, 0));
+      *reinterpret_cast<uint4 *>(sX + tc::img128_offset((uint32_t)tid, 8, 128)) =
+          *reinterpret_cast<const uint4 *>(ft + tc::img16_offset((uint32_t)tid, 8));
+    }
+    block_sync_async();
+    // F1: z1 = x W1^T (K = 64)
+    if (tid == 0) {
+      const uint32_t a = tc::smem_u32(sX), b = tc::smem_u32(sW1);
+      for (int kk = 0; kk < 4; ++kk)
+        tc::mma_bf16(T0, tc::desc_sw128(a + (uint32_t)kk * 32u), tc::desc_sw128(b + (uint32_t)kk * 32u),
+                     tc::idesc_bf16(128, 128), kk > 0 ? 1u : 0u);
+      tc::mma_commit(&bar_mma);
+    }
+    if (!block_wait(&bar_mma, phase)) { err = true; break; }
+    epi_hidden(T0 + lane_off, vec + kVecB1, sH1, (uint32_t)tid);
+    block_sync_async();
+    // F2: z2 = h1 W2^T
+    if (tid == 0) {
+      mma_k128(T0, sH1, sW2, 128, 0u);
+      tc::mma_commit(&bar_mma);
+    }
+    if (!block_wait(&bar_mma, phase)) { err = true; break; }
+    epi_hidden(T0 + lane_off, vec + kVecB2, sH2, (uint32_t)tid);
+    block_sync_async();
+    // F3: z3 = h2 W3^T
+    if (tid == 0) {
+      mma_k128(T0, sH2, sW3, 128, 0u);
+      tc::mma_commit(&bar_mma);
+    }
+    if (!block_wait(&bar_mma, phase)) { err = true; break; }
+    // e3: dz3 = dg w4 silu'(z3 + b3) -> D; gradients of b3, w4, b4
+    gb4 += dg;
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
+      float v[32], dz[32], hw[32];
+      tc::tmem_ld32(T0 + lane_off + (uint32_t)(c * 32), v);
+#pragma unroll
+      for (int i = 0; i < 32; ++i) {
+        const int k = c * 32 + i;
+        const float z = v[i] + vec[kVecB3 + k];
+        dz[i] = dg * vec[kVecW4 + k] * tc::silu_grad(z);
+        hw[i] = dg * tc::silu(z);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) store_bf16_chunk(sD, (uint32_t)tid, c * 32 + q * 8, dz + q * 8);
+      const float s3 = colsum32(dz, red, warp, lane);
+      const float s4 = colsum32(hw, red, warp, lane);
+      if (warp == c) {
+        gb3 += s3;
+        gw4 += s4;
+      }
+    }
+    block_sync_async();
+    // B3: dh2 = dz3 W3 -> T0; dW3 += dz3^T h2 -> TW3; z2 again -> T1
+    if (tid == 0) {
+      mma_nn(T0, sD, sW3, 128);
+      mma_tn_rows(TW3, sD, sH2, 128, t > 0 ? 1u : 0u);
+      mma_k128(T1, sH1, sW2, 128, 0u);
+      tc::mma_commit(&bar_mma);
+    }
+    if (!block_wait(&bar_mma, phase)) { err = true; break; }
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
+      float dh[32], z[32], dz[32];
+      tc::tmem_ld32(T0 + lane_off + (uint32_t)(c * 32), dh);
+      tc::tmem_ld32(T1 + lane_off + (uint32_t)(c * 32), z);
+#pragma unroll
+      for (int i = 0; i < 32; ++i) dz[i] = dh[i] * tc::silu_grad(z[i] + vec[kVecB2 + c * 32 + i]);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) store_bf16_chunk(sD, (uint32_t)tid, c * 32 + q * 8, dz + q * 8);
+      const float s2 = colsum32(dz, red, warp, lane);
+      if (warp == c) gb2 += s2;
+    }
+    block_sync_async();
+    // B2: dh1 = dz2 W2 -> T0; dW2 += dz2^T h1 -> TW2; z1 again -> T1
+    if (tid == 0) {
+      mma_nn(T0, sD, sW2, 128);
+      mma_tn_rows(TW2, sD, sH1, 128, t > 0 ? 1u : 0u);
+      const uint32_t a = tc::smem_u32(sX), b = tc::smem_u32(sW1);
+      for (int kk = 0; kk < 4; ++kk)
+        tc::mma_bf16(T1, tc::desc_sw128(a + (uint32_t)kk * 32u), tc::desc_sw128(b + (uint32_t)kk * 32u),
+                     tc::idesc_bf16(128, 128), kk > 0 ? 1u : 0u);
+      tc::mma_commit(&bar_mma);
+    }
+    if (!block_wait(&bar_mma, phase)) { err = true; break; }
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
+      float dh[32], z[32], dz[32];
+      tc::tmem_ld32(T0 + lane_off + (uint32_t)(c * 32), dh);
+      tc::tmem_ld32(T1 + lane_off + (uint32_t)(c * 32), z);
+#pragma unroll
+      for (int i = 0; i < 32; ++i) dz[i] = dh[i] * tc::silu_grad(z[i] + vec[kVecB1 + c * 32 + i]);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) store_bf16_chunk(sD, (uint32_t)tid, c * 32 + q * 8, dz + q * 8);
+      const float s1 = colsum32(dz, red, warp, lane);
+      if (warp == c) gb1 += s1;
+    }
+    block_sync_async();
+    // B1: dW1 (tile) = dz1^T x -> T0 columns 0..63
+    if (tid == 0) {
+      mma_tn_rows(T0, sD, sX, 64, 0u);
+      tc::mma_commit(&bar_mma);
+    }
+    if (!block_wait(&bar_mma, phase)) { err = true; break; }
+    {
+      float v[32];
+      tc::tmem_ld32(T0 + lane_off, v);
+#pragma unroll
+      for (int i = 0; i < 32; ++i) dw1[i] += v[i];
+      tc::tmem_ld32(T0 + lane_off + 32u, v);
+#pragma unroll
+      for (int i = 0; i < 32; ++i) dw1[32 + i] += v[i];
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+  }
+  if (!err && total > 0) {
+    // flush: thread o owns output row o of dW2, dW3 (TMEM lane o) and dW1 (registers)
+    float *gr = P.grad;
+    for (int c = 0; c < 4; ++c) {
+      float v[32];
+      tc::tmem_ld32(TW3 + lane_off + (uint32_t)(c * 32), v);
+      for (int i = 0; i < 32; ++i) atomicAdd(gr + kPW3 + tid * 128 + c * 32 + i, v[i]);
+      tc::tmem_ld32(TW2 + lane_off + (uint32_t)(c * 32), v);
+      for (int i = 0; i < 32; ++i) atomicAdd(gr + kPW2 + tid * 128 + c * 32 + i, v[i]);
+    }
+    for (int i = 0; i < kCvIn; ++i) atomicAdd(gr + kPW1 + tid * kCvIn + i, dw1[i]);
+    // bias / output-layer sums: warp c holds columns c*32 + lane
+    atomicAdd(gr + kPB1 + tid, gb1);
+    atomicAdd(gr + kPB2 + tid, gb2);
+    atomicAdd(gr + kPB3 + tid, gb3);
+    atomicAdd(gr + kPW4 + tid, gw4);
+    float s = gb4;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) atomicAdd(gr + kPB4, s);
+  }
+  if (err && tid == 0) atomicAdd(P.status + 2, 1u);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_dealloc(tm, 512);
+}
+
+// ------------------------------------------------------------------ small kernels
+// FP32 parameters -> BF16 images and the FP32 vectors
+__global__ void cv_pack_kernel(const float *p, uint8_t *img, float *vec) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < 128 * kCvIn) {  // W1 [o][k]
+    const int o = i / kCvIn, k = i % kCvIn;
+    const __nv_bfloat16 b = __float2bfloat16_rn(p[kPW1 + i]);
+    *reinterpret_cast<__nv_bfloat16 *>(img + kImgW1 + tc::img16_offset(o, k)) = b;
+    *reinterpret_cast<__nv_bfloat16 *>(img + kImgW1x64 + tc::img128_offset(o, k, 128)) = b;
+  }
+  if (i < 128 * 64 && (i % 64) >= kCvIn) {  // W1x64 padding
+    const int o = i / 64, k = i % 64;
+    *reinterpret_cast<__nv_bfloat16 *>(img + kImgW1x64 + tc::img128_offset(o, k, 128)) = __float2bfloat16_rn(0.0f);
+  }
+  if (i < 128 * 128) {
+    const int o = i / 128, k = i % 128;
+    *reinterpret_cast<__nv_bfloat16 *>(img + kImgW2 + tc::img128_offset(o, k, 128)) = __float2bfloat16_rn(p[kPW2 + i]);
+    *reinterpret_cast<__nv_bfloat16 *>(img + kImgW3 + tc::img128_offset(o, k, 128)) = __float2bfloat16_rn(p[kPW3 + i]);
+  }
+  if (i < 128) {
+    vec[kVecB1 + i] = p[kPB1 + i];
+    vec[kVecB2 + i] = p[kPB2 + i];
+    vec[kVecB3 + i] = p[kPB3 + i];
+    vec[kVecW4 + i] = p[kPW4 + i];
+  }
+  if (i == 0) vec[kVecB4] = p[kPB4];
+}
+
+// Adam (bias-corrected): b1t = 1 - beta1^t, b2t = 1 - beta2^t
+__global__ void cv_adam_kernel(float *p, float *m, float *v, const float *g, float lr, float b1t, float b2t) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kPCount) return;
+  const float gi = g[i];
+  const float mi = fmaf(0.9f, m[i], 0.1f * gi);
+  const float vi = fmaf(0.999f, v[i], 0.001f * gi * gi);
+  m[i] = mi;
+  v[i] = vi;
+  p[i] -= lr * (mi / b1t) / (sqrtf(vi / b2t) + 1e-8f);
+}
+
+// r_p = Y_p - C_p - mean(Y - C); coef_p = dL/dC_p = -2 r_p / n; loss = mean r^2.
+// One block of 1024 threads.
+__global__ void cv_resid_kernel(const float *Y, const float *cv, unsigned long long n, float *coef, double *loss) {
+  __shared__ double red[32];
+  __shared__ double mean_sh;
+  double s = 0.0;
+  for (unsigned long long i = threadIdx.x; i < n; i += blockDim.x) s += (double)Y[i] - (double)cv[i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    mean_sh = t / (double)n;
+  }
+  __syncthreads();
+  const double mu = mean_sh;
+  double ss = 0.0;
+  for (unsigned long long i = threadIdx.x; i < n; i += blockDim.x) {
+    const double r = (double)Y[i] - (double)cv[i] - mu;
+    ss += r * r;
+    coef[i] = (float)(-2.0 * r / (double)n);
+  }
+  __syncthreads();
+  for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = ss;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    *loss = t / (double)n;
+  }
+}
+
+// sums4 += {sum Y, sum Y^2, sum (Y - C), sum (Y - C)^2} (FP64, per-block partials + atomics)
+__global__ void cv_reduce_kernel(const float *Y, const float *cv, unsigned long long n, double *sums4) {
+  double a[4] = {0.0, 0.0, 0.0, 0.0};
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    const double y = Y[i], z = (double)Y[i] - (double)cv[i];
+    a[0] += y;
+    a[1] += y * y;
+    a[2] += z;
+    a[3] += z * z;
+  }
+  __shared__ double red[4][8];
+  for (int q = 0; q < 4; ++q) {
+    double s = a[q];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[threadIdx.x][w];
+    atomicAdd(sums4 + threadIdx.x, t);
+  }
+}
+
+}  // namespace dev
+
+static constexpr uint32_t kFwdSmem = kImgFwdBytes + 32768u + 2u * kCvTileBytes + 1024u;
+static constexpr uint32_t kBwdSmem = 196608u + 1024u;
+
+cudaError_t launch_cv_mlp(const CvMlpParams &P, unsigned int blocks, cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(dev::cv_mlp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  dev::cv_mlp_kernel<<<blocks, 128, kFwdSmem, st>>>(P);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cv_bwd(const CvMlpParams &P, unsigned int blocks, cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(dev::cv_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  dev::cv_bwd_kernel<<<blocks, 128, kBwdSmem, st>>>(P);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cv_pack(const float *params, uint8_t *img, float *vec, cudaStream_t st) {
+  dev::cv_pack_kernel<<<(128 * 128 + 255) / 256, 256, 0, st>>>(params, img, vec);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cv_adam(float *params, float *m, float *v, const float *grad, float lr, float b1t, float b2t,
+                           cudaStream_t st) {
+  dev::cv_adam_kernel<<<(kPCount + 255) / 256, 256, 0, st>>>(params, m, v, grad, lr, b1t, b2t);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cv_resid(const float *Y, const float *cv, unsigned long long n, float *coef, double *loss_out,
+                            cudaStream_t st) {
+  dev::cv_resid_kernel<<<1, 1024, 0, st>>>(Y, cv, n, coef, loss_out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cv_reduce(const float *Y, const float *cv, unsigned long long n, double *sums4,
+                             cudaStream_t st) {
+  dev::cv_reduce_kernel<<<1216, 256, 0, st>>>(Y, cv, n, sums4);
+  return cudaGetLastError();
+}
+
+}  // namespace myql

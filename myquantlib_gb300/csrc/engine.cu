@@ -272,7 +272,7 @@ unsigned long long u999_threshold() {
   return x;
 }
 
-myql_status make_plan(const myql_mc_job &job, Plan &pl) {
+myql_status make_plan(const myql_mc_job &job, Plan &pl, bool stepped) {
   const myql_model &m = job.model;
   const myql_instrument &in = job.instrument;
   const myql_mc_config &c = job.config;
@@ -280,7 +280,7 @@ myql_status make_plan(const myql_mc_job &job, Plan &pl) {
   pl.s1 = pl.nf >= 1 ? c.scheme[0] : 0;
   pl.s2 = pl.nf >= 2 ? c.scheme[1] : 0;
   pl.tracker = tracker_of(in);
-  pl.path_dep = pl.tracker != TRK_EUROPEAN;
+  pl.path_dep = pl.tracker != TRK_EUROPEAN || stepped;
   pl.n_fields = tracker_fields(pl.tracker);
   pl.mode = c.greek_mode;
   pl.M = c.num_paths;

@@ -112,7 +112,8 @@ struct Plan {
 // planning helpers (engine.cu)
 int tracker_of(const myql_instrument &in);
 myql_status validate_job(const myql_mc_job &job);
-myql_status make_plan(const myql_mc_job &job, Plan &pl);
+// stepped: per-step GBM and jump constants even for Europeans (control variates)
+myql_status make_plan(const myql_mc_job &job, Plan &pl, bool stepped = false);
 void fill_factor(FactorConst &fc, const myql_heston_params &h, double v0, int scheme, double r_part,
                  double dt);
 unsigned long long u999_threshold();

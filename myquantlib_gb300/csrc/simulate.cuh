@@ -99,11 +99,26 @@ __device__ __forceinline__ float jump_draw(const SimParams &P, const ScenarioCon
   return C.jump_comp + total;
 }
 
+// Observer of a path's steps (the control-variate kernels record hedge-time
+// states and martingale increments through it).  NoHook compiles away.
+struct NoHook {
+  static constexpr bool active = false;
+  __device__ __forceinline__ void begin(float, float) {}
+  // log-spot increment of the step: root * G + drift, G ~ N(0,1) independent of the variances
+  __device__ __forceinline__ void diffusion(float, float, float) {}
+  __device__ __forceinline__ void jump(float) {}
+  // after step k (1-based): log-spot, variances, tracker accumulator
+  __device__ __forceinline__ void step_end(int, float, float, float, float) {}
+  __device__ __forceinline__ void finish() {}
+};
+
 // Simulates one path of one scenario; writes the tracker's terminal record.
-template <int NF, int S1, int S2, bool PD>
-__device__ __forceinline__ void sim_path(const SimParams &P, const ScenarioConst &C, Xo &rng,
-                                         float (&out)[kMaxFields], unsigned int &caphits,
-                                         unsigned int &fallbacks) {
+// With an active hook every path is stepped (no single-draw GBM European) and
+// the hook sees each step.
+template <int NF, int S1, int S2, bool PD, class Hook>
+__device__ __forceinline__ void sim_path_h(const SimParams &P, const ScenarioConst &C, Xo &rng,
+                                           float (&out)[kMaxFields], unsigned int &caphits,
+                                           unsigned int &fallbacks, Hook &hook) {
   float X = 0.0f;
   float va = C.f[0].v0, vb = C.f[1].v0;
   const int trk = P.tracker;
@@ -121,7 +136,8 @@ __device__ __forceinline__ void sim_path(const SimParams &P, const ScenarioConst
     }
   }
   const int n = P.n_steps;
-  if (NF == 0 && !PD) {
+  if (Hook::active) hook.begin(va, vb);
+  if (NF == 0 && !PD && !Hook::active) {
     // GBM European: one Gaussian over T plus one jump (ASVJstepper.hpp:145-161)
     const float G = inv_normal_bits(draw(rng));
     X = fmaf(C.gbm_vol, G, C.gbm_drift);
@@ -132,11 +148,14 @@ __device__ __forceinline__ void sim_path(const SimParams &P, const ScenarioConst
       const float G = inv_normal_bits(draw(rng));
       if (NF == 0) {
         X += fmaf(C.gbm_vol, G, C.gbm_drift);
+        if (Hook::active) hook.diffusion(C.gbm_vol, G, C.gbm_drift);
       } else if (NF == 1) {
         const FactorConst &f = C.f[0];
         const float vn = evolve<S1>(va, rng, f, P, 0, caphits, fallbacks);
         const float root = sqrt_approx(f.C3 * (va + vn));
-        X += fmaf(root, G, fmaf(f.C2, vn, fmaf(f.C1, va, f.C0)));
+        const float drift = fmaf(f.C2, vn, fmaf(f.C1, va, f.C0));
+        X += fmaf(root, G, drift);
+        if (Hook::active) hook.diffusion(root, G, drift);
         va = vn;
       } else {
         const FactorConst &f0 = C.f[0];
@@ -147,11 +166,16 @@ __device__ __forceinline__ void sim_path(const SimParams &P, const ScenarioConst
         const float drift = fmaf(f1.C2, vbn, fmaf(f1.C1, vb, fmaf(f0.C2, van,
                                  fmaf(f0.C1, va, f0.C0 + f1.C0))));
         X += fmaf(root, G, drift);
+        if (Hook::active) hook.diffusion(root, G, drift);
         va = van;
         vb = vbn;
       }
       if (PD) {
-        if (P.jump_kind) X += jump_draw(P, C, rng, caphits);
+        if (P.jump_kind) {
+          const float J = jump_draw(P, C, rng, caphits);
+          X += J;
+          if (Hook::active) hook.jump(J);
+        }
         const float t = (float)(k + 1) * dt;
         switch (trk) {
           case TRK_GEO_ASIAN: acc += X; break;
@@ -173,9 +197,15 @@ __device__ __forceinline__ void sim_path(const SimParams &P, const ScenarioConst
           default: break;
         }
       }
+      if (Hook::active) hook.step_end(k + 1, X, va, vb, acc);
     }
-    if (!PD && NF > 0 && P.jump_kind) X += jump_draw(P, C, rng, caphits);
+    if (!PD && (NF > 0 || Hook::active) && P.jump_kind) {
+      const float J = jump_draw(P, C, rng, caphits);
+      X += J;
+      if (Hook::active) hook.jump(J);
+    }
   }
+  if (Hook::active) hook.finish();
   out[0] = X;
   if (PD) {
     switch (trk) {
@@ -194,6 +224,14 @@ __device__ __forceinline__ void sim_path(const SimParams &P, const ScenarioConst
       default: break;
     }
   }
+}
+
+template <int NF, int S1, int S2, bool PD>
+__device__ __forceinline__ void sim_path(const SimParams &P, const ScenarioConst &C, Xo &rng,
+                                         float (&out)[kMaxFields], unsigned int &caphits,
+                                         unsigned int &fallbacks) {
+  NoHook h;
+  sim_path_h<NF, S1, S2, PD>(P, C, rng, out, caphits, fallbacks, h);
 }
 
 template <int NF, int S1, int S2, bool PD>

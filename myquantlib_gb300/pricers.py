@@ -451,6 +451,49 @@ class Engine:
         _abi.check(self.lib.myql_mc_price_batch(self.handle, arr, n, ptrs, C.byref(st)))
         return [o.reshape(2 * _abi.Q_COUNT, 1) for o in outs], st
 
+    # ---- neural control variate
+    def cv_init(self, seed: int = 1):
+        _abi.check(self.lib.myql_cv_init(self.handle, seed))
+
+    def cv_params(self) -> np.ndarray:
+        out = np.zeros(_abi.CV_PARAMS, dtype=np.float32)
+        _abi.check(self.lib.myql_cv_get_params(self.handle, _fptr(out), out.size))
+        return out
+
+    def cv_set_params(self, params) -> None:
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        if p.size != _abi.CV_PARAMS:
+            raise ValueError(f"need {_abi.CV_PARAMS} parameters")
+        _abi.check(self.lib.myql_cv_set_params(self.handle, _fptr(p), p.size))
+
+    def cv_forward(self, feats, dM, n_paths: int, n_hedge: int) -> tuple[np.ndarray, np.ndarray]:
+        f = np.ascontiguousarray(feats, dtype=np.float32)
+        d = np.ascontiguousarray(dM, dtype=np.float32)
+        cv = np.zeros(n_paths, dtype=np.float32)
+        g = np.zeros(n_paths * n_hedge, dtype=np.float32)
+        _abi.check(self.lib.myql_cv_forward(self.handle, _fptr(f), _fptr(d), n_paths, n_hedge, _fptr(cv), _fptr(g)))
+        return cv, g
+
+    def cv_gradient(self, feats, dM, Y, n_paths: int, n_hedge: int) -> tuple[float, np.ndarray]:
+        f = np.ascontiguousarray(feats, dtype=np.float32)
+        d = np.ascontiguousarray(dM, dtype=np.float32)
+        y = np.ascontiguousarray(Y, dtype=np.float32)
+        grad = np.zeros(_abi.CV_PARAMS, dtype=np.float32)
+        loss = C.c_double()
+        _abi.check(self.lib.myql_cv_gradient(self.handle, _fptr(f), _fptr(d), _fptr(y), n_paths, n_hedge,
+                                             _fptr(grad), C.byref(loss)))
+        return loss.value, grad
+
+    def cv_train(self, job: "_Job", cfg: "_abi.CvConfigC") -> "_abi.CvResultC":
+        res = _abi.CvResultC()
+        _abi.check(self.lib.myql_cv_train(self.handle, C.byref(job.c), C.byref(cfg), C.byref(res)))
+        return res
+
+    def cv_price(self, job: "_Job", cfg: "_abi.CvConfigC") -> "_abi.CvResultC":
+        res = _abi.CvResultC()
+        _abi.check(self.lib.myql_cv_price(self.handle, C.byref(job.c), C.byref(cfg), C.byref(res)))
+        return res
+
     def paths(self, job: "_Job") -> np.ndarray:
         nsc, nf = C.c_uint32(), C.c_uint32()
         _abi.check(self.lib.myql_mc_paths(self.handle, C.byref(job.c), None, 0, C.byref(nsc),
@@ -500,6 +543,10 @@ class Engine:
 
 def _ptr(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _fptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
 
 
 _default_engine: Engine | None = None
@@ -649,3 +696,64 @@ class MonteCarloPricer:
         eng = self.engine or default_engine()
         raw, st = eng.price(self.job(S0, r, q, instr))
         return result_from_raw(raw, self.mode, instr.is_strip, st)
+
+
+@dataclass
+class ControlVariateConfig:
+    """Settings of the neural martingale control variate (no counterpart in the reference)."""
+    hedge_every: int = 8          # time steps per hedge interval
+    iterations: int = 300         # Adam steps
+    pilot_paths: int = 1 << 18    # training paths (independent seed)
+    batch_paths: int = 8192       # paths per Adam step
+    learning_rate: float = 2e-3
+    seed: int = 1
+
+    def c(self) -> _abi.CvConfigC:
+        c = _abi.CvConfigC()
+        c.hedge_every, c.iterations, c.pilot_paths = self.hedge_every, self.iterations, self.pilot_paths
+        c.batch_paths, c.learning_rate, c.seed = self.batch_paths, self.learning_rate, self.seed
+        return c
+
+
+@dataclass
+class ControlVariateResult:
+    price: float
+    price_std_err: float
+    plain_price: float
+    plain_std_err: float
+    variance_ratio: float
+    train: object = None
+    raw: object = None
+
+
+class NeuralCVPricer:
+    """MonteCarloPricer with a learned martingale control variate (GreekMode::None).
+
+    `train(S0, r, q, instrument)` fits the network on pilot paths of the model;
+    `calculate(S0, r, q, instrument)` prices with it and also reports the plain
+    Monte Carlo estimator of the same paths.  Scalar European / Asian instruments.
+    """
+
+    def __init__(self, model, stepper: ASVJStepper | None = None, cfg: MonteCarloConfig | None = None,
+                 cv: ControlVariateConfig | None = None, engine: Engine | None = None):
+        self.model, self.stepper = model, stepper
+        self.cfg = cfg or MonteCarloConfig()
+        self.cv = cv or ControlVariateConfig()
+        self.engine = engine
+        self.train_result = None
+
+    def _job(self, S0, r, q, instr):
+        return make_job(self.model, self.stepper, instr, GreekMode.NONE, self.cfg, S0, r, q)
+
+    def train(self, S0: float, r: float, q: float, instr: _Instrument):
+        eng = self.engine or default_engine()
+        self.train_result = eng.cv_train(self._job(S0, r, q, instr), self.cv.c())
+        return self.train_result
+
+    def calculate(self, S0: float, r: float, q: float, instr: _Instrument) -> ControlVariateResult:
+        eng = self.engine or default_engine()
+        if self.train_result is None:
+            self.train(S0, r, q, instr)
+        res = eng.cv_price(self._job(S0, r, q, instr), self.cv.c())
+        return ControlVariateResult(res.price, res.price_std_err, res.plain_price, res.plain_std_err,
+                                    res.variance_ratio, self.train_result, res)

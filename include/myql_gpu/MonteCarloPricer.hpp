@@ -244,6 +244,7 @@ template <typename PayoffPolicy, typename StrikeContainer = double> class Europe
   double get_maturity() const { return T_; }
   void lower(myql_instrument &in) const {
     in.kind = MYQL_INSTR_EUROPEAN;
+    in.fixed_strike = 1;  // a strike-vs-terminal payoff
     in.payoff = PayoffPolicy::code;
     in.option_type = PayoffPolicy::Type == OptionType::Call ? MYQL_CALL : MYQL_PUT;
     in.payoff_eps = payoff_func_.eps;
@@ -322,6 +323,7 @@ class BarrierOption {
   double get_maturity() const { return T_; }
   void lower(myql_instrument &in) const {
     in.kind = MYQL_INSTR_BARRIER;
+    in.fixed_strike = 1;
     in.payoff = PayoffT::code;
     in.option_type = PayoffT::Type == OptionType::Call ? MYQL_CALL : MYQL_PUT;
     in.payoff_eps = payoff_func_.eps;

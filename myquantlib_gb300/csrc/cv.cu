@@ -129,6 +129,41 @@ myql_status cv_plan(CtxBase *ctx, const myql_mc_job &job, const myql_cv_config &
   C.vb_scale = pl.nf >= 2 ? (float)(1.0 / std::max(job.model.heston[1].theta, 1e-4)) : 0.0f;
   C.S0 = (float)job.S0;
   klass = batch_class(pl.nf, pl.s1, pl.s2);
+  // conditional mean of e^{dX} per step, from the FP32 constants the kernel steps with
+  const ScenarioConst &sc = pl.sim.sc[0];
+  double A = 0.0, B[2] = {0.0, 0.0};
+  if (pl.nf == 0) {
+    A = (double)sc.gbm_drift + 0.5 * (double)sc.gbm_vol * (double)sc.gbm_vol;
+  } else {
+    for (int f = 0; f < pl.nf; ++f) {
+      const FactorConst &fc = sc.f[f];
+      const double C0 = fc.C0, C1 = fc.C1, C2 = fc.C2, C3 = fc.C3, w0 = fc.w0, w1 = fc.w1, w2 = fc.w2;
+      const double u = C2 + 0.5 * C3;  // exponent of v' in e^{dX} after averaging over G
+      double alpha = 0.0, beta = 0.0;
+      const int sch = job.config.scheme[f];
+      if (sch == MYQL_SCHEME_NV) {  // v' = w0 (sqrt(w0 v + w1) + w2 Z)^2 + w1
+        const double den = 1.0 - 2.0 * u * w0 * w2 * w2;
+        if (!(den > 0.0)) return set_error(MYQL_ERR_UNSUPPORTED, "E[S_T] is infinite under this discretisation");
+        alpha = u * w0 * w0 / den;
+        beta = u * w1 + u * w0 * w1 / den - 0.5 * std::log(den);
+      } else if (sch == MYQL_SCHEME_EXACT) {  // v' = Gamma(w1 + N) w2, N ~ Poisson(w0 v)
+        const double den = 1.0 - u * w2;
+        if (!(den > 0.0)) return set_error(MYQL_ERR_UNSUPPORTED, "E[S_T] is infinite under this discretisation");
+        alpha = w0 * u * w2 / den;
+        beta = -w1 * std::log(den);
+      } else {  // NCI: v' = chi2_{w1 + 2N} w2, N ~ Poisson(w0 v)
+        const double den = 1.0 - 2.0 * u * w2;
+        if (!(den > 0.0)) return set_error(MYQL_ERR_UNSUPPORTED, "E[S_T] is infinite under this discretisation");
+        alpha = w0 * 2.0 * u * w2 / den;
+        beta = -0.5 * w1 * std::log(den);
+      }
+      A += C0 + beta;
+      B[f] = C1 + 0.5 * C3 + alpha;
+    }
+  }
+  C.mu_A = (float)A;
+  C.mu_Ba = (float)B[0];
+  C.mu_Bb = (float)B[1];
   return MYQL_OK;
 }
 
@@ -163,8 +198,9 @@ myql_status simulate_chunks(CtxBase *ctx, CvSimParams C, int klass, uint64_t see
   return MYQL_OK;
 }
 
-unsigned int mlp_blocks(const CtxBase *ctx, uint64_t n_pb) {
-  return (unsigned int)std::max<uint64_t>(1, std::min<uint64_t>(n_pb, (uint64_t)ctx->sm_count));
+// persistent grids: the forward kernel fits two blocks per SM, the backward one
+unsigned int mlp_blocks(const CtxBase *ctx, uint64_t n_pb, int per_sm = 1) {
+  return (unsigned int)std::max<uint64_t>(1, std::min<uint64_t>(n_pb, (uint64_t)ctx->sm_count * per_sm));
 }
 
 myql_status forward(CtxBase *ctx, CvState &S, const uint8_t *feat, const float *dM, uint64_t n_paths, uint32_t nh,
@@ -181,7 +217,7 @@ myql_status forward(CtxBase *ctx, CvState &S, const uint8_t *feat, const float *
   F.n_pb = (unsigned int)((n_paths + 127) / 128);
   F.n_hedge = nh;
   F.status = (unsigned int *)ctx->status.p;
-  cudaError_t e = launch_cv_mlp(F, mlp_blocks(ctx, F.n_pb), ctx->stream);
+  cudaError_t e = launch_cv_mlp(F, mlp_blocks(ctx, F.n_pb, 2), ctx->stream);
   ctx->launches++;
   return cuda_status(e, "cv_mlp launch");
 }
@@ -376,6 +412,21 @@ myql_status myql_cv_train(myql_ctx *ctx_, const myql_mc_job *job, const myql_cv_
   s = simulate_chunks(ctx, C, klass, pilot_seed, 0, P, Sp, (P + Sp - 1) / Sp * Sp, S.p_feat, S.p_dM, S.p_Y,
                       [](uint64_t) { return MYQL_OK; });
   if (s != MYQL_OK) return s;
+  // start from the best constant hedge: b4 = Cov(Y, S) / Var(S), S = sum_j dM_j
+  {
+    double m5[5] = {0, 0, 0, 0, 0};
+    e = cudaMemsetAsync(S.sums.p, 0, 40, ctx->stream);
+    if (e == cudaSuccess)
+      e = launch_cv_beta((const float *)S.p_Y.p, (const float *)S.p_dM.p, P, nh, (double *)S.sums.p, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(m5, S.sums.p, 40, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_status(e, "control-variate constant hedge");
+    const double n = (double)P, ms = m5[0] / n, my = m5[3] / n;
+    const double var_s = m5[1] / n - ms * ms, cov = m5[2] / n - my * ms;
+    p0[kPB4] = var_s > 0.0 ? (float)(cov / var_s) : 0.0f;
+    s = upload_params(ctx, S, p0.data());
+    if (s != MYQL_OK) return s;
+  }
   const uint64_t bp = std::min<uint64_t>(P, (cfg->batch_paths + 127) / 128 * 128);
   const uint64_t n_pb = P / 128, b_pb = bp / 128;
   e = S.p_cv.ensure(P * 4);

@@ -5,11 +5,14 @@
 //     C = sum_j g(state at t_j) * dM_j,
 // where dM_j is the martingale increment of the discounted asset
 // M_t = S_t e^{-(r-q) t} over the hedge interval [t_j, t_{j+1}).  Per step k
-// the increment is taken conditionally centred under the discrete scheme:
-//     dM_k = M_k e^{a_k} expm1(root G - root^2 / 2) + M_k' expm1(J_k),
-// with a_k = drift_k + root^2/2 - (r-q) dt, G independent of the variances and
-// E[e^{J}] = 1 (compensated jumps), so E[g_j dM_k] = 0 for any g_j that depends
-// on the path up to t_j: the estimator Y - C is unbiased whatever the network.
+// the increment is centred by its exact conditional mean under the discrete
+// scheme: with dX_k = C0 + C1 v + C2 v' + sqrt(C3 (v + v')) G (summed over the
+// factors) and the variance transition's moment generating function,
+//     log E[e^{dX_k} | v] = mu_k = A + B_1 v_1 + B_2 v_2        (affine in v)
+//     dM_k = M_k e^{mu_k - (r-q) dt} expm1(dX_k - mu_k) + M_k' expm1(J_k)
+// (E[e^{J}] = 1 for the compensated jumps), so E[g_j dM_k] = 0 for any g_j
+// that depends on the path up to t_j: the estimator Y - C is unbiased whatever
+// the network.
 //
 // Network: 16 input slots (6 used: t/T, x-scaled log-spot, scaled v1, v2, the
 // running average to date, 1) -> 128 -> 128 -> 128 (SiLU) -> 1, BF16 weights and
@@ -64,6 +67,7 @@ struct CvSimParams {
   int hedge_every, n_hedge;
   float rq_dt;          // (r - q) dt
   float inv_T, x_scale, va_scale, vb_scale, S0;
+  float mu_A, mu_Ba, mu_Bb;  // log E[e^{dX} | v] = mu_A + mu_Ba v1 + mu_Bb v2
 };
 
 struct CvMlpParams {
@@ -92,6 +96,7 @@ struct CvHook {
   uint32_t lane;
   int j, he, n;
   float m, m_mid, acc, dt;
+  float va_c, vb_c;  // variances at the start of the current step
 
   __device__ __forceinline__ void write_feat(int jj, float t, float X, float va, float vb, float avg) {
     __nv_bfloat162 p0 = __floats2bfloat162_rn(t * P->inv_T, X * P->x_scale);
@@ -116,16 +121,20 @@ struct CvHook {
     m = 1.0f;
     acc = 0.0f;
     j = 0;
+    va_c = va;
+    vb_c = vb;
     write_feat(0, 0.0f, 0.0f, va, vb, 0.0f);
   }
   __device__ __forceinline__ void diffusion(float root, float G, float drift) {
-    const float half_var = 0.5f * root * root;
-    const float a = drift + half_var - P->rq_dt;
-    acc = fmaf(m * __expf(a), expm1f(fmaf(root, G, -half_var)), acc);
-    m_mid = m * __expf(fmaf(root, G, drift) - P->rq_dt);
+    const float dx = fmaf(root, G, drift);
+    const float mu = fmaf(P->mu_Bb, vb_c, fmaf(P->mu_Ba, va_c, P->mu_A));
+    acc = fmaf(m * __expf(mu - P->rq_dt), expm1f(dx - mu), acc);
+    m_mid = m * __expf(dx - P->rq_dt);
   }
   __device__ __forceinline__ void jump(float J) { acc = fmaf(m_mid, expm1f(J), acc); }
   __device__ __forceinline__ void step_end(int k, float X, float va, float vb, float trk) {
+    va_c = va;
+    vb_c = vb;
     m = __expf(X - P->rq_dt * (float)k);
     if (k < n && k % he == 0) {
       dm0[(size_t)j * 128] = acc * P->S0;
@@ -161,6 +170,8 @@ cudaError_t launch_cv_adam(float *params, float *m, float *v, const float *grad,
                            cudaStream_t st);
 cudaError_t launch_cv_resid(const float *Y, const float *cv, unsigned long long n, float *coef, double *loss_out,
                             cudaStream_t st);
+cudaError_t launch_cv_beta(const float *Y, const float *dM, unsigned long long n, unsigned int n_hedge,
+                           double *sums5, cudaStream_t st);
 cudaError_t launch_cv_reduce(const float *Y, const float *cv, unsigned long long n, double *sums4,
                              cudaStream_t st);
 

@@ -32,10 +32,11 @@ __device__ __forceinline__ uint8_t *align1024(uint8_t *p) {
   return p + (((a + 1023u) & ~1023u) - a);
 }
 
-// z (TMEM, 128 columns of this thread's row) + bias -> SiLU -> BF16 IMG128 row of H
-__device__ __forceinline__ void epi_hidden(uint32_t tm_row, const float *bias, uint8_t *H, uint32_t row) {
+// z (TMEM, columns [32 c0, 32 c1) of this thread's row) + bias -> SiLU -> BF16 IMG128 row of H
+__device__ __forceinline__ void epi_hidden(uint32_t tm_row, const float *bias, uint8_t *H, uint32_t row, int c0 = 0,
+                                           int c1 = 4) {
 #pragma unroll 1
-  for (int c = 0; c < 4; ++c) {
+  for (int c = c0; c < c1; ++c) {
     float v[32];
     tc::tmem_ld32(tm_row + (uint32_t)(c * 32), v);
 #pragma unroll
@@ -54,11 +55,11 @@ __device__ __forceinline__ void epi_hidden(uint32_t tm_row, const float *bias, u
   }
 }
 
-// output layer: g = b4 + sum_k silu(z3_k + b3_k) w4_k
-__device__ __forceinline__ float epi_out(uint32_t tm_row, const float *vec) {
-  float g = vec[kVecB4];
+// output layer over columns [32 c0, 32 c1): sum_k silu(z3_k + b3_k) w4_k (+ b4 when c0 == 0)
+__device__ __forceinline__ float epi_out(uint32_t tm_row, const float *vec, int c0 = 0, int c1 = 4) {
+  float g = c0 == 0 ? vec[kVecB4] : 0.0f;
 #pragma unroll 1
-  for (int c = 0; c < 4; ++c) {
+  for (int c = c0; c < c1; ++c) {
     float v[32];
     tc::tmem_ld32(tm_row + (uint32_t)(c * 32), v);
 #pragma unroll
@@ -122,16 +123,23 @@ __device__ __forceinline__ void block_sync_async() {
 }
 
 // ------------------------------------------------------------------ forward
-__global__ void __launch_bounds__(128, 1) cv_mlp_kernel(const __grid_constant__ CvMlpParams P) {
+// 8 warps: warps w and w + 4 read the same TMEM lane quarter (rows 32 (w % 4) ..)
+// and take the low / high 64 columns of every layer.
+constexpr int kFwdThreads = 256;
+
+__global__ void __launch_bounds__(kFwdThreads, 2) cv_mlp_kernel(const __grid_constant__ CvMlpParams P) {
   extern __shared__ uint8_t dyn[];
   __shared__ __align__(8) uint64_t bar_w, bar_x[2], bar_mma;
   __shared__ uint32_t tmem_base;
   __shared__ float vec[kVecCount];
+  __shared__ float part[128];
   uint8_t *sm = align1024(dyn);
   uint8_t *sW1 = sm + kImgW1, *sW2 = sm + kImgW2, *sW3 = sm + kImgW3, *sH = sm + kImgFwdBytes;
   uint8_t *sX = sH + 32768;
   const int tid = threadIdx.x, warp = tid >> 5;
-  for (int i = tid; i < kVecCount; i += 128) vec[i] = P.vec[i];
+  const uint32_t row = (uint32_t)(tid & 127);
+  const int half = warp >> 2;  // column half: [64 half, 64 half + 64)
+  for (int i = tid; i < kVecCount; i += kFwdThreads) vec[i] = P.vec[i];
   if (tid == 0) {
     tc::mbar_init(&bar_w, 1);
     tc::mbar_init(&bar_x[0], 1);
@@ -147,7 +155,8 @@ __global__ void __launch_bounds__(128, 1) cv_mlp_kernel(const __grid_constant__ 
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tm = tmem_base;
-  const uint32_t tm_row = tm + ((uint32_t)(warp * 32) << 16);
+  const uint32_t tm_row = tm + ((uint32_t)((warp & 3) * 32) << 16);
+  const int c0 = 2 * half, c1 = 2 * half + 2;
   const unsigned int n_mine = P.n_pb > blockIdx.x ? (P.n_pb - 1 - blockIdx.x) / gridDim.x + 1 : 0;
   const unsigned long long total = (unsigned long long)n_mine * P.n_hedge;
   auto tile_of = [&](unsigned long long t) {
@@ -190,33 +199,37 @@ __global__ void __launch_bounds__(128, 1) cv_mlp_kernel(const __grid_constant__ 
     }
     if (__syncthreads_or(!ok)) { err = true; break; }
     if (!block_wait(&bar_mma, phase)) { err = true; break; }
-    epi_hidden(tm_row, vec + kVecB1, sH, (uint32_t)tid);
+    epi_hidden(tm_row, vec + kVecB1, sH, row, c0, c1);
     block_sync_async();
     if (tid == 0) {
       mma_k128(tm, sH, sW2, 128, 0u);
       tc::mma_commit(&bar_mma);
     }
     if (!block_wait(&bar_mma, phase)) { err = true; break; }
-    epi_hidden(tm_row, vec + kVecB2, sH, (uint32_t)tid);
+    epi_hidden(tm_row, vec + kVecB2, sH, row, c0, c1);
     block_sync_async();
     if (tid == 0) {
       mma_k128(tm, sH, sW3, 128, 0u);
       tc::mma_commit(&bar_mma);
     }
     if (!block_wait(&bar_mma, phase)) { err = true; break; }
-    const float g = epi_out(tm_row, vec);
-    const unsigned long long row = tile * 128ull + (unsigned long long)tid;
-    acc = fmaf(g, P.dM[row], acc);
-    if (P.g_out) P.g_out[row] = g;
-    if (j == P.n_hedge - 1) {
-      const unsigned long long pb = tile / P.n_hedge;
-      const unsigned long long path = pb * 128ull + (unsigned long long)tid;
-      if (path < P.n_paths) P.cv[path] = acc;
-      acc = 0.0f;
-    }
+    const float gpart = epi_out(tm_row, vec, c0, c1);
+    if (half == 1) part[row] = gpart;
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
+    if (half == 0) {
+      const float g = gpart + part[row];
+      const unsigned long long r = tile * 128ull + row;
+      acc = fmaf(g, P.dM[r], acc);
+      if (P.g_out) P.g_out[r] = g;
+      if (j == P.n_hedge - 1) {
+        const unsigned long long path = (tile / P.n_hedge) * 128ull + row;
+        if (path < P.n_paths) P.cv[path] = acc;
+        acc = 0.0f;
+      }
+    }
+    // the next tile's writes of `part` come after its three MMA waits, each a block barrier
   }
   if (err) {
     if (tid == 0) {
@@ -560,7 +573,37 @@ __global__ void cv_reduce_kernel(const float *Y, const float *cv, unsigned long 
   }
 }
 
+// Moments for the constant hedge that starts the training: per path
+// S_p = sum_j dM_pj; sums5 += {S, S^2, Y S, Y, Y^2}.
+__global__ void cv_beta_kernel(const float *Y, const float *dM, unsigned long long n, unsigned int n_hedge,
+                               double *sums5) {
+  double a[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  for (unsigned long long p = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; p < n;
+       p += (unsigned long long)gridDim.x * blockDim.x) {
+    const unsigned long long pb = p >> 7, lane = p & 127u;
+    double sp = 0.0;
+    for (unsigned int j = 0; j < n_hedge; ++j) sp += (double)dM[(pb * n_hedge + j) * 128ull + lane];
+    const double y = Y[p];
+    a[0] += sp;
+    a[1] += sp * sp;
+    a[2] += y * sp;
+    a[3] += y;
+    a[4] += y * y;
+  }
+  for (int q = 0; q < 5; ++q) {
+    double s = a[q];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(sums5 + q, s);
+  }
+}
+
 }  // namespace dev
+
+cudaError_t launch_cv_beta(const float *Y, const float *dM, unsigned long long n, unsigned int n_hedge,
+                           double *sums5, cudaStream_t st) {
+  dev::cv_beta_kernel<<<304, 256, 0, st>>>(Y, dM, n, n_hedge, sums5);
+  return cudaGetLastError();
+}
 
 static constexpr uint32_t kFwdSmem = kImgFwdBytes + 32768u + 2u * kCvTileBytes + 1024u;
 static constexpr uint32_t kBwdSmem = 196608u + 1024u;
@@ -569,10 +612,14 @@ cudaError_t launch_cv_mlp(const CvMlpParams &P, unsigned int blocks, cudaStream_
   static bool attr = false;
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(dev::cv_mlp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem);
+    // two blocks per SM (2 x ~113 KB) need the full shared-memory carveout
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(dev::cv_mlp_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               (int)cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  dev::cv_mlp_kernel<<<blocks, 128, kFwdSmem, st>>>(P);
+  dev::cv_mlp_kernel<<<blocks, dev::kFwdThreads, kFwdSmem, st>>>(P);
   return cudaGetLastError();
 }
 

@@ -120,7 +120,7 @@ def test_cv_heston_european_unbiased_and_gains(engine):
     res = engine.cv_price(heston_call_job(1 << 18), cfg)
     assert abs(res.plain_price - FOURIER_C1) < 4 * res.plain_std_err
     assert abs(res.price - FOURIER_C1) < 4 * res.price_std_err + 1e-3, (res.price, res.price_std_err)
-    assert res.variance_ratio > 5.0, res.variance_ratio
+    assert res.variance_ratio > 10.0, res.variance_ratio
 
 
 def test_cv_double_bates_asian_against_plain_engine(engine):
@@ -131,7 +131,7 @@ def test_cv_double_bates_asian_against_plain_engine(engine):
     ref, ref_se = raw[0, 0], raw[1, 0]
     assert abs(res.price - ref) < 4 * np.hypot(res.price_std_err, ref_se), (res.price, ref, res.price_std_err, ref_se)
     assert abs(res.plain_price - ref) < 4 * np.hypot(res.plain_std_err, ref_se)
-    assert res.variance_ratio > 3.0, res.variance_ratio
+    assert res.variance_ratio > 8.0, res.variance_ratio
 
 
 def test_cv_untrained_network_is_still_unbiased(engine):

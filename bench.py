@@ -372,6 +372,101 @@ def run_batch(args) -> dict:
     return line
 
 
+# ---------------------------------------------------------------- neural control variate
+CV_TARGETS = {"asian": 1e-3, "european": 1e-4}
+
+
+def cv_jobs(m, kind: str, paths: int, seed: int = 42):
+    """The control-variate workloads: the Double Bates arithmetic Asian call (factors
+    (v0 .03, kappa 2, theta .03, sigma .4, rho -.7) and (.02, .5, .02, .3, -.3), Merton
+    (.3, -.05, .1), K 100, T 2, 256 steps, SchemeNCI) and the Heston European call
+    (kappa 1.5, theta .04, sigma .3, rho -.7, v0 .04, K 100, T 1, 100 steps, SchemeNV)."""
+    if kind == "asian":
+        model = m.DoubleBatesModel(m.HestonParams(2.0, 0.03, 0.4, -0.7, 0.03),
+                                   m.HestonParams(0.5, 0.02, 0.3, -0.3, 0.02), m.MertonParams(0.3, -0.05, 0.1))
+        instr = m.AsianOption(m.TrackerArithAsian, m.PayoffVanilla(), True, 100.0, 2.0)
+        stepper = m.DoubleBatesStepper(m.SchemeNCI, m.SchemeNCI, m.TrackerArithAsian)
+        steps = 256
+    else:
+        model = m.HestonModel(m.HestonParams(1.5, 0.04, 0.3, -0.7, 0.04))
+        instr = m.EuropeanOption(100.0, 1.0)
+        stepper = m.HestonStepper(m.SchemeNV)
+        steps = 100
+    cfg = m.MonteCarloConfig(num_paths=paths, time_steps=steps, seed=seed)
+    return m.make_job(model, stepper, instr, m.GreekMode.NONE, cfg, 100.0, 0.02, 0.0), steps
+
+
+def cv_config(m, kind: str, pilot: int = 1 << 20, iterations: int = 250):
+    return m.pricers.ControlVariateConfig(hedge_every=8 if kind == "asian" else 5, iterations=iterations,
+                                          pilot_paths=pilot, batch_paths=8192, learning_rate=3e-3, seed=7).c()
+
+
+def time_to_se(eng, m, kind: str, probe_paths: int = 1 << 22) -> dict:
+    """Wall time until the relative standard error reaches the target, plain GPU Monte
+    Carlo against the neural control variate (its pilot simulation and training
+    included).  A probe run fixes each estimator's variance; each is then run again at
+    the path count that meets the target and timed end to end through the public API."""
+    import torch
+    target = CV_TARGETS[kind]
+    job, steps = cv_jobs(m, kind, probe_paths)
+    raw, _ = eng.price(job)
+    price, se = raw[0, 0], raw[1, 0]
+    n_plain = int(probe_paths * (se / (target * price)) ** 2) + 1
+    cfg = cv_config(m, kind)
+    t0 = time.perf_counter()
+    tr = eng.cv_train(cv_jobs(m, kind, 1 << 16)[0], cfg)
+    probe = eng.cv_price(cv_jobs(m, kind, probe_paths, seed=43)[0], cfg)
+    n_cv = int(probe_paths * (probe.price_std_err / (target * probe.price)) ** 2) + 1
+    # timed runs (fresh seeds), each through the public API, synchronised
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    raw, _ = eng.price(cv_jobs(m, kind, n_plain, seed=44)[0])
+    t_plain = time.perf_counter() - t0
+    rel_plain = raw[1, 0] / raw[0, 0]
+    t0 = time.perf_counter()
+    tr = eng.cv_train(cv_jobs(m, kind, 1 << 16, seed=45)[0], cfg)
+    res = eng.cv_price(cv_jobs(m, kind, max(n_cv, 128), seed=46)[0], cfg)
+    t_cv = time.perf_counter() - t0
+    return {"instrument": "Double Bates arithmetic Asian call" if kind == "asian" else "Heston European call",
+            "target_rel_se": target, "plain_paths": n_plain, "plain_s": t_plain, "plain_rel_se": rel_plain,
+            "plain_path_steps_per_s": n_plain * steps / t_plain,
+            "cv_paths": n_cv, "cv_s": t_cv, "cv_rel_se": res.price_std_err / res.price, "cv_train_s": tr.train_ms / 1e3,
+            "cv_pilot_paths": int(tr.paths), "cv_iterations": int(cfg.iterations),
+            "variance_ratio": res.variance_ratio, "speedup": t_plain / t_cv,
+            "price_cv": res.price, "price_plain": float(raw[0, 0])}
+
+
+def run_cv(args) -> dict:
+    """Headline metric part 1: time-to-relative-SE of the neural control variate against
+    plain GPU Monte Carlo (seconds, lower is better), for the Asian (target 1e-3) and the
+    European (target 1e-4) workloads."""
+    import myquantlib_gb300 as m
+    if int(os.environ.get("RANK", "0")) != 0:
+        return {}
+    eng = m.Engine(0)
+    for kind in ("asian", "european"):  # warm-up: tables, stream tables, first launches
+        eng.price(cv_jobs(m, kind, 1 << 16)[0])
+        eng.cv_train(cv_jobs(m, kind, 1 << 16)[0], cv_config(m, kind, pilot=1 << 16, iterations=10))
+    with ClockSampler(0) as clk:
+        res = {kind: time_to_se(eng, m, kind) for kind in ("asian", "european")}
+    a = res["asian"]
+    return {"metric": "time-to-relative-SE (s) neural-CV vs plain MC", "value": a["cv_s"], "unit": "s",
+            "n_gpus": 1, "steps": 1, "warmup": 1, "ms_per_step": a["cv_s"] * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 paths, bf16 MLP (fp32 accumulation)",
+            "data": "synthetic", "config": {"workload": "neural martingale control variate, Double Bates Asian "
+                                                        "(and Heston European)", "l2": "inputs larger than L2"},
+            "time_to_se": res, "clocks": clk.summary()}
+
+
+def run_ncu_cv_case() -> None:
+    """A small control-variate case for ncu: 2^16 pilot paths, 40 Adam steps, 2^18 priced paths."""
+    import myquantlib_gb300 as m
+    eng = m.Engine(0)
+    cfg = cv_config(m, "asian", pilot=1 << 16, iterations=40)
+    eng.cv_train(cv_jobs(m, "asian", 1 << 16)[0], cfg)
+    eng.cv_price(cv_jobs(m, "asian", 1 << 18)[0], cfg)
+
+
 def run_ncu_case(full: bool = False) -> None:
     """One maturity (T = 1) of the workload, priced twice, for an ncu capture: 2^18 paths (a few
     hundred MB on the device), or the full 2^22 paths for one-pass metrics."""
@@ -390,8 +485,9 @@ def main():
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
     ap.add_argument("--cpu-paths", type=int, default=8192, help="paths of the smaller CPU-baseline sample")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
-    ap.add_argument("--workload", choices=["strip", "batch"], default="strip",
-                    help="strip: the Bates Full-Greeks strip (headline); batch: uneven requests in one launch")
+    ap.add_argument("--workload", choices=["strip", "batch", "cv"], default="strip",
+                    help="strip: the Bates Full-Greeks strip (headline); batch: uneven requests in one launch; "
+                         "cv: time-to-relative-SE of the neural control variate against plain MC")
     ap.add_argument("--batch-jobs", type=int, default=4096)
     ap.add_argument("--ncu-case", action="store_true",
                     help="profiling case: one maturity (T=1), 2^18 paths, two requests, no timing")
@@ -399,12 +495,15 @@ def main():
                     help="profiling case at the full 2^22 paths (for one-pass metrics only)")
     args = ap.parse_args()
     if args.ncu_case or args.ncu_full:
-        run_ncu_case(full=args.ncu_full)
+        if args.workload == "cv":
+            run_ncu_cv_case()
+        else:
+            run_ncu_case(full=args.ncu_full)
         return
     if args.impl == "reference":
         line = run_reference(args)
     else:
-        line = run_batch(args) if args.workload == "batch" else run_engine(args)
+        line = {"batch": run_batch, "cv": run_cv}.get(args.workload, run_engine)(args)
     if line:
         print(json.dumps(line), flush=True)
 

@@ -62,7 +62,7 @@ myql_status upload_params(CtxBase *ctx, CvState &S, const float *p) {
   if (e == cudaSuccess) e = S.img.ensure(kImgBytes);
   if (e == cudaSuccess) e = S.vec.ensure(kVecCount * 4);
   if (e == cudaSuccess) e = S.loss.ensure(8 * 4096);
-  if (e == cudaSuccess) e = S.sums.ensure(64);
+  if (e == cudaSuccess) e = S.sums.ensure(128);
   if (e == cudaSuccess) e = cudaMemcpyAsync(S.params.p, p, kPCount * 4, cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(S.adam_m.p, 0, kPCount * 4, ctx->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(S.adam_v.p, 0, kPCount * 4, ctx->stream);
@@ -374,7 +374,7 @@ myql_status myql_cv_gradient(myql_ctx *ctx_, const float *feats, const float *dM
                           (float *)S.cv.p, nullptr);
   if (s != MYQL_OK) return s;
   e = launch_cv_resid((const float *)S.Y.p, (const float *)S.cv.p, n_paths, (float *)S.coef.p, (double *)S.loss.p,
-                      ctx->stream);
+                      (double *)S.sums.p + 6, ctx->stream);
   if (e != cudaSuccess) return cuda_status(e, "cv_resid launch");
   s = backward(ctx, S, (const uint8_t *)S.feat.p, (const float *)S.dM.p, n_paths, n_hedge);
   if (s != MYQL_OK) return s;
@@ -444,7 +444,7 @@ myql_status myql_cv_train(myql_ctx *ctx_, const myql_mc_job *job, const myql_cv_
     float *cvb = (float *)S.p_cv.p + b0 * 128;
     s = forward(ctx, S, f, dm, nb * 128, nh, cvb, nullptr);
     if (s != MYQL_OK) return s;
-    e = launch_cv_resid(Y, cvb, nb * 128, (float *)S.coef.p, loss + it, ctx->stream);
+    e = launch_cv_resid(Y, cvb, nb * 128, (float *)S.coef.p, loss + it, (double *)S.sums.p + 6, ctx->stream);
     if (e != cudaSuccess) return cuda_status(e, "cv_resid launch");
     s = backward(ctx, S, f, dm, nb * 128, nh);
     if (s != MYQL_OK) return s;

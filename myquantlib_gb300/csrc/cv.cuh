@@ -169,7 +169,7 @@ cudaError_t launch_cv_pack(const float *params, uint8_t *img, float *vec, cudaSt
 cudaError_t launch_cv_adam(float *params, float *m, float *v, const float *grad, float lr, float b1t, float b2t,
                            cudaStream_t st);
 cudaError_t launch_cv_resid(const float *Y, const float *cv, unsigned long long n, float *coef, double *loss_out,
-                            cudaStream_t st);
+                            double *acc, cudaStream_t st);
 cudaError_t launch_cv_beta(const float *Y, const float *dM, unsigned long long n, unsigned int n_hedge,
                            double *sums5, cudaStream_t st);
 cudaError_t launch_cv_reduce(const float *Y, const float *cv, unsigned long long n, double *sums4,

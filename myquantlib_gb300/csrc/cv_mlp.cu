@@ -22,6 +22,8 @@
 // Every mbarrier wait is bounded; a wait that runs out sets status[2], makes
 // the whole block leave its tile loop, waits (bounded) for its own bulk
 // copies in flight and frees its TMEM.
+#include <algorithm>
+
 #include "cv.cuh"
 
 namespace myql {
@@ -244,26 +246,20 @@ __global__ void __launch_bounds__(kFwdThreads, 2) cv_mlp_kernel(const __grid_con
 }
 
 // ------------------------------------------------------------------ backward
-// column sums over the block's 128 rows of a per-row 32-vector; lane i of the
-// returned value holds the sum of column i (valid in every warp after the call
-// through `red`, [4][32] floats of shared memory)
-__device__ __forceinline__ float colsum32(const float (&v)[32], float *red, int warp, int lane) {
-  float mine = 0.0f;
+// Column sums over a warp's 32 rows of a per-row 32-vector by transposed
+// halving: 31 shuffles; afterwards lane l holds the sum of column l.
+__device__ __forceinline__ float warp_colsum32(float (&v)[32], int lane) {
 #pragma unroll
-  for (int i = 0; i < 32; ++i) {
-    float s = v[i];
-    s += __shfl_xor_sync(0xffffffffu, s, 16);
-    s += __shfl_xor_sync(0xffffffffu, s, 8);
-    s += __shfl_xor_sync(0xffffffffu, s, 4);
-    s += __shfl_xor_sync(0xffffffffu, s, 2);
-    s += __shfl_xor_sync(0xffffffffu, s, 1);
-    if (lane == i) mine = s;
+  for (int off = 16; off >= 1; off >>= 1) {
+    const bool upper = (lane & off) != 0;
+#pragma unroll
+    for (int i = 0; i < off; ++i) {
+      const float send = upper ? v[i] : v[i + off];
+      const float keep = upper ? v[i + off] : v[i];
+      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+    }
   }
-  red[warp * 32 + lane] = mine;
-  __syncthreads();
-  const float tot = red[lane] + red[32 + lane] + red[64 + lane] + red[96 + lane];
-  __syncthreads();
-  return tot;
+  return v[0];
 }
 
 __device__ __forceinline__ void store_bf16_chunk(uint8_t *img, uint32_t row, int k0, const float *x) {
@@ -276,21 +272,27 @@ __device__ __forceinline__ void store_bf16_chunk(uint8_t *img, uint32_t row, int
   *reinterpret_cast<uint4 *>(img + tc::img128_offset(row, (uint32_t)k0, 128)) = make_uint4(w[0], w[1], w[2], w[3]);
 }
 
-__global__ void __launch_bounds__(128, 1) cv_bwd_kernel(const __grid_constant__ CvMlpParams P) {
+// 8 warps: warp w serves rows 32 (w % 4) .. (its TMEM lane quarter) and the
+// column half w / 4 of every 128-wide layer.
+constexpr int kBwdThreads = 256;
+
+__global__ void __launch_bounds__(kBwdThreads, 1) cv_bwd_kernel(const __grid_constant__ CvMlpParams P) {
   extern __shared__ uint8_t dyn[];
   __shared__ __align__(8) uint64_t bar_w, bar_mma;
   __shared__ uint32_t tmem_base;
   __shared__ float vec[kVecCount];
-  __shared__ float red[128];
   uint8_t *sm = align1024(dyn);
   // [W1x64 16K][W2 32K][W3 32K][X64 16K][H1 32K][H2 32K][D 32K]
   uint8_t *sW1 = sm, *sW2 = sm + 16384, *sW3 = sm + 49152, *sX = sm + 81920, *sH1 = sm + 98304;
   uint8_t *sH2 = sm + 131072, *sD = sm + 163840;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  for (int i = tid; i < kVecCount; i += 128) vec[i] = P.vec[i];
+  const uint32_t row = (uint32_t)(tid & 127);
+  const int half = warp >> 2, c0 = 2 * half, c1 = 2 * half + 2;
+  for (int i = tid; i < kVecCount; i += kBwdThreads) vec[i] = P.vec[i];
   // padding chunks of the x image stay zero
-  for (int c = 2; c < 8; ++c)
-    *reinterpret_cast<uint4 *>(sX + tc::img128_offset((uint32_t)tid, (uint32_t)(c * 8), 128)) = make_uint4(0, 0, 0, 0);
+  for (int i = tid; i < 128 * 6; i += kBwdThreads)
+    *reinterpret_cast<uint4 *>(sX + tc::img128_offset((uint32_t)(i / 6), (uint32_t)((2 + i % 6) * 8), 128)) =
+        make_uint4(0, 0, 0, 0);
   if (tid == 0) {
     tc::mbar_init(&bar_w, 1);
     tc::mbar_init(&bar_mma, 1);
@@ -304,7 +306,7 @@ __global__ void __launch_bounds__(128, 1) cv_bwd_kernel(const __grid_constant__ 
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tm = tmem_base;
-  const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+  const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
   const uint32_t T0 = tm, T1 = tm + 128, TW3 = tm + 256, TW2 = tm + 384;
   if (tid == 0) {
     tc::mbar_arrive_expect_tx(&bar_w, 16384u + 65536u);
@@ -317,22 +319,24 @@ __global__ void __launch_bounds__(128, 1) cv_bwd_kernel(const __grid_constant__ 
   const unsigned int n_mine = P.n_pb > blockIdx.x ? (P.n_pb - 1 - blockIdx.x) / gridDim.x + 1 : 0;
   const unsigned long long total = (unsigned long long)n_mine * P.n_hedge;
   uint32_t phase = 0;
-  float dw1[64];
+  float dw1[kCvIn];
 #pragma unroll
-  for (int i = 0; i < 64; ++i) dw1[i] = 0.0f;
-  float gb1 = 0.0f, gb2 = 0.0f, gb3 = 0.0f, gw4 = 0.0f, gb4 = 0.0f;
+  for (int i = 0; i < kCvIn; ++i) dw1[i] = 0.0f;
+  // column sums, column = 64 half + 32 (c - c0) + lane, over this warp's row quarter
+  float gb1[2] = {0.0f, 0.0f}, gb2[2] = {0.0f, 0.0f}, gb3[2] = {0.0f, 0.0f}, gw4[2] = {0.0f, 0.0f};
+  float gb4 = 0.0f;
   for (unsigned long long t = 0; t < total && !err; ++t) {
     const unsigned long long pb = (unsigned long long)blockIdx.x + (t / P.n_hedge) * gridDim.x;
     const unsigned long long tile = pb * P.n_hedge + t % P.n_hedge;
-    const unsigned long long row = tile * 128ull + (unsigned long long)tid;
-    const unsigned long long path = pb * 128ull + (unsigned long long)tid;
-    const float dg = path < P.n_paths ? P.coef[path] * P.dM[row] : 0.0f;
-    {  // x row -> X64 image (features 0..15; 16..63 stay zero)
+    const unsigned long long path = pb * 128ull + row;
+    const float dg = path < P.n_paths ? P.coef[path] * P.dM[tile * 128ull + row] : 0.0f;
+    if (half == 0) {  // x row -> X64 image (features 0..15; 16..63 stay zero)
       const uint8_t *ft = P.feat + tile * kCvTileBytes;
-      *reinterpret_cast<uint4 *>(sX + tc::img128_offset((uint32_t)tid, 0, 128)) =
-          *reinterpret_cast<const uint4 *>(ft + tc::img16_offset((uint32_t)tid, 0));
-      *reinterpret_cast<uint4 *>(sX + tc::img128_offset((uint32_t)tid, 8, 128)) =
-          *reinterpret_cast<const uint4 *>(ft + tc::img16_offset((uint32_t)tid, 8));
+      *reinterpret_cast<uint4 *>(sX + tc::img128_offset(row, 0, 128)) =
+          *reinterpret_cast<const uint4 *>(ft + tc::img16_offset(row, 0));
+      *reinterpret_cast<uint4 *>(sX + tc::img128_offset(row, 8, 128)) =
+          *reinterpret_cast<const uint4 *>(ft + tc::img16_offset(row, 8));
+      gb4 += dg;
     }
     block_sync_async();
     // F1: z1 = x W1^T (K = 64)
@@ -344,7 +348,7 @@ __global__ void __launch_bounds__(128, 1) cv_bwd_kernel(const __grid_constant__ 
       tc::mma_commit(&bar_mma);
     }
     if (!block_wait(&bar_mma, phase)) { err = true; break; }
-    epi_hidden(T0 + lane_off, vec + kVecB1, sH1, (uint32_t)tid);
+    epi_hidden(T0 + lane_off, vec + kVecB1, sH1, row, c0, c1);
     block_sync_async();
     // F2: z2 = h1 W2^T
     if (tid == 0) {
@@ -352,7 +356,7 @@ __global__ void __launch_bounds__(128, 1) cv_bwd_kernel(const __grid_constant__ 
       tc::mma_commit(&bar_mma);
     }
     if (!block_wait(&bar_mma, phase)) { err = true; break; }
-    epi_hidden(T0 + lane_off, vec + kVecB2, sH2, (uint32_t)tid);
+    epi_hidden(T0 + lane_off, vec + kVecB2, sH2, row, c0, c1);
     block_sync_async();
     // F3: z3 = h2 W3^T
     if (tid == 0) {
@@ -360,10 +364,9 @@ __global__ void __launch_bounds__(128, 1) cv_bwd_kernel(const __grid_constant__ 
       tc::mma_commit(&bar_mma);
     }
     if (!block_wait(&bar_mma, phase)) { err = true; break; }
-    // e3: dz3 = dg w4 silu'(z3 + b3) -> D; gradients of b3, w4, b4
-    gb4 += dg;
+    // e3: dz3 = dg w4 silu'(z3 + b3) -> D; column sums for b3 and w4
 #pragma unroll 1
-    for (int c = 0; c < 4; ++c) {
+    for (int c = c0; c < c1; ++c) {
       float v[32], dz[32], hw[32];
       tc::tmem_ld32(T0 + lane_off + (uint32_t)(c * 32), v);
 #pragma unroll
@@ -374,13 +377,9 @@ __global__ void __launch_bounds__(128, 1) cv_bwd_kernel(const __grid_constant__ 
         hw[i] = dg * tc::silu(z);
       }
 #pragma unroll
-      for (int q = 0; q < 4; ++q) store_bf16_chunk(sD, (uint32_t)tid, c * 32 + q * 8, dz + q * 8);
-      const float s3 = colsum32(dz, red, warp, lane);
-      const float s4 = colsum32(hw, red, warp, lane);
-      if (warp == c) {
-        gb3 += s3;
-        gw4 += s4;
-      }
+      for (int q = 0; q < 4; ++q) store_bf16_chunk(sD, row, c * 32 + q * 8, dz + q * 8);
+      gb3[c - c0] += warp_colsum32(dz, lane);
+      gw4[c - c0] += warp_colsum32(hw, lane);
     }
     block_sync_async();
     // B3: dh2 = dz3 W3 -> T0; dW3 += dz3^T h2 -> TW3; z2 again -> T1
@@ -392,16 +391,15 @@ __global__ void __launch_bounds__(128, 1) cv_bwd_kernel(const __grid_constant__ 
     }
     if (!block_wait(&bar_mma, phase)) { err = true; break; }
 #pragma unroll 1
-    for (int c = 0; c < 4; ++c) {
+    for (int c = c0; c < c1; ++c) {
       float dh[32], z[32], dz[32];
       tc::tmem_ld32(T0 + lane_off + (uint32_t)(c * 32), dh);
       tc::tmem_ld32(T1 + lane_off + (uint32_t)(c * 32), z);
 #pragma unroll
       for (int i = 0; i < 32; ++i) dz[i] = dh[i] * tc::silu_grad(z[i] + vec[kVecB2 + c * 32 + i]);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) store_bf16_chunk(sD, (uint32_t)tid, c * 32 + q * 8, dz + q * 8);
-      const float s2 = colsum32(dz, red, warp, lane);
-      if (warp == c) gb2 += s2;
+      for (int q = 0; q < 4; ++q) store_bf16_chunk(sD, row, c * 32 + q * 8, dz + q * 8);
+      gb2[c - c0] += warp_colsum32(dz, lane);
     }
     block_sync_async();
     // B2: dh1 = dz2 W2 -> T0; dW2 += dz2^T h1 -> TW2; z1 again -> T1
@@ -416,56 +414,55 @@ __global__ void __launch_bounds__(128, 1) cv_bwd_kernel(const __grid_constant__ 
     }
     if (!block_wait(&bar_mma, phase)) { err = true; break; }
 #pragma unroll 1
-    for (int c = 0; c < 4; ++c) {
+    for (int c = c0; c < c1; ++c) {
       float dh[32], z[32], dz[32];
       tc::tmem_ld32(T0 + lane_off + (uint32_t)(c * 32), dh);
       tc::tmem_ld32(T1 + lane_off + (uint32_t)(c * 32), z);
 #pragma unroll
       for (int i = 0; i < 32; ++i) dz[i] = dh[i] * tc::silu_grad(z[i] + vec[kVecB1 + c * 32 + i]);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) store_bf16_chunk(sD, (uint32_t)tid, c * 32 + q * 8, dz + q * 8);
-      const float s1 = colsum32(dz, red, warp, lane);
-      if (warp == c) gb1 += s1;
+      for (int q = 0; q < 4; ++q) store_bf16_chunk(sD, row, c * 32 + q * 8, dz + q * 8);
+      gb1[c - c0] += warp_colsum32(dz, lane);
     }
     block_sync_async();
-    // B1: dW1 (tile) = dz1^T x -> T0 columns 0..63
+    // B1: dW1 (tile) = dz1^T x -> T0 columns 0..63 (only the 16 input slots are kept)
     if (tid == 0) {
       mma_tn_rows(T0, sD, sX, 64, 0u);
       tc::mma_commit(&bar_mma);
     }
     if (!block_wait(&bar_mma, phase)) { err = true; break; }
-    {
+    if (half == 0) {
       float v[32];
       tc::tmem_ld32(T0 + lane_off, v);
 #pragma unroll
-      for (int i = 0; i < 32; ++i) dw1[i] += v[i];
-      tc::tmem_ld32(T0 + lane_off + 32u, v);
-#pragma unroll
-      for (int i = 0; i < 32; ++i) dw1[32 + i] += v[i];
+      for (int i = 0; i < kCvIn; ++i) dw1[i] += v[i];
     }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
   }
   if (!err && total > 0) {
-    // flush: thread o owns output row o of dW2, dW3 (TMEM lane o) and dW1 (registers)
+    // flush: thread (quarter, half) owns output row o = row of dW2, dW3 (TMEM lane o), columns of its half
     float *gr = P.grad;
-    for (int c = 0; c < 4; ++c) {
+    for (int c = c0; c < c1; ++c) {
       float v[32];
       tc::tmem_ld32(TW3 + lane_off + (uint32_t)(c * 32), v);
-      for (int i = 0; i < 32; ++i) atomicAdd(gr + kPW3 + tid * 128 + c * 32 + i, v[i]);
+      for (int i = 0; i < 32; ++i) atomicAdd(gr + kPW3 + row * 128 + c * 32 + i, v[i]);
       tc::tmem_ld32(TW2 + lane_off + (uint32_t)(c * 32), v);
-      for (int i = 0; i < 32; ++i) atomicAdd(gr + kPW2 + tid * 128 + c * 32 + i, v[i]);
+      for (int i = 0; i < 32; ++i) atomicAdd(gr + kPW2 + row * 128 + c * 32 + i, v[i]);
     }
-    for (int i = 0; i < kCvIn; ++i) atomicAdd(gr + kPW1 + tid * kCvIn + i, dw1[i]);
-    // bias / output-layer sums: warp c holds columns c*32 + lane
-    atomicAdd(gr + kPB1 + tid, gb1);
-    atomicAdd(gr + kPB2 + tid, gb2);
-    atomicAdd(gr + kPB3 + tid, gb3);
-    atomicAdd(gr + kPW4 + tid, gw4);
+    if (half == 0)
+      for (int i = 0; i < kCvIn; ++i) atomicAdd(gr + kPW1 + row * kCvIn + i, dw1[i]);
+    for (int c = c0; c < c1; ++c) {
+      const int col = c * 32 + lane;
+      atomicAdd(gr + kPB1 + col, gb1[c - c0]);
+      atomicAdd(gr + kPB2 + col, gb2[c - c0]);
+      atomicAdd(gr + kPB3 + col, gb3[c - c0]);
+      atomicAdd(gr + kPW4 + col, gw4[c - c0]);
+    }
     float s = gb4;
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) atomicAdd(gr + kPB4, s);
+    if (lane == 0 && half == 0) atomicAdd(gr + kPB4, s);
   }
   if (err && tid == 0) atomicAdd(P.status + 2, 1u);
   tc::fence_before_sync();
@@ -515,37 +512,27 @@ __global__ void cv_adam_kernel(float *p, float *m, float *v, const float *g, flo
 }
 
 // r_p = Y_p - C_p - mean(Y - C); coef_p = dL/dC_p = -2 r_p / n; loss = mean r^2.
-// One block of 1024 threads.
-__global__ void cv_resid_kernel(const float *Y, const float *cv, unsigned long long n, float *coef, double *loss) {
-  __shared__ double red[32];
-  __shared__ double mean_sh;
+// Pass 1 sums Y - C into acc[0]; pass 2 writes coef and sums r^2 into acc[1].
+__global__ void cv_resid_sum_kernel(const float *Y, const float *cv, unsigned long long n, double *acc) {
   double s = 0.0;
-  for (unsigned long long i = threadIdx.x; i < n; i += blockDim.x) s += (double)Y[i] - (double)cv[i];
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+       i += (unsigned long long)gridDim.x * blockDim.x)
+    s += (double)Y[i] - (double)cv[i];
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
-    mean_sh = t / (double)n;
-  }
-  __syncthreads();
-  const double mu = mean_sh;
+  if ((threadIdx.x & 31) == 0) atomicAdd(acc, s);
+}
+__global__ void cv_resid_coef_kernel(const float *Y, const float *cv, unsigned long long n, double *acc,
+                                     float *coef, double *loss) {
+  const double mu = acc[0] / (double)n;
   double ss = 0.0;
-  for (unsigned long long i = threadIdx.x; i < n; i += blockDim.x) {
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
     const double r = (double)Y[i] - (double)cv[i] - mu;
     ss += r * r;
     coef[i] = (float)(-2.0 * r / (double)n);
   }
-  __syncthreads();
   for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = ss;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
-    *loss = t / (double)n;
-  }
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss, ss / (double)n);
 }
 
 // sums4 += {sum Y, sum Y^2, sum (Y - C), sum (Y - C)^2} (FP64, per-block partials + atomics)
@@ -630,7 +617,7 @@ cudaError_t launch_cv_bwd(const CvMlpParams &P, unsigned int blocks, cudaStream_
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  dev::cv_bwd_kernel<<<blocks, 128, kBwdSmem, st>>>(P);
+  dev::cv_bwd_kernel<<<blocks, dev::kBwdThreads, kBwdSmem, st>>>(P);
   return cudaGetLastError();
 }
 
@@ -645,9 +632,15 @@ cudaError_t launch_cv_adam(float *params, float *m, float *v, const float *grad,
   return cudaGetLastError();
 }
 
+// acc: two doubles of scratch; loss_out is overwritten with mean r^2
 cudaError_t launch_cv_resid(const float *Y, const float *cv, unsigned long long n, float *coef, double *loss_out,
-                            cudaStream_t st) {
-  dev::cv_resid_kernel<<<1, 1024, 0, st>>>(Y, cv, n, coef, loss_out);
+                            double *acc, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(acc, 0, 8, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(loss_out, 0, 8, st);
+  if (e != cudaSuccess) return e;
+  const unsigned int blocks = (unsigned int)std::min<unsigned long long>(304ull, (n + 255) / 256);
+  dev::cv_resid_sum_kernel<<<blocks, 256, 0, st>>>(Y, cv, n, acc);
+  dev::cv_resid_coef_kernel<<<blocks, 256, 0, st>>>(Y, cv, n, acc, coef, loss_out);
   return cudaGetLastError();
 }
 

@@ -1,0 +1,66 @@
+"""Replicas: one pricing request split over processes or GPUs.
+
+Paths are independent, so a request of M paths runs as W replicas of M / W
+paths on disjoint xoshiro stream ranges (replica r takes streams
+[r S / W, (r + 1) S / W) of the request's S streams) and the results are pooled
+from the FP64 moments (n * mean, n * E[x^2]) of each replica -- the reduction
+the reference does with its OpenMP critical merge (MonteCarloPricer.hpp:413-440).
+When M is a multiple of S every stream runs the same paths as in the single
+request, so the pooled result equals the single request's up to FP64
+summation order.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from . import pricers as _p
+
+
+def shard_job(job: "_p._Job", rank: int, world: int) -> "_p._Job":
+    """The replica of `job` that rank `rank` of `world` prices: M / W paths on the
+    stream range [r S / W, (r + 1) S / W) of the request's S streams."""
+    M = int(job.c.config.num_paths)
+    S = int(job.c.config.n_streams) or min(131072, M)
+    if M % world or S % world:
+        raise ValueError(f"num_paths {M} and the {S} streams must divide into {world} replicas")
+    c = _abi.McJobC()                    # byte copy; the strikes array stays shared
+    C.memmove(C.addressof(c), C.addressof(job.c), C.sizeof(c))
+    c.config.num_paths = M // world
+    c.config.n_streams = S // world
+    c.config.stream_offset = int(job.c.config.stream_offset) + rank * (S // world)
+    return _p._Job(c, job.strikes)
+
+
+def moments(raw: np.ndarray, n_paths: int) -> np.ndarray:
+    """(2Q, n) result rows of one replica -> FP64 moment sums [n mean; n E[x^2]] (discounted units)."""
+    v, se = raw[0::2], raw[1::2]
+    return np.concatenate([n_paths * v, n_paths * (se * se * n_paths + v * v)], axis=0)
+
+
+def combine(mom: np.ndarray, n_total: int) -> np.ndarray:
+    """Pooled moment sums -> (2Q, n) result rows (compute_stats, MonteCarloPricer.hpp:448-457)."""
+    q = mom.shape[0] // 2
+    mean = mom[:q] / n_total
+    var = np.maximum(mom[q:] / n_total - mean * mean, 0.0)
+    out = np.empty((2 * q, mom.shape[1]))
+    out[0::2] = mean
+    out[1::2] = np.sqrt(var / n_total)
+    return out
+
+
+def allreduce_price(raw: np.ndarray, n_local: int, group=None) -> np.ndarray:
+    """Pools one replica's result with every rank's through torch.distributed (one FP64 sum)."""
+    import torch
+    import torch.distributed as dist
+    world = dist.get_world_size(group)
+    mom = torch.from_numpy(moments(np.asarray(raw, dtype=np.float64), n_local))
+    if dist.get_backend(group) == "nccl":
+        mom = mom.cuda()
+    dist.all_reduce(mom, op=dist.ReduceOp.SUM, group=group)
+    return combine(mom.cpu().numpy(), n_local * world)
+
+
+assert _abi.Q_COUNT == 10

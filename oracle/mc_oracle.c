@@ -1055,6 +1055,7 @@ int myql_oracle_mc_price(const myql_mc_job *job, int layout, int n_threads, doub
     /* stream states: sequential jumps from the seeded generator */
     xo_t *streams = (xo_t *)malloc(S * sizeof(xo_t));
     xo_seed(&streams[0], job->config.seed);
+    for (uint64_t k = 0; k < job->config.stream_offset; ++k) xo_jump(&streams[0]); /* first stream index */
     for (uint64_t k = 1; k < S; ++k) {
       streams[k] = streams[k - 1];
       xo_jump(&streams[k]);

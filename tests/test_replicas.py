@@ -1,0 +1,90 @@
+"""Replicas on CPU ranks (gloo, world size 2): each rank prices its shard of a
+request with the oracle on its own stream range, the ranks pool the FP64
+moments with one all-reduce, and the pooled result equals the single request
+over all the streams."""
+import os
+import socket
+
+import numpy as np
+import pytest
+import torch.distributed as dist
+import torch.multiprocessing as mp
+
+import jobspec
+import myquantlib_gb300 as m
+from myquantlib_gb300 import replicas
+
+SPEC = {"name": "bates_nci_strip", "config": {"paths": 4096, "steps": 20}, "mode": "essential",
+        "instrument": {"K": [90.0, 100.0, 110.0], "T": 1.0, "kind": "european"},
+        "model": {"heston": [[2.0, 0.05, 0.9, -0.6, 0.05]], "jump": {"kind": "merton", "lambda": 0.5, "mu": -0.1,
+                                                                   "delta": 0.15}},
+        "schemes": ["NCI"]}
+
+
+def _job(paths, streams):
+    spec = dict(SPEC, config={"paths": paths, "steps": 20})
+    j = jobspec.make_job(spec)
+    j.c.config.n_streams = streams
+    return j
+
+
+def _rank(rank, world, port, out_q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        from oracle import oracle
+        shard = replicas.shard_job(_job(4096, 512 * world), rank, world)
+        raw, _ = oracle.mc_price(shard, oracle.LAYOUT_STREAMS, 1)
+        pooled = replicas.allreduce_price(raw, int(shard.c.config.num_paths))
+        out_q.put((rank, int(shard.c.config.stream_offset), pooled))
+    finally:
+        dist.destroy_process_group()
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def test_two_rank_pool_equals_single_request(oracle_lib):
+    world = 2
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank, args=(r, world, port, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    got = [q.get(timeout=120) for _ in range(world)]
+    for p in procs:
+        p.join(60)
+        assert p.exitcode == 0
+    got.sort(key=lambda t: t[0])
+    assert [g[1] for g in got] == [0, 512]
+    want, _ = oracle_lib.mc_price(_job(4096, 512 * world), oracle_lib.LAYOUT_STREAMS, 1)
+    for _, _, pooled in got:
+        np.testing.assert_allclose(pooled[:6], want[:6], rtol=1e-11, atol=1e-13)
+
+
+def test_shard_job_layout():
+    j = _job(1 << 20, 0)
+    s = replicas.shard_job(j, 3, 4)
+    assert int(s.c.config.num_paths) == 1 << 18
+    assert int(s.c.config.n_streams) == 32768 and int(s.c.config.stream_offset) == 3 * 32768
+    with pytest.raises(ValueError):
+        replicas.shard_job(_job(1001, 0), 0, 2)
+
+
+def test_combine_is_compute_stats():
+    """Pooling per-replica (mean, standard error) rows reproduces the statistics of all samples."""
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((3, 1000)) * 2 + 1
+    mom = 0
+    for part in (x[:, :400], x[:, 400:]):
+        rows = np.empty((6, 1))
+        rows[0::2, 0] = part.mean(1)
+        rows[1::2, 0] = np.sqrt(part.var(1) / part.shape[1])
+        mom = mom + replicas.moments(rows, part.shape[1])
+    pooled = replicas.combine(mom, 1000)
+    np.testing.assert_allclose(pooled[0::2, 0], x.mean(1), rtol=1e-12)
+    np.testing.assert_allclose(pooled[1::2, 0], np.sqrt(x.var(1) / 1000), rtol=1e-10)

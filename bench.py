@@ -6,11 +6,13 @@ Heston(kappa 2, theta 0.05, sigma 0.9 [Feller violated], rho -0.6, v0 0.05) +
 Merton jumps (lambda 0.5, mu -0.1, delta 0.15); SchemeNCI; European calls with
 64 strikes uniform on [60, 140] x 8 maturities {0.25, 0.5, 1, 1.5, 2, 2.5, 3, 4};
 200 steps per year; 2^22 paths; GreekMode::Full (CRN delta, gamma, vega, theta,
-rho, vanna, charm: 7 simulated scenarios per path); S0 100, r 0.02, q 0, seed 42.
+rho, vanna, charm: 7 scenarios per path, of which the two rho scenarios of these
+European options are derived from the base path); S0 100, r 0.02, q 0, seed 42.
 One step = pricing the whole strip = 8 pricing requests (one per maturity, as
 the reference prices one maturity per MonteCarloPricer::calculate call).
 
-Metric: paths*steps/s = simulated path-steps (all 7 scenarios) per second.
+Metric: paths*steps/s = path-steps of the workload (paths x time steps, each with
+its 7 Full-Greek scenarios) per second.
   value -- device time of the 8 requests (CUDA events on the launching stream,
            inputs resident, L2 flushed between steps)
   e2e   -- the same through the C ABI (myql_mc_price) with pinned host strike
@@ -42,7 +44,8 @@ STRIKES = list(60.0 + 80.0 * np.arange(64) / 63.0)
 PATHS = 1 << 22
 STEPS_PER_YEAR = 200
 SEED = 42
-N_SCENARIOS = 7
+N_SCENARIOS = 7      # base, v0 up/down, T up/down, r up/down
+N_SIMULATED = 5      # the r-bumped scenarios of a European are the base path shifted by (r' - r) T
 # algorithmic work per simulated path-step of this workload (Bates, NCI):
 # inverse normal 42 ALU + 1 XU, Poisson inversion 58 ALU + 3 XU, NCI Hermite
 # lookup with its uniform 46 ALU, log-S update 7 ALU + 1 XU; one 16-byte table
@@ -62,8 +65,9 @@ def workload_jobs(m, stream_offset: int = 0, paths: int = PATHS):
 
 
 def path_steps(paths: int = PATHS) -> tuple[int, int]:
+    """(simulated scenario path-steps, workload path-steps) of one pass over the strip."""
     base = sum(paths * int(round(STEPS_PER_YEAR * T)) for T in MATURITIES)
-    return base * N_SCENARIOS, base
+    return base * N_SIMULATED, base
 
 
 class ClockSampler:
@@ -158,8 +162,8 @@ def cpu_reference(args, scale_to_full: bool = True) -> dict:
     slope = (t2 - t1) / (p2 - p1)
     intercept = max(t1 - slope * p1, 0.0)
     full_time = intercept + slope * PATHS
-    sim, _ = path_steps(PATHS)
-    rate = sim / full_time
+    _, base = path_steps(PATHS)
+    rate = base / full_time
     return {"value": rate, "unit": "paths*steps/s", "cores": cores, "kind": "port",
             "sample": (f"whole workload (8 maturities x 64 strikes, Full Greeks) at {p1} and {p2} "
                        f"paths ({t1:.1f} s, {t2:.1f} s on {cores} threads), extrapolated linearly in "
@@ -191,7 +195,8 @@ def workload_config(args) -> dict:
     sim, base = path_steps()
     return {"workload": "Bates SchemeNCI European call strip, Full CRN Greeks (configuration 2)",
             "strikes": 64, "maturities": MATURITIES, "paths": PATHS, "steps_per_year": STEPS_PER_YEAR,
-            "scenarios_per_path": N_SCENARIOS, "simulated_path_steps_per_step": sim,
+            "scenarios_per_path": N_SCENARIOS, "simulated_scenarios_per_path": N_SIMULATED,
+            "simulated_path_steps_per_step": sim,
             "base_path_steps_per_step": base, "l2": "flushed between steps (256 MiB write)",
             "parallelism": f"replicas x{args.gpus} (disjoint xoshiro stream ranges)"}
 
@@ -277,8 +282,8 @@ def run_engine(args) -> dict:
         buf = _t.tensor([t_dev, e2e_s], device=f"cuda:{local}", dtype=_t.float64)
         dist.all_reduce(buf, op=dist.ReduceOp.MAX)
         t_dev, e2e_s = float(buf[0]), float(buf[1])
-    value = world * sim * args.steps / t_dev
-    e2e = world * sim * args.steps / e2e_s
+    value = world * base * args.steps / t_dev
+    e2e = world * base * args.steps / e2e_s
     if rank != 0:
         return {}
 
@@ -377,6 +382,7 @@ CV_TARGETS = {"asian": 1e-3, "european": 1e-4}
 
 
 def cv_jobs(m, kind: str, paths: int, seed: int = 42):
+    kind = kind.split("_")[0]
     """The control-variate workloads: the Double Bates arithmetic Asian call (factors
     (v0 .03, kappa 2, theta .03, sigma .4, rho -.7) and (.02, .5, .02, .3, -.3), Merton
     (.3, -.05, .1), K 100, T 2, 256 steps, SchemeNCI) and the Heston European call
@@ -397,6 +403,7 @@ def cv_jobs(m, kind: str, paths: int, seed: int = 42):
 
 
 def cv_config(m, kind: str, pilot: int = 1 << 20, iterations: int = 250):
+    kind = kind.split("_")[0]
     return m.pricers.ControlVariateConfig(hedge_every=8 if kind == "asian" else 5, iterations=iterations,
                                           pilot_paths=pilot, batch_paths=8192, learning_rate=3e-3, seed=7).c()
 
@@ -427,7 +434,10 @@ def time_to_se(eng, m, kind: str, probe_paths: int = 1 << 22) -> dict:
     tr = eng.cv_train(cv_jobs(m, kind, 1 << 16, seed=45)[0], cfg)
     res = eng.cv_price(cv_jobs(m, kind, max(n_cv, 128), seed=46)[0], cfg)
     t_cv = time.perf_counter() - t0
-    return {"instrument": "Double Bates arithmetic Asian call" if kind == "asian" else "Heston European call",
+    t_plain_path = t_plain / n_plain
+    t_cv_path = (t_cv - tr.total_ms / 1e3) / max(n_cv, 128)
+    return {"instrument": "Double Bates arithmetic Asian call" if kind.startswith("asian") else "Heston European call",
+            "pricing_only_speedup": res.variance_ratio * t_plain_path / t_cv_path,
             "target_rel_se": target, "plain_paths": n_plain, "plain_s": t_plain, "plain_rel_se": rel_plain,
             "plain_path_steps_per_s": n_plain * steps / t_plain,
             "cv_paths": n_cv, "cv_s": t_cv, "cv_rel_se": res.price_std_err / res.price, "cv_train_s": tr.train_ms / 1e3,
@@ -449,6 +459,8 @@ def run_cv(args) -> dict:
         eng.cv_train(cv_jobs(m, kind, 1 << 16)[0], cv_config(m, kind, pilot=1 << 16, iterations=10))
     with ClockSampler(0) as clk:
         res = {kind: time_to_se(eng, m, kind) for kind in ("asian", "european")}
+        CV_TARGETS["asian_1e-4"] = 1e-4
+        res["asian_1e-4"] = time_to_se(eng, m, "asian_1e-4")
     a = res["asian"]
     return {"metric": "time-to-relative-SE (s) neural-CV vs plain MC", "value": a["cv_s"], "unit": "s",
             "n_gpus": 1, "steps": 1, "warmup": 1, "ms_per_step": a["cv_s"] * 1e3, "higher_is_better": False,

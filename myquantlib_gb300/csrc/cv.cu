@@ -23,6 +23,7 @@ struct CvState : ExtState {
   DevBuf params, adam_m, adam_v, grad, img, vec, coef, loss, sums;
   DevBuf p_feat, p_dM, p_Y, p_cv;  // pilot set
   DevBuf feat, dM, Y, cv;          // pricing chunk / caller data
+  DevBuf gdm;                      // per-row g dM of the tile-major forward
   bool init = false;
   uint64_t adam_t = 0;
 };
@@ -207,6 +208,14 @@ myql_status forward(CtxBase *ctx, CvState &S, const uint8_t *feat, const float *
                     float *cv, float *g_out) {
   CvMlpParams F;
   std::memset(&F, 0, sizeof F);
+  const uint64_t n_pb = (n_paths + 127) / 128;
+  // few path blocks (training minibatches): spread the tiles over every SM
+  if (n_pb < (uint64_t)ctx->sm_count * 8) {
+    cudaError_t e = S.gdm.ensure(n_pb * nh * 128 * 4);
+    if (e != cudaSuccess) return cuda_status(e, "control-variate row buffer");
+    F.tile_major = 1;
+    F.gdm = (float *)S.gdm.p;
+  }
   F.feat = feat;
   F.dM = dM;
   F.img = (const uint8_t *)S.img.p;
@@ -217,8 +226,12 @@ myql_status forward(CtxBase *ctx, CvState &S, const uint8_t *feat, const float *
   F.n_pb = (unsigned int)((n_paths + 127) / 128);
   F.n_hedge = nh;
   F.status = (unsigned int *)ctx->status.p;
-  cudaError_t e = launch_cv_mlp(F, mlp_blocks(ctx, F.n_pb, 2), ctx->stream);
+  cudaError_t e = launch_cv_mlp(F, mlp_blocks(ctx, F.tile_major ? n_pb * nh : n_pb, 2), ctx->stream);
   ctx->launches++;
+  if (e == cudaSuccess && F.tile_major) {
+    e = launch_cv_rowsum(F.gdm, n_paths, nh, cv, ctx->stream);
+    ctx->launches++;
+  }
   return cuda_status(e, "cv_mlp launch");
 }
 
@@ -236,7 +249,7 @@ myql_status backward(CtxBase *ctx, CvState &S, const uint8_t *feat, const float 
   B.n_hedge = nh;
   B.status = (unsigned int *)ctx->status.p;
   cudaError_t e = cudaMemsetAsync(S.grad.p, 0, kPCount * 4, ctx->stream);
-  if (e == cudaSuccess) e = launch_cv_bwd(B, mlp_blocks(ctx, B.n_pb), ctx->stream);
+  if (e == cudaSuccess) e = launch_cv_bwd(B, mlp_blocks(ctx, (uint64_t)B.n_pb * nh), ctx->stream);
   ctx->launches++;
   return cuda_status(e, "cv_bwd launch");
 }

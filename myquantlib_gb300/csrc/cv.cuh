@@ -75,8 +75,10 @@ struct CvMlpParams {
   const float *dM;
   const uint8_t *img;   // packed weights (kImgBytes)
   const float *vec;     // kVecCount floats
-  float *cv;            // per path: sum_j g_j dM_j
+  float *cv;            // per path: sum_j g_j dM_j (path-major forward)
   float *g_out;         // optional per-row g
+  float *gdm;           // tile-major forward: per-row g dM, summed per path by cv_rowsum_kernel
+  int tile_major;       // forward: 1 = blocks take tiles round robin, 0 = whole path blocks
   const float *coef;    // backward: dL/dC per path
   float *grad;          // backward: FP32 parameter-blob gradient (accumulated)
   unsigned long long n_paths;
@@ -172,6 +174,8 @@ cudaError_t launch_cv_resid(const float *Y, const float *cv, unsigned long long 
                             double *acc, cudaStream_t st);
 cudaError_t launch_cv_beta(const float *Y, const float *dM, unsigned long long n, unsigned int n_hedge,
                            double *sums5, cudaStream_t st);
+cudaError_t launch_cv_rowsum(const float *gdm, unsigned long long n_paths, unsigned int n_hedge, float *cv,
+                             cudaStream_t st);
 cudaError_t launch_cv_reduce(const float *Y, const float *cv, unsigned long long n, double *sums4,
                              cudaStream_t st);
 

@@ -159,9 +159,18 @@ __global__ void __launch_bounds__(kFwdThreads, 2) cv_mlp_kernel(const __grid_con
   const uint32_t tm = tmem_base;
   const uint32_t tm_row = tm + ((uint32_t)((warp & 3) * 32) << 16);
   const int c0 = 2 * half, c1 = 2 * half + 2;
-  const unsigned int n_mine = P.n_pb > blockIdx.x ? (P.n_pb - 1 - blockIdx.x) / gridDim.x + 1 : 0;
-  const unsigned long long total = (unsigned long long)n_mine * P.n_hedge;
+  // path-major: whole path blocks per block (per-path sums in registers);
+  // tile-major: tiles round robin over the blocks (per-row products to P.gdm)
+  const unsigned long long n_tiles = (unsigned long long)P.n_pb * P.n_hedge;
+  unsigned long long total;
+  if (P.tile_major) {
+    total = n_tiles > blockIdx.x ? (n_tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  } else {
+    const unsigned int n_mine = P.n_pb > blockIdx.x ? (P.n_pb - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    total = (unsigned long long)n_mine * P.n_hedge;
+  }
   auto tile_of = [&](unsigned long long t) {
+    if (P.tile_major) return (unsigned long long)blockIdx.x + t * gridDim.x;
     return ((unsigned long long)blockIdx.x + (t / P.n_hedge) * gridDim.x) * P.n_hedge + t % P.n_hedge;
   };
   int pending = -1;  // x buffer with a bulk copy in flight (thread 0) and its phase parity
@@ -182,7 +191,7 @@ __global__ void __launch_bounds__(kFwdThreads, 2) cv_mlp_kernel(const __grid_con
   float acc = 0.0f;
   for (unsigned long long t = 0; t < total && !err; ++t) {
     const unsigned long long tile = tile_of(t);
-    const unsigned int j = (unsigned int)(t % P.n_hedge);
+    const unsigned int j = (unsigned int)(tile % P.n_hedge);
     if (tid == 0) {
       if (t + 1 < total) {
         const int nb = (int)((t + 1) & 1);
@@ -223,12 +232,16 @@ __global__ void __launch_bounds__(kFwdThreads, 2) cv_mlp_kernel(const __grid_con
     if (half == 0) {
       const float g = gpart + part[row];
       const unsigned long long r = tile * 128ull + row;
-      acc = fmaf(g, P.dM[r], acc);
       if (P.g_out) P.g_out[r] = g;
-      if (j == P.n_hedge - 1) {
-        const unsigned long long path = (tile / P.n_hedge) * 128ull + row;
-        if (path < P.n_paths) P.cv[path] = acc;
-        acc = 0.0f;
+      if (P.tile_major) {
+        P.gdm[r] = g * P.dM[r];
+      } else {
+        acc = fmaf(g, P.dM[r], acc);
+        if (j == P.n_hedge - 1) {
+          const unsigned long long path = (tile / P.n_hedge) * 128ull + row;
+          if (path < P.n_paths) P.cv[path] = acc;
+          acc = 0.0f;
+        }
       }
     }
     // the next tile's writes of `part` come after its three MMA waits, each a block barrier
@@ -316,8 +329,9 @@ __global__ void __launch_bounds__(kBwdThreads, 1) cv_bwd_kernel(const __grid_con
   bool ok = true;
   if (tid == 0) ok = tc::mbar_wait(&bar_w, 0, kCvWaitNs);
   bool err = __syncthreads_or(!ok) != 0;
-  const unsigned int n_mine = P.n_pb > blockIdx.x ? (P.n_pb - 1 - blockIdx.x) / gridDim.x + 1 : 0;
-  const unsigned long long total = (unsigned long long)n_mine * P.n_hedge;
+  // tiles round robin over the blocks
+  const unsigned long long n_tiles = (unsigned long long)P.n_pb * P.n_hedge;
+  const unsigned long long total = n_tiles > blockIdx.x ? (n_tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
   uint32_t phase = 0;
   float dw1[kCvIn];
 #pragma unroll
@@ -326,8 +340,8 @@ __global__ void __launch_bounds__(kBwdThreads, 1) cv_bwd_kernel(const __grid_con
   float gb1[2] = {0.0f, 0.0f}, gb2[2] = {0.0f, 0.0f}, gb3[2] = {0.0f, 0.0f}, gw4[2] = {0.0f, 0.0f};
   float gb4 = 0.0f;
   for (unsigned long long t = 0; t < total && !err; ++t) {
-    const unsigned long long pb = (unsigned long long)blockIdx.x + (t / P.n_hedge) * gridDim.x;
-    const unsigned long long tile = pb * P.n_hedge + t % P.n_hedge;
+    const unsigned long long tile = (unsigned long long)blockIdx.x + t * gridDim.x;
+    const unsigned long long pb = tile / P.n_hedge;
     const unsigned long long path = pb * 128ull + row;
     const float dg = path < P.n_paths ? P.coef[path] * P.dM[tile * 128ull + row] : 0.0f;
     if (half == 0) {  // x row -> X64 image (features 0..15; 16..63 stay zero)
@@ -535,6 +549,16 @@ __global__ void cv_resid_coef_kernel(const float *Y, const float *cv, unsigned l
   if ((threadIdx.x & 31) == 0) atomicAdd(loss, ss / (double)n);
 }
 
+// cv[p] = sum_j gdm[row (p, j)] in hedge order (tile-major forward)
+__global__ void cv_rowsum_kernel(const float *gdm, unsigned long long n, unsigned int n_hedge, float *cv) {
+  const unsigned long long p = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const unsigned long long base = (p >> 7) * n_hedge * 128ull + (p & 127u);
+  float s = 0.0f;
+  for (unsigned int j = 0; j < n_hedge; ++j) s += gdm[base + (unsigned long long)j * 128ull];
+  cv[p] = s;
+}
+
 // sums4 += {sum Y, sum Y^2, sum (Y - C), sum (Y - C)^2} (FP64, per-block partials + atomics)
 __global__ void cv_reduce_kernel(const float *Y, const float *cv, unsigned long long n, double *sums4) {
   double a[4] = {0.0, 0.0, 0.0, 0.0};
@@ -641,6 +665,12 @@ cudaError_t launch_cv_resid(const float *Y, const float *cv, unsigned long long 
   const unsigned int blocks = (unsigned int)std::min<unsigned long long>(304ull, (n + 255) / 256);
   dev::cv_resid_sum_kernel<<<blocks, 256, 0, st>>>(Y, cv, n, acc);
   dev::cv_resid_coef_kernel<<<blocks, 256, 0, st>>>(Y, cv, n, acc, coef, loss_out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cv_rowsum(const float *gdm, unsigned long long n_paths, unsigned int n_hedge, float *cv,
+                             cudaStream_t st) {
+  dev::cv_rowsum_kernel<<<(unsigned int)((n_paths + 255) / 256), 256, 0, st>>>(gdm, n_paths, n_hedge, cv);
   return cudaGetLastError();
 }
 

@@ -279,7 +279,7 @@ static __device__ __noinline__ int poisson_inv(float lam, unsigned long long x, 
         ++caphits;
         break;
       }
-      p *= lam / (float)n;
+      p *= __fdividef(lam, (float)n);  // n <= cap: approximate division, 2 ulp
       F += p;
       if (p < F * 5.0e-8f) break;  // F has stopped moving: deep upper tail
     }
@@ -302,7 +302,7 @@ __device__ __forceinline__ int poisson_small(float mean, float exp_neg_mean, Xo 
     }
     u -= p;
     ++k;
-    p = mean * p / (float)k;
+    p = __fdividef(mean * p, (float)k);
   }
   return k;
 }

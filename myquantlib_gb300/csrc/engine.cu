@@ -399,6 +399,7 @@ myql_status make_plan(const myql_mc_job &job, Plan &pl, bool stepped) {
       for (int f = 0; f < pl.nf; ++f)
         fill_factor(C.f[f], m.heston[f], d.v0[f], c.scheme[f], r_part, d.dt);
     }
+    if (!pl.path_dep && (i == SC_RUP || i == SC_RDN)) C.x_shift = (float)((d.r - r) * d.T);
     // jump window: dt for path-dependent trackers, the whole (bumped) T otherwise
     const double window = pl.path_dep ? d.dt : d.T;
     if (m.jump != MYQL_JUMP_NONE) {

@@ -61,7 +61,8 @@ struct ScenarioConst {
   float jump_mean;            // Poisson mean of one jump window (dt or T)
   float jump_exp_neg_mean;    // exp(-jump_mean)
   float jump_comp;            // drift compensation of the window
-  float pad;
+  float x_shift;              // rho bumps of European instruments: log-spot shift (r' - r) T
+                              // of a scenario derived from the base path, not simulated
 };
 
 struct SimParams {

@@ -249,10 +249,18 @@ __global__ void __launch_bounds__(kSimBlock) simulate_kernel(const __grid_consta
   for (unsigned long long i = P.path_begin + s; i < P.path_end; i += S) {
     const Xo start = rng;
     const size_t col = (size_t)(i - P.rec_offset);
+    float x_base = 0.0f;
     for (int sc = 0; sc < P.n_sc; ++sc) {
-      Xo r = start;
       float f[kMaxFields];
+      if (!PD && (sc == SC_RUP || sc == SC_RDN)) {
+        // A rate bump moves only the drift: X_T(r') = X_T(r) + (r' - r) T on the same
+        // variance path and jumps (the reference re-simulates it with the same numbers).
+        P.records[(size_t)sc * F * P.rec_stride + col] = x_base + P.sc[sc].x_shift;
+        continue;
+      }
+      Xo r = start;
       sim_path<NF, S1, S2, PD>(P, P.sc[sc], r, f, caphits, fallbacks);
+      if (sc == 0) x_base = f[0];
       float *dst = P.records + (size_t)sc * F * P.rec_stride + col;
       dst[0] = f[0];
       if (PD) {

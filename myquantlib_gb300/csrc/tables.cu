@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(256) fma_peak_kernel(float *sink, float seed) 
     a4 = fmaf(a4, m, c); a5 = fmaf(a5, m, c); a6 = fmaf(a6, m, c); a7 = fmaf(a7, m, c);
   }
   const float s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
-  if (s == 12345.678f) sink[blockIdx.x] = s;
+  sink[blockIdx.x * blockDim.x + threadIdx.x] = s;  // keeps every chain live
 }
 
 // 8 independent ex2.approx chains per thread: the MUFU rate.
@@ -266,18 +266,18 @@ __global__ void __launch_bounds__(256) mufu_peak_kernel(float *sink, float seed)
   float s = 0.0f;
 #pragma unroll
   for (int j = 0; j < 8; ++j) s += a[j];
-  if (s == 12345.678f) sink[blockIdx.x] = s;
+  sink[blockIdx.x * blockDim.x + threadIdx.x] = s;  // keeps every chain live
 }
 }  // namespace dev
 
 cudaError_t run_peak_probe(int kind, int sm_count, cudaStream_t stream, double *ops_per_s) {
   float *sink = nullptr;
   cudaEvent_t e0, e1;
-  cudaError_t e = cudaMalloc(&sink, 65536 * sizeof(float));
+  const int blocks = sm_count * 8;
+  cudaError_t e = cudaMalloc(&sink, (size_t)blocks * 256 * sizeof(float));
   if (e != cudaSuccess) return e;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  const int blocks = sm_count * 8;
   double best = 0.0;
   for (int rep = 0; rep < 4 && e == cudaSuccess; ++rep) {
     cudaEventRecord(e0, stream);

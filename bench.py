@@ -214,7 +214,8 @@ def run_engine(args) -> dict:
         import torch.distributed as dist
         dist.init_process_group("nccl")
     eng = m.Engine(local)
-    streams_per_rank = 131072
+    from myquantlib_gb300.replicas import default_streams
+    streams_per_rank = default_streams(PATHS)  # disjoint stream ranges per replica
     jobs = workload_jobs(m, stream_offset=rank * streams_per_rank)
     nk = len(STRIKES)
     stream = torch.cuda.Stream(device=local)

@@ -139,7 +139,8 @@ typedef struct myql_mc_config {
   double fd_bump, vol_bump, t_bump, r_bump;
   int32_t scheme[2];  /* myql_scheme per variance factor (the Stepper's VolScheme1/2) */
   int32_t greek_mode; /* myql_greek_mode (the pricer's GreekMode template argument)   */
-  uint64_t n_streams; /* xoshiro streams (0 = default 131072, capped at num_paths)    */
+  uint64_t n_streams; /* xoshiro streams; 0 = min(num_paths, clamp(num_paths / 8,
+                         131072, 524288)); path i runs on stream i mod n_streams       */
   uint64_t stream_offset; /* index of the first stream: replicas or ranks that take
                              disjoint stream ranges draw independent paths          */
 } myql_mc_config;

@@ -78,15 +78,47 @@ template <typename T> struct MonteCarloResult<GreekMode::Full, T> {
   size_t total_steps{};
 };
 
-template <GreekMode Mode, typename T> struct MlmcResult {
-  T price{};
-  T price_std_err{};
+// MLMC results: the Greek fields exist for Essential / Full as in the reference, whose MLMC
+// pricer computes prices only (the bumped payoffs of calculate_to_buffer are discarded,
+// MultiLevelMonteCarloPricer.hpp:278-283, 320-326), so they stay zero there and here.
+template <typename T> struct MlmcLevels {
   size_t total_steps{};
   std::vector<size_t> paths_per_level{};
   std::vector<T> mean_diffs{};
   std::vector<T> var_diffs{};
   double alpha_estimated{};
   double beta_estimated{};
+};
+template <GreekMode Mode, typename T> struct MlmcResult;
+template <typename T> struct MlmcResult<GreekMode::None, T> : MlmcLevels<T> {
+  T price{};
+  T price_std_err{};
+};
+template <typename T> struct MlmcResult<GreekMode::Essential, T> : MlmcLevels<T> {
+  T price{};
+  T price_std_err{};
+  T delta{};
+  T delta_std_err{};
+  T gamma{};
+  T gamma_std_err{};
+};
+template <typename T> struct MlmcResult<GreekMode::Full, T> : MlmcLevels<T> {
+  T price{};
+  T price_std_err{};
+  T delta{};
+  T delta_std_err{};
+  T gamma{};
+  T gamma_std_err{};
+  std::array<T, 2> vega{};
+  std::array<T, 2> vega_std_err{};
+  T theta{};
+  T theta_std_err{};
+  T rho{};
+  T rho_std_err{};
+  std::array<T, 2> vanna{};
+  std::array<T, 2> vanna_std_err{};
+  T charm{};
+  T charm_std_err{};
 };
 
 // ---------------------------------------------------------------- model parameters
@@ -564,14 +596,14 @@ class MultiLevelMonteCarloPricer {
   using ResultType = typename Instrument::ResultType;
   using ReturnStruct = MlmcResult<Mode, ResultType>;
   static_assert(std::is_same_v<ResultType, double>, "MLMC prices scalar instruments");
-  static_assert(Mode == GreekMode::None, "the GPU MLMC pricer computes prices (GreekMode::None)");
 
   MultiLevelMonteCarloPricer(const Model &model, const MLMCConfig &cfg) : model_(model), cfg_(cfg) {}
 
   ReturnStruct calculate(double S0, double r, double q, const Instrument &instr) const {
     std::vector<double> strikes = detail::strikes_of(instr.strikes_);
     const myql_mc_job jb = detail::lower_job<Model, CoupledStepperType, Instrument>(
-        model_, instr, Mode, cfg_.N0, cfg_.base_steps, cfg_.seed, cfg_.fd_bump, 1e-4, 1e-4, 1e-4, S0, r, q, strikes);
+        model_, instr, GreekMode::None, cfg_.N0, cfg_.base_steps, cfg_.seed, cfg_.fd_bump, 1e-4, 1e-4, 1e-4, S0, r,
+        q, strikes);
     myql_mlmc_config mc;
     std::memset(&mc, 0, sizeof mc);
     mc.epsilon = cfg_.epsilon;

@@ -286,7 +286,7 @@ myql_status make_plan(const myql_mc_job &job, Plan &pl, bool stepped) {
   pl.M = c.num_paths;
   pl.steps = (int)c.time_steps;
   pl.T = in.maturity;
-  const uint64_t S_req = c.n_streams ? c.n_streams : kDefaultStreams;
+  const uint64_t S_req = c.n_streams ? c.n_streams : default_streams(pl.M);
   pl.S = std::min<uint64_t>(S_req, pl.M);
   if (pl.S > (1u << 26)) return set_error(MYQL_ERR_TOO_LARGE, "at most 2^26 streams");
   const double S0 = job.S0, r = job.r, q = job.q, T = in.maturity;

@@ -13,6 +13,14 @@ constexpr int kQ = 10;             // quantities (myql_quantity)
 constexpr int kSimBlock = 128;     // threads per block of the path kernels
 constexpr int kPayoffBlock = 128;  // threads per block of the payoff kernel
 constexpr uint32_t kDefaultStreams = 131072u;
+// Default xoshiro stream count of a request of M paths: min(M, clamp(M / 8, 2^17, 2^19)).
+// Large requests get more streams (at most 8 paths each up to 2^22 paths), so the path
+// kernels keep every SM full; the layout depends only on M, never on the GPU.
+inline unsigned long long default_streams(unsigned long long M) {
+  unsigned long long s = M / 8;
+  s = s < 131072ull ? 131072ull : (s > 524288ull ? 524288ull : s);
+  return s < M ? s : M;
+}
 
 // Scenario slots, in the order the reference simulates them for GreekMode::Full
 // (MonteCarloPricer.hpp:302-410).

@@ -19,11 +19,16 @@ from . import _abi
 from . import pricers as _p
 
 
+def default_streams(M: int) -> int:
+    """The engine's stream count for a request of M paths when none is given."""
+    return min(M, max(131072, min(524288, M // 8)))
+
+
 def shard_job(job: "_p._Job", rank: int, world: int) -> "_p._Job":
     """The replica of `job` that rank `rank` of `world` prices: M / W paths on the
     stream range [r S / W, (r + 1) S / W) of the request's S streams."""
     M = int(job.c.config.num_paths)
-    S = int(job.c.config.n_streams) or min(131072, M)
+    S = int(job.c.config.n_streams) or default_streams(M)
     if M % world or S % world:
         raise ValueError(f"num_paths {M} and the {S} streams must divide into {world} replicas")
     c = _abi.McJobC()                    # byte copy; the strikes array stays shared

@@ -1050,7 +1050,12 @@ int myql_oracle_mc_price(const myql_mc_job *job, int layout, int n_threads, doub
       }
     }
   } else {
-    uint64_t S = job->config.n_streams ? job->config.n_streams : 131072ull;
+    /* default stream count of the engine: min(M, clamp(M / 8, 2^17, 2^19)) */
+    uint64_t S = job->config.n_streams;
+    if (!S) {
+      S = M / 8;
+      S = S < 131072ull ? 131072ull : (S > 524288ull ? 524288ull : S);
+    }
     if (S > M) S = M;
     /* stream states: sequential jumps from the seeded generator */
     xo_t *streams = (xo_t *)malloc(S * sizeof(xo_t));

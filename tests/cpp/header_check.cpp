@@ -62,6 +62,11 @@ int main(int argc, char **argv) {
   using LbDigital = LookbackOption<PayoffCashOrNothing<OptionType::Call>, true>;
   MonteCarloPricer<MertonModel, MertonJDStepper<TrackerLookback>, LbDigital, GreekMode::Essential> p4(merton, cfg);
 
+  MLMCConfig mcfg;
+  mcfg.epsilon = 0.05;
+  MultiLevelMonteCarloPricer<HestonModel, CoupledHestonStepper<SchemeNV, TrackerBarrier<false>>,
+                             DownAndOutPut<>, GreekMode::Essential>
+      mlmc(heston, mcfg);
   if (mode == "lower") {
     std::vector<double> s;
     dump("heston_eur", p1.job(100.0, 0.02, 0.0, Eur(100.0, 1.0), s));
@@ -76,6 +81,9 @@ int main(int argc, char **argv) {
   const auto r = p1.calculate(100.0, 0.02, 0.0, Eur(100.0, 1.0));
   std::printf("{\"price\": %.17g, \"price_std_err\": %.17g, \"delta\": %.17g, \"gamma\": %.17g, \"total_steps\": %zu}\n",
               r.price, r.price_std_err, r.delta, r.gamma, r.total_steps);
+  const auto ml = mlmc.calculate(100.0, 0.02, 0.0, DownAndOutPut<>(100.0, 80.0, 1.0));
+  std::printf("{\"mlmc_price\": %.17g, \"mlmc_se\": %.17g, \"mlmc_levels\": %zu, \"mlmc_delta\": %.17g}\n",
+              ml.price, ml.price_std_err, ml.paths_per_level.size(), ml.delta);
   // an invalid request surfaces as the reference's exception type
   try {
     HestonModel bad(HestonParams{1.5, 0.04, 0.9, -0.7, 0.04});

@@ -101,4 +101,6 @@ def test_header_prices_on_the_gpu(tmp_path):
     assert abs(res["price"] - 8.628108103110) < 4 * res["price_std_err"]
     assert res["total_steps"] == (1 << 18) * 100
     assert 0.4 < res["delta"] < 0.8
-    assert lines[1]["nv_error"] == "runtime_error"
+    assert lines[1]["mlmc_levels"] >= 3 and lines[1]["mlmc_delta"] == 0.0
+    assert 1.0 < lines[1]["mlmc_price"] < 4.0 and lines[1]["mlmc_se"] > 0
+    assert lines[2]["nv_error"] == "runtime_error"

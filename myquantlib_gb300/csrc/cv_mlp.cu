@@ -57,6 +57,45 @@ __device__ __forceinline__ void epi_hidden(uint32_t tm_row, const float *bias, u
   }
 }
 
+// inference variant of epi_hidden: the SiLU in packed BF16
+__device__ __forceinline__ void epi_hidden_bf16(uint32_t tm_row, const float *bias, uint8_t *H, uint32_t row,
+                                                int c0, int c1) {
+#pragma unroll 1
+  for (int c = c0; c < c1; ++c) {
+    float v[32];
+    tc::tmem_ld32(tm_row + (uint32_t)(c * 32), v);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      uint32_t w[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int k = c * 32 + q * 8 + 2 * e;
+        w[e] = tc::silu2_bf16(v[q * 8 + 2 * e] + bias[k], v[q * 8 + 2 * e + 1] + bias[k + 1]);
+      }
+      *reinterpret_cast<uint4 *>(H + tc::img128_offset(row, (uint32_t)(c * 32 + q * 8), 128)) =
+          make_uint4(w[0], w[1], w[2], w[3]);
+    }
+  }
+}
+
+// inference variant of epi_out: SiLU in packed BF16, the dot product in FP32
+__device__ __forceinline__ float epi_out_bf16(uint32_t tm_row, const float *vec, int c0, int c1) {
+  float g = c0 == 0 ? vec[kVecB4] : 0.0f;
+#pragma unroll 1
+  for (int c = c0; c < c1; ++c) {
+    float v[32];
+    tc::tmem_ld32(tm_row + (uint32_t)(c * 32), v);
+#pragma unroll
+    for (int i = 0; i < 32; i += 2) {
+      const int k = c * 32 + i;
+      const float2 h = tc::bf16x2_to_float2(tc::silu2_bf16(v[i] + vec[kVecB3 + k], v[i + 1] + vec[kVecB3 + k + 1]));
+      g = fmaf(h.x, vec[kVecW4 + k], g);
+      g = fmaf(h.y, vec[kVecW4 + k + 1], g);
+    }
+  }
+  return g;
+}
+
 // output layer over columns [32 c0, 32 c1): sum_k silu(z3_k + b3_k) w4_k (+ b4 when c0 == 0)
 __device__ __forceinline__ float epi_out(uint32_t tm_row, const float *vec, int c0 = 0, int c1 = 4) {
   float g = c0 == 0 ? vec[kVecB4] : 0.0f;
@@ -210,21 +249,21 @@ __global__ void __launch_bounds__(kFwdThreads, 2) cv_mlp_kernel(const __grid_con
     }
     if (__syncthreads_or(!ok)) { err = true; break; }
     if (!block_wait(&bar_mma, phase)) { err = true; break; }
-    epi_hidden(tm_row, vec + kVecB1, sH, row, c0, c1);
+    epi_hidden_bf16(tm_row, vec + kVecB1, sH, row, c0, c1);
     block_sync_async();
     if (tid == 0) {
       mma_k128(tm, sH, sW2, 128, 0u);
       tc::mma_commit(&bar_mma);
     }
     if (!block_wait(&bar_mma, phase)) { err = true; break; }
-    epi_hidden(tm_row, vec + kVecB2, sH, row, c0, c1);
+    epi_hidden_bf16(tm_row, vec + kVecB2, sH, row, c0, c1);
     block_sync_async();
     if (tid == 0) {
       mma_k128(tm, sH, sW3, 128, 0u);
       tc::mma_commit(&bar_mma);
     }
     if (!block_wait(&bar_mma, phase)) { err = true; break; }
-    const float gpart = epi_out(tm_row, vec, c0, c1);
+    const float gpart = epi_out_bf16(tm_row, vec, c0, c1);
     if (half == 1) part[row] = gpart;
     tc::fence_before_sync();
     __syncthreads();

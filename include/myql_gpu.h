@@ -379,6 +379,22 @@ myql_status myql_cv_forward(myql_ctx *ctx, const float *feats, const float *dM, 
 myql_status myql_cv_gradient(myql_ctx *ctx, const float *feats, const float *dM, const float *Y,
                              uint64_t n_paths, uint32_t n_hedge, float *grad, double *loss);
 
+/* MLMC with the control variate on every level: level 0 prices plain paths
+ * minus sum_j g dM_j; level l > 0 the difference P_fine - P_coarse minus
+ * sum_j g(fine state at t_j) (dM_fine,j - dM_coarse,j), each increment centred
+ * under its own discretisation, hedged every max(1, coarse steps / 32) coarse
+ * steps.  When cv->iterations > 0 the network is first trained on plain paths
+ * of base_steps * 2^min(L_max, 5) steps (hedged every step); with 0 the
+ * context's network is used.  plain_var (optional, MYQL_MLMC_MAX_LEVELS
+ * doubles) receives the uncorrected level variances of the same paths.
+ * Scalar European, Asian and barrier instruments; every path is stepped. */
+myql_status myql_mlmc_cv_price(myql_ctx *ctx, const myql_mc_job *job, const myql_mlmc_config *mlmc,
+                               const myql_cv_config *cv, myql_mlmc_result *res, double *plain_var);
+/* One level of the above with the context's network: sums4 = {sum Y, sum Y^2,
+ * sum (Y - C), sum (Y - C)^2} of dN discounted level differences Y. */
+myql_status myql_mlmc_cv_level(myql_ctx *ctx, const myql_mc_job *job, const myql_mlmc_config *mlmc,
+                               uint32_t level, uint64_t dN, double *sums4);
+
 /* One-tile tcgen05 GEMM D[128][N] = A[128][K] * B[N][K]^T with the operands
  * rounded to BF16 and FP32 accumulation, through the shared-memory operand
  * layouts and descriptors the control-variate MLP kernels use: mode 0 K = 16,

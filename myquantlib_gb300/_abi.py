@@ -144,6 +144,10 @@ _SIGS = {
                                   C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "myql_cv_gradient": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                    C.c_uint64, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_double)]),
+    "myql_mlmc_cv_price": (C.c_int, [C.c_void_p, C.POINTER(McJobC), C.POINTER(MlmcConfigC), C.POINTER(CvConfigC),
+                                     C.POINTER(MlmcResultC), C.POINTER(C.c_double)]),
+    "myql_mlmc_cv_level": (C.c_int, [C.c_void_p, C.POINTER(McJobC), C.POINTER(MlmcConfigC), C.c_uint32,
+                                     C.c_uint64, C.POINTER(C.c_double)]),
     "myql_probe_mma": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                  C.POINTER(C.c_float)]),
 }

@@ -82,8 +82,8 @@ myql_status check_job(const myql_mc_job &job) {
   const int trk = tracker_of(job.instrument);
   if (job.instrument.is_strip || job.instrument.n_strikes != 1)
     return set_error(MYQL_ERR_UNSUPPORTED, "control variates take scalar instruments");
-  if (trk != TRK_EUROPEAN && trk != TRK_ARITH_ASIAN && trk != TRK_GEO_ASIAN)
-    return set_error(MYQL_ERR_UNSUPPORTED, "control variates cover European and Asian instruments");
+  if (trk == TRK_LOOKBACK)
+    return set_error(MYQL_ERR_UNSUPPORTED, "control variates cover European, Asian and barrier instruments");
   return MYQL_OK;
 }
 
@@ -93,6 +93,11 @@ myql_status check_cfg(const myql_cv_config *c) {
                                            "batch_paths >= 128, learning_rate > 0");
   return MYQL_OK;
 }
+
+}  // namespace
+myql_status cv_feat_consts(const myql_mc_job &job, const Plan &pl, const ScenarioConst &sc, double dt,
+                           CvFeatConsts &F);
+namespace {
 
 // Simulation constants of the control-variate kernels for one job.
 myql_status cv_plan(CtxBase *ctx, const myql_mc_job &job, const myql_cv_config &cfg, Plan &pl, CvSimParams &C,
@@ -119,19 +124,27 @@ myql_status cv_plan(CtxBase *ctx, const myql_mc_job &job, const myql_cv_config &
   C.df = pl.df;
   C.hedge_every = (int)cfg.hedge_every;
   C.n_hedge = (pl.steps + (int)cfg.hedge_every - 1) / (int)cfg.hedge_every;
+  klass = batch_class(pl.nf, pl.s1, pl.s2);
+  return cv_feat_consts(job, pl, pl.sim.sc[0], job.instrument.maturity / pl.steps, C.fc);
+}
+}  // namespace
+
+// Feature scales and the conditional mean of e^{dX} per step for one
+// discretisation (its scenario constants, step dt).
+myql_status cv_feat_consts(const myql_mc_job &job, const Plan &pl, const ScenarioConst &sc, double dt,
+                           CvFeatConsts &F) {
   const double T = job.instrument.maturity;
-  C.rq_dt = (float)((job.r - job.q) * T / pl.steps);
-  C.inv_T = (float)(1.0 / T);
+  F.rq_dt = (float)((job.r - job.q) * dt);
+  F.inv_T = (float)(1.0 / T);
   double vref = 0.0;
   if (pl.nf == 0) vref = job.model.vol * job.model.vol;
   for (int f = 0; f < pl.nf; ++f) vref += std::max(job.model.heston[f].theta, 1e-4);
-  C.x_scale = (float)(1.0 / std::sqrt(std::max(vref, 1e-6) * T));
-  C.va_scale = pl.nf >= 1 ? (float)(1.0 / std::max(job.model.heston[0].theta, 1e-4)) : 0.0f;
-  C.vb_scale = pl.nf >= 2 ? (float)(1.0 / std::max(job.model.heston[1].theta, 1e-4)) : 0.0f;
-  C.S0 = (float)job.S0;
-  klass = batch_class(pl.nf, pl.s1, pl.s2);
+  F.x_scale = (float)(1.0 / std::sqrt(std::max(vref, 1e-6) * T));
+  F.va_scale = pl.nf >= 1 ? (float)(1.0 / std::max(job.model.heston[0].theta, 1e-4)) : 0.0f;
+  F.vb_scale = pl.nf >= 2 ? (float)(1.0 / std::max(job.model.heston[1].theta, 1e-4)) : 0.0f;
+  F.S0 = (float)job.S0;
+  F.tracker = pl.tracker;
   // conditional mean of e^{dX} per step, from the FP32 constants the kernel steps with
-  const ScenarioConst &sc = pl.sim.sc[0];
   double A = 0.0, B[2] = {0.0, 0.0};
   if (pl.nf == 0) {
     A = (double)sc.gbm_drift + 0.5 * (double)sc.gbm_vol * (double)sc.gbm_vol;
@@ -162,11 +175,12 @@ myql_status cv_plan(CtxBase *ctx, const myql_mc_job &job, const myql_cv_config &
       B[f] = C1 + 0.5 * C3 + alpha;
     }
   }
-  C.mu_A = (float)A;
-  C.mu_Ba = (float)B[0];
-  C.mu_Bb = (float)B[1];
+  F.mu_A = (float)A;
+  F.mu_Ba = (float)B[0];
+  F.mu_Bb = (float)B[1];
   return MYQL_OK;
 }
+namespace {
 
 // Simulates paths [0, M) of (seed, stream_offset) into feat / dM / Y, in chunks
 // that are multiples of the stream count; `chunk_cb` consumes each chunk.
@@ -287,6 +301,47 @@ double ms_since(std::chrono::steady_clock::time_point t0) {
 }
 
 }  // namespace
+}  // namespace myql
+
+namespace myql {
+
+// One MLMC level evaluation with the context's network: simulate (features,
+// increments, discounted differences), MLP forward, FP64 sums
+// {sum Y, sum Y^2, sum (Y - C), sum (Y - C)^2} added into sums4.
+myql_status cv_level_eval(CtxBase *ctx, MlmcCvParams &Q, int klass, uint64_t dN, double *sums4) {
+  CvState &S = state(ctx);
+  if (!S.init) return set_error(MYQL_ERR_INVALID_ARG, "no control-variate network in this context");
+  const uint64_t pbs = (dN + 127) / 128, nh = (uint64_t)Q.n_hedge;
+  if (pbs * nh * kCvTileBytes > (8ull << 30)) return set_error(MYQL_ERR_TOO_LARGE, "MLMC batch above 8 GiB of features");
+  cudaError_t e = S.feat.ensure(pbs * nh * kCvTileBytes);
+  if (e == cudaSuccess) e = S.dM.ensure(pbs * nh * 128 * 4);
+  if (e == cudaSuccess) e = S.Y.ensure(pbs * 128 * 4);
+  if (e == cudaSuccess) e = S.cv.ensure(pbs * 128 * 4);
+  if (e != cudaSuccess) return cuda_status(e, "MLMC control-variate buffers");
+  Q.feat = (uint8_t *)S.feat.p;
+  Q.dM = (float *)S.dM.p;
+  Q.Y = (float *)S.Y.p;
+  Q.M.dN = dN;
+  e = launch_mlmc_cv_level(Q, klass, ctx->stream);
+  if (e != cudaSuccess) return cuda_status(e, "MLMC control-variate level launch");
+  ctx->launches++;
+  myql_status s = forward(ctx, S, (const uint8_t *)S.feat.p, (const float *)S.dM.p, dN, (uint32_t)nh,
+                          (float *)S.cv.p, nullptr);
+  if (s != MYQL_OK) return s;
+  double h4[4] = {0, 0, 0, 0};
+  e = cudaMemsetAsync(S.sums.p, 0, 32, ctx->stream);
+  if (e == cudaSuccess) e = launch_cv_reduce((const float *)S.Y.p, (const float *)S.cv.p, dN, (double *)S.sums.p, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h4, S.sums.p, 32, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_status(e, "MLMC control-variate sums");
+  ctx->launches++;
+  for (int i = 0; i < 4; ++i) sums4[i] += h4[i];
+  return MYQL_OK;
+}
+
+myql_status cv_feat_consts(const myql_mc_job &job, const Plan &pl, const ScenarioConst &sc, double dt,
+                           CvFeatConsts &F);
+
 }  // namespace myql
 
 using namespace myql;

@@ -15,7 +15,7 @@
 // the network.
 //
 // Network: 16 input slots (6 used: t/T, x-scaled log-spot, scaled v1, v2, the
-// running average to date, 1) -> 128 -> 128 -> 128 (SiLU) -> 1, BF16 weights and
+// average to date (Asian) or the knocked flag (barrier), 1) -> 128 -> 128 -> 128 (SiLU) -> 1, BF16 weights and
 // activations, FP32 accumulation on the tcgen05 tensor cores.
 //
 // Data layout (HBM): rows are (path, hedge time); a tile is 128 consecutive
@@ -56,6 +56,14 @@ constexpr int kVecB1 = 0, kVecB2 = 128, kVecB3 = 256, kVecW4 = 384, kVecB4 = 512
 
 constexpr unsigned long long kCvWaitNs = 2000000000ull;  // bounded waits: 2 s
 
+// Per-discretisation constants of the hedge features and increments.
+struct CvFeatConsts {
+  float rq_dt;                      // (r - q) dt
+  float inv_T, x_scale, va_scale, vb_scale, S0;
+  float mu_A, mu_Ba, mu_Bb;         // log E[e^{dX} | v] = mu_A + mu_Ba v1 + mu_Bb v2
+  int tracker;
+};
+
 struct CvSimParams {
   SimParams sim;        // one scenario (base), path-dependent stepping
   PayoffParams pay;     // scalar instrument
@@ -65,9 +73,7 @@ struct CvSimParams {
   float *Y;             // discounted payoff per path (launch-local index)
   unsigned long long path_begin, path_end;
   int hedge_every, n_hedge;
-  float rq_dt;          // (r - q) dt
-  float inv_T, x_scale, va_scale, vb_scale, S0;
-  float mu_A, mu_Ba, mu_Bb;  // log E[e^{dX} | v] = mu_A + mu_Ba v1 + mu_Bb v2
+  CvFeatConsts fc;
 };
 
 struct CvMlpParams {
@@ -86,13 +92,61 @@ struct CvMlpParams {
   unsigned int *status;  // [2] += 1 on a wait that ran out
 };
 
+// One MLMC level evaluation with the control variate: level 0 plain paths
+// (CvHook), level l > 0 coupled pairs (MlmcCvHook); Y = df (P_fine - P_coarse).
+struct MlmcCvParams {
+  MlmcParams M;
+  uint8_t *feat;
+  float *dM;
+  float *Y;
+  int hedge_every;  // steps (level 0) or coarse steps (level > 0) per hedge interval
+  int n_hedge;
+  CvFeatConsts fine, coarse;
+  double df;
+};
+
 namespace dev {
+
+// One feature row (IMG16 slot `lane` of a tile): t/T, scaled log-spot, scaled
+// variances, path state, 1.
+__device__ __forceinline__ void cv_write_feat(const CvFeatConsts *P, uint8_t *tile, uint32_t lane, float t,
+                                              float X, float va, float vb, float st) {
+  __nv_bfloat162 p0 = __floats2bfloat162_rn(t * P->inv_T, X * P->x_scale);
+  __nv_bfloat162 p1 = __floats2bfloat162_rn(va * P->va_scale, vb * P->vb_scale);
+  __nv_bfloat162 p2 = __floats2bfloat162_rn(st, 1.0f);
+  uint4 c0;
+  c0.x = *reinterpret_cast<uint32_t *>(&p0);
+  c0.y = *reinterpret_cast<uint32_t *>(&p1);
+  c0.z = *reinterpret_cast<uint32_t *>(&p2);
+  c0.w = 0u;
+  *reinterpret_cast<uint4 *>(tile + tc::img16_offset(lane, 0)) = c0;
+  *reinterpret_cast<uint4 *>(tile + tc::img16_offset(lane, 8)) = make_uint4(0u, 0u, 0u, 0u);
+}
+
+// Path state beside (t, X, v) after k steps of size dt: the average to date
+// (Asian) or the knocked flag of the base barrier (barrier instruments).
+__device__ __forceinline__ float cv_path_state(const CvFeatConsts *P, int k, float dt, float X, float trk,
+                                               bool hit) {
+  if (k == 0) return 0.0f;
+  if (P->tracker == TRK_ARITH_ASIAN) return dt * (0.5f + trk - 0.5f * __expf(X)) * P->inv_T;
+  if (P->tracker == TRK_GEO_ASIAN) return dt * (trk - 0.5f * X) * P->inv_T;
+  if (P->tracker >= TRK_BARRIER_UP) return hit ? 1.0f : 0.0f;
+  return 0.0f;
+}
+
+// Centred increment of the discounted asset over one step that started at m
+// (relative to S0) with log-spot increment dx = root G + drift and start
+// variances (va, vb): m e^{mu - (r-q) dt} expm1(dx - mu), mu = log E[e^{dx} | v].
+__device__ __forceinline__ float cv_step_incr(const CvFeatConsts *P, float m, float dx, float va, float vb) {
+  const float mu = fmaf(P->mu_Bb, vb, fmaf(P->mu_Ba, va, P->mu_A));
+  return m * __expf(mu - P->rq_dt) * expm1f(dx - mu);
+}
 
 // Path observer writing the features at hedge times and the centred
 // martingale increments of every hedge interval.
 struct CvHook {
   static constexpr bool active = true;
-  const CvSimParams *P;
+  const CvFeatConsts *P;
   uint8_t *tile0;  // feature tile of hedge 0 for this path's block
   float *dm0;      // dM entry of hedge 0 for this path
   uint32_t lane;
@@ -100,41 +154,21 @@ struct CvHook {
   float m, m_mid, acc, dt;
   float va_c, vb_c;  // variances at the start of the current step
 
-  __device__ __forceinline__ void write_feat(int jj, float t, float X, float va, float vb, float avg) {
-    __nv_bfloat162 p0 = __floats2bfloat162_rn(t * P->inv_T, X * P->x_scale);
-    __nv_bfloat162 p1 = __floats2bfloat162_rn(va * P->va_scale, vb * P->vb_scale);
-    __nv_bfloat162 p2 = __floats2bfloat162_rn(avg, 1.0f);
-    uint4 c0;
-    c0.x = *reinterpret_cast<uint32_t *>(&p0);
-    c0.y = *reinterpret_cast<uint32_t *>(&p1);
-    c0.z = *reinterpret_cast<uint32_t *>(&p2);
-    c0.w = 0u;
-    uint8_t *tile = tile0 + (size_t)jj * kCvTileBytes;
-    *reinterpret_cast<uint4 *>(tile + tc::img16_offset(lane, 0)) = c0;
-    *reinterpret_cast<uint4 *>(tile + tc::img16_offset(lane, 8)) = make_uint4(0u, 0u, 0u, 0u);
-  }
-  __device__ __forceinline__ float average_to_date(int k, float X, float trk) const {
-    if (k == 0) return 0.0f;
-    if (P->sim.tracker == TRK_ARITH_ASIAN) return dt * (0.5f + trk - 0.5f * __expf(X)) * P->inv_T;
-    if (P->sim.tracker == TRK_GEO_ASIAN) return dt * (trk - 0.5f * X) * P->inv_T;
-    return 0.0f;
-  }
   __device__ __forceinline__ void begin(float va, float vb) {
     m = 1.0f;
     acc = 0.0f;
     j = 0;
     va_c = va;
     vb_c = vb;
-    write_feat(0, 0.0f, 0.0f, va, vb, 0.0f);
+    cv_write_feat(P, tile0, lane, 0.0f, 0.0f, va, vb, 0.0f);
   }
   __device__ __forceinline__ void diffusion(float root, float G, float drift) {
     const float dx = fmaf(root, G, drift);
-    const float mu = fmaf(P->mu_Bb, vb_c, fmaf(P->mu_Ba, va_c, P->mu_A));
-    acc = fmaf(m * __expf(mu - P->rq_dt), expm1f(dx - mu), acc);
+    acc += cv_step_incr(P, m, dx, va_c, vb_c);
     m_mid = m * __expf(dx - P->rq_dt);
   }
   __device__ __forceinline__ void jump(float J) { acc = fmaf(m_mid, expm1f(J), acc); }
-  __device__ __forceinline__ void step_end(int k, float X, float va, float vb, float trk) {
+  __device__ __forceinline__ void step_end(int k, float X, float va, float vb, float trk, bool hit) {
     va_c = va;
     vb_c = vb;
     m = __expf(X - P->rq_dt * (float)k);
@@ -142,10 +176,64 @@ struct CvHook {
       dm0[(size_t)j * 128] = acc * P->S0;
       acc = 0.0f;
       ++j;
-      write_feat(j, (float)k * dt, X, va, vb, average_to_date(k, X, trk));
+      cv_write_feat(P, tile0 + (size_t)j * kCvTileBytes, lane, (float)k * dt, X, va, vb,
+                    cv_path_state(P, k, dt, X, trk, hit));
     }
   }
   __device__ __forceinline__ void finish() { dm0[(size_t)j * 128] = acc * P->S0; }
+};
+
+// Observer of a coupled (fine, coarse) path pair: features of the fine path at
+// the hedge times (every `hc` coarse steps) and, per hedge interval, the
+// difference of the fine and coarse centred increments -- the martingale part
+// of the level correction's asset exposure.
+struct MlmcCvHook {
+  static constexpr bool active = true;
+  const CvFeatConsts *F, *Cc;  // fine / coarse discretisation
+  uint8_t *tile0;
+  float *dm0;
+  uint32_t lane;
+  int j, hc, nc;
+  float mf, mf_mid, mc, mc_mid, acc, dtf;
+
+  __device__ __forceinline__ void begin(float va, float vb) {
+    mf = mc = 1.0f;
+    acc = 0.0f;
+    j = 0;
+    cv_write_feat(F, tile0, lane, 0.0f, 0.0f, va, vb, 0.0f);
+  }
+  __device__ __forceinline__ void fine(float root, float G, float drift, float va, float vb) {
+    const float dx = fmaf(root, G, drift);
+    acc += cv_step_incr(F, mf, dx, va, vb);
+    mf_mid = mf * __expf(dx - F->rq_dt);
+    mf = mf_mid;
+  }
+  __device__ __forceinline__ void fine_jump(float J) {
+    acc = fmaf(mf_mid, expm1f(J), acc);
+    mf = mf_mid * __expf(J);
+  }
+  __device__ __forceinline__ void coarse(float root, float G, float drift, float va, float vb) {
+    const float dx = fmaf(root, G, drift);
+    acc -= cv_step_incr(Cc, mc, dx, va, vb);
+    mc_mid = mc * __expf(dx - Cc->rq_dt);
+    mc = mc_mid;
+  }
+  __device__ __forceinline__ void coarse_jump(float J) {
+    acc = fmaf(-mc_mid, expm1f(J), acc);
+    mc = mc_mid * __expf(J);
+  }
+  __device__ __forceinline__ void coarse_end(int kc, float Xf, float Xc, float va, float vb, float trk, bool hit) {
+    mf = __expf(Xf - F->rq_dt * (float)(2 * kc));
+    mc = __expf(Xc - Cc->rq_dt * (float)kc);
+    if (kc < nc && kc % hc == 0) {
+      dm0[(size_t)j * 128] = acc * F->S0;
+      acc = 0.0f;
+      ++j;
+      cv_write_feat(F, tile0 + (size_t)j * kCvTileBytes, lane, (float)(2 * kc) * dtf, Xf, va, vb,
+                    cv_path_state(F, 2 * kc, dtf, Xf, trk, hit));
+    }
+  }
+  __device__ __forceinline__ void finish() { dm0[(size_t)j * 128] = acc * F->S0; }
 };
 
 // Terminal record -> the payoff pass's view of one path (base scenario).
@@ -157,6 +245,12 @@ __device__ __forceinline__ PathView record_view(const PayoffParams &Q, const flo
   switch (Q.tracker) {
     case TRK_GEO_ASIAN: v.Y = Q.S0 * __expf(fmaf(Q.avg_c1[0], r[1], Q.avg_c0[0])); break;
     case TRK_ARITH_ASIAN: v.Y = Q.S0 * fmaf(Q.avg_c1[0], r[1], Q.avg_c0[0]); break;
+    case TRK_BARRIER_UP:
+    case TRK_BARRIER_DOWN:
+      v.hit[0] = r[1];
+      v.hit[1] = r[2];
+      v.hit[2] = r[3];
+      break;
     default: break;
   }
   return v;
@@ -165,6 +259,7 @@ __device__ __forceinline__ PathView record_view(const PayoffParams &Q, const flo
 }  // namespace dev
 
 cudaError_t launch_cv_sim(const CvSimParams &P, int klass, cudaStream_t st);
+cudaError_t launch_mlmc_cv_level(const MlmcCvParams &Q, int klass, cudaStream_t st);
 cudaError_t launch_cv_mlp(const CvMlpParams &P, unsigned int blocks, cudaStream_t st);
 cudaError_t launch_cv_bwd(const CvMlpParams &P, unsigned int blocks, cudaStream_t st);
 cudaError_t launch_cv_pack(const float *params, uint8_t *img, float *vec, cudaStream_t st);

@@ -26,7 +26,7 @@ __global__ void __launch_bounds__(kSimBlock) cv_sim_kernel(const __grid_constant
     const unsigned long long li = i - P.path_begin;
     const unsigned long long pb = li >> 7;
     CvHook h;
-    h.P = &P;
+    h.P = &P.fc;
     h.lane = (uint32_t)(li & 127u);
     h.tile0 = P.feat + pb * (unsigned long long)P.n_hedge * kCvTileBytes;
     h.dm0 = P.dM + pb * (unsigned long long)P.n_hedge * 128ull + h.lane;

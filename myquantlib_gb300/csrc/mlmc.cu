@@ -9,14 +9,20 @@
 // one launch of mlmc_level_kernel over a persistent pool of xoshiro streams
 // that lives for the whole calculate() (the reference's rng_pool, :55-61).
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <vector>
 
+#include "cv.cuh"
 #include "engine.h"
 #include "mlmc.cuh"
 
 namespace myql {
+
+myql_status cv_level_eval(CtxBase *ctx, MlmcCvParams &Q, int klass, uint64_t dN, double *sums4);
+myql_status cv_feat_consts(const myql_mc_job &job, const Plan &pl, const ScenarioConst &sc, double dt,
+                           CvFeatConsts &F);
 
 cudaError_t launch_mlmc_f01(const MlmcParams &M, int s1, bool pd, cudaStream_t st);
 cudaError_t launch_mlmc_f2(const MlmcParams &M, int s1, int s2, bool pd, cudaStream_t st);
@@ -83,9 +89,11 @@ void asian_consts(const myql_mc_job &job, const Plan &pl, double dt, int n_steps
 
 using namespace myql;
 
+// cv: when set, every level runs with the control variate of the context's
+// network; plain_var (optional) receives the uncorrected level variances.
 static myql_status mlmc_run(myql_ctx *ctx_, const myql_mc_job *job_in, const myql_mlmc_config *cfg,
                             myql_mlmc_result *res, int probe_level, uint64_t probe_dN,
-                            double *probe_sums);
+                            double *probe_sums, bool cv = false, double *plain_var = nullptr);
 
 extern "C" myql_status myql_mlmc_price(myql_ctx *ctx_, const myql_mc_job *job_in,
                                        const myql_mlmc_config *cfg, myql_mlmc_result *res) {
@@ -101,9 +109,34 @@ extern "C" myql_status myql_mlmc_level(myql_ctx *ctx_, const myql_mc_job *job, c
   return mlmc_run(ctx_, job, cfg, &unused, (int)level, dN, sums);
 }
 
+extern "C" myql_status myql_mlmc_cv_price(myql_ctx *ctx_, const myql_mc_job *job_in, const myql_mlmc_config *cfg,
+                                          const myql_cv_config *cv_cfg, myql_mlmc_result *res,
+                                          double *plain_var) {
+  if (!res || !job_in || !cfg) return set_error(MYQL_ERR_INVALID_ARG, "null argument");
+  if (cv_cfg && cv_cfg->iterations > 0) {
+    // the network learns the hedge on plain paths of a middle level's step
+    myql_mc_job train = *job_in;
+    train.config.time_steps = cfg->base_steps << std::min<uint64_t>(cfg->L_max, 5);
+    train.config.greek_mode = MYQL_GREEKS_NONE;
+    myql_cv_config c = *cv_cfg;
+    c.hedge_every = 1;
+    const myql_status s = myql_cv_train(ctx_, &train, &c, nullptr);
+    if (s != MYQL_OK) return s;
+  }
+  return mlmc_run(ctx_, job_in, cfg, res, -1, 0, nullptr, true, plain_var);
+}
+
+extern "C" myql_status myql_mlmc_cv_level(myql_ctx *ctx_, const myql_mc_job *job, const myql_mlmc_config *cfg,
+                                          uint32_t level, uint64_t dN, double *sums4) {
+  if (!sums4 || dN == 0) return set_error(MYQL_ERR_INVALID_ARG, "need dN > 0 and an output");
+  if (cfg && level > cfg->L_max) return set_error(MYQL_ERR_INVALID_ARG, "level above L_max");
+  myql_mlmc_result unused;
+  return mlmc_run(ctx_, job, cfg, &unused, (int)level, dN, sums4, true);
+}
+
 static myql_status mlmc_run(myql_ctx *ctx_, const myql_mc_job *job_in, const myql_mlmc_config *cfg,
                             myql_mlmc_result *res, int probe_level, uint64_t probe_dN,
-                            double *probe_sums) {
+                            double *probe_sums, bool cv, double *plain_var) {
   CtxBase *ctx = reinterpret_cast<CtxBase *>(ctx_);
   if (!ctx || !job_in || !cfg || !res) return set_error(MYQL_ERR_INVALID_ARG, "null argument");
   cudaError_t e = cudaSetDevice(ctx->device);
@@ -121,8 +154,10 @@ static myql_status mlmc_run(myql_ctx *ctx_, const myql_mc_job *job_in, const myq
   job.config.fd_bump = cfg->fd_bump;
   myql_status s = validate_job(job);
   if (s != MYQL_OK) return s;
+  if (cv && tracker_of(job.instrument) == TRK_LOOKBACK)
+    return set_error(MYQL_ERR_UNSUPPORTED, "control variates cover European, Asian and barrier instruments");
   Plan pl;
-  s = make_plan(job, pl);
+  s = make_plan(job, pl, cv);  // the control variate steps every path (per-step jumps)
   if (s != MYQL_OK) return s;
   const double T = job.instrument.maturity;
   const double df = std::exp(-job.r * T);
@@ -164,6 +199,8 @@ static myql_status mlmc_run(myql_ctx *ctx_, const myql_mc_job *job_in, const myq
   }
 
   std::vector<double> host_part((size_t)max_blocks * 2);
+  std::vector<std::array<double, 2>> plain_sums(L_max + 1, {0.0, 0.0});
+  std::vector<uint64_t> plain_n(L_max + 1, 0);
   cudaEventRecord(ctx->ev0, ctx->stream);
   uint32_t launches = 0;
   auto evaluate_level = [&](size_t l, uint64_t dN, double &sum, double &sum_sq) -> myql_status {
@@ -191,6 +228,35 @@ static myql_status mlmc_run(myql_ctx *ctx_, const myql_mc_job *job_in, const myq
     M.level = (int)l;
     M.dN = dN;
     M.n_used = (unsigned int)std::min<uint64_t>(S, dN);
+    if (cv) {
+      MlmcCvParams Q;
+      std::memset(&Q, 0, sizeof Q);
+      Q.M = M;
+      Q.df = df;
+      const int n = l == 0 ? (int)cfg->base_steps : M.n_coarse;  // steps (level 0) or coarse steps
+      Q.hedge_every = std::max(1, n / 32);
+      Q.n_hedge = (n + Q.hedge_every - 1) / Q.hedge_every;
+      const double dt0 = l == 0 ? T / (double)cfg->base_steps : T / (double)fine;
+      myql_status s2 = cv_feat_consts(job, pl, M.sim.sc[0], dt0, Q.fine);
+      if (s2 == MYQL_OK && l > 0) s2 = cv_feat_consts(job, pl, M.sim.sc[1], 2.0 * dt0, Q.coarse);
+      if (s2 != MYQL_OK) return s2;
+      double s4[4] = {0, 0, 0, 0};
+      s2 = cv_level_eval(ctx, Q, batch_class(pl.nf, pl.s1, pl.s2), dN, s4);
+      if (s2 != MYQL_OK) return s2;
+      launches += 3;
+      if (probe_sums && probe_level >= 0) {  // level probe: discounted sums as they are
+        for (int i = 0; i < 4; ++i) probe_sums[i] += s4[i];
+        return MYQL_OK;
+      }
+      sum += s4[2] / df;
+      sum_sq += s4[3] / (df * df);
+      if (plain_var) {
+        plain_sums[l][0] += s4[0] / df;
+        plain_sums[l][1] += s4[1] / (df * df);
+        plain_n[l] += dN;
+      }
+      return MYQL_OK;
+    }
     cudaError_t er = launch_mlmc_level(M, pl.s1, pl.s2, pl.path_dep, ctx->stream);
     if (er != cudaSuccess) return cuda_status(er, "MLMC level launch");
     ++launches;
@@ -211,6 +277,7 @@ static myql_status mlmc_run(myql_ctx *ctx_, const myql_mc_job *job_in, const myq
 
   if (probe_level >= 0) {
     probe_sums[0] = probe_sums[1] = 0.0;
+    if (cv) probe_sums[2] = probe_sums[3] = 0.0;
     s = evaluate_level((size_t)probe_level, probe_dN, probe_sums[0], probe_sums[1]);
     if (s != MYQL_OK) return s;
     return read_status(ctx, nullptr);
@@ -312,6 +379,12 @@ static myql_status mlmc_run(myql_ctx *ctx_, const myql_mc_job *job_in, const myq
     var_total += V_l[l] / N_l[l];
   }
   res->price_std_err = std::sqrt(var_total) * df;
+  if (plain_var)
+    for (size_t l = 0; l <= L; ++l) {
+      const double n = (double)std::max<uint64_t>(plain_n[l], 1);
+      const double mean = plain_sums[l][0] / n;
+      plain_var[l] = std::max(plain_sums[l][1] / n - mean * mean, 0.0) * df * df;
+    }
   cudaEventRecord(ctx->ev1, ctx->stream);
   cudaEventSynchronize(ctx->ev1);
   float ms = 0.0f;

@@ -108,11 +108,28 @@ __device__ __forceinline__ void trk_final(const SimParams &P, const TrkState &t,
   }
 }
 
+// Observer of a coupled (fine, coarse) path pair (the control variate of the
+// level corrections); NoCoupledHook compiles away.  Each call gets the log-spot
+// increment root * G + drift of one step and the variances it started from.
+struct NoCoupledHook {
+  static constexpr bool active = false;
+  __device__ __forceinline__ void begin(float, float) {}
+  __device__ __forceinline__ void fine(float, float, float, float, float) {}
+  __device__ __forceinline__ void fine_jump(float) {}
+  __device__ __forceinline__ void coarse(float, float, float, float, float) {}
+  __device__ __forceinline__ void coarse_jump(float) {}
+  // after coarse step kc (1-based): fine and coarse log-spots, fine variances, fine
+  // tracker accumulator, fine base-barrier hit so far
+  __device__ __forceinline__ void coarse_end(int, float, float, float, float, float, bool) {}
+  __device__ __forceinline__ void finish() {}
+};
+
 // One coupled (fine, coarse) path pair.
-template <int NF, int S1, int S2, bool PD>
+template <int NF, int S1, int S2, bool PD, class Hook = NoCoupledHook>
 __device__ __forceinline__ void coupled_path(const SimParams &P, int n_coarse, Xo &rng,
                                              float (&of)[kMaxFields], float (&oc)[kMaxFields],
-                                             unsigned int &caphits, unsigned int &fallbacks) {
+                                             unsigned int &caphits, unsigned int &fallbacks,
+                                             Hook hook = Hook()) {
   const ScenarioConst &Fc = P.sc[0];  // fine constants
   const ScenarioConst &Cc = P.sc[1];  // coarse constants
   float Xf = 0.0f, Xc = 0.0f;
@@ -142,6 +159,7 @@ __device__ __forceinline__ void coupled_path(const SimParams &P, int n_coarse, X
   }
   float vf0 = Fc.f[0].v0, vf1 = Fc.f[1].v0, vc0 = Cc.f[0].v0, vc1 = Cc.f[1].v0;
   const float dtf = Fc.dt, dtc = Cc.dt;
+  if (Hook::active) hook.begin(vf0, vf1);
   for (int k = 0; k < n_coarse; ++k) {
     const float G1 = inv_normal_bits(draw(rng));
     const float G2 = inv_normal_bits(draw(rng));
@@ -150,19 +168,28 @@ __device__ __forceinline__ void coupled_path(const SimParams &P, int n_coarse, X
     if (NF == 0) {
       Xc += fmaf(Cc.gbm_vol, Gc, Cc.gbm_drift);
       Xf += fmaf(Fc.gbm_vol, G1, Fc.gbm_drift);
+      if (Hook::active) {
+        hook.coarse(Cc.gbm_vol, Gc, Cc.gbm_drift, 0.0f, 0.0f);
+        hook.fine(Fc.gbm_vol, G1, Fc.gbm_drift, 0.0f, 0.0f);
+      }
       if (PD) {
         if (P.jump_kind) j1 = jump_draw(P, Fc, rng, caphits);
         Xf += j1;
+        if (Hook::active && P.jump_kind) hook.fine_jump(j1);
         trk_update(P, tf, Xf, (float)(2 * k + 1) * dtf);
       }
       Xf += fmaf(Fc.gbm_vol, G2, Fc.gbm_drift);
+      if (Hook::active) hook.fine(Fc.gbm_vol, G2, Fc.gbm_drift, 0.0f, 0.0f);
       if (PD) {
         if (P.jump_kind) j2 = jump_draw(P, Fc, rng, caphits);
         Xf += j2;
+        if (Hook::active && P.jump_kind) hook.fine_jump(j2);
         trk_update(P, tf, Xf, (float)(2 * k + 2) * dtf);
         Xc += j1 + j2;
+        if (Hook::active && P.jump_kind) hook.coarse_jump(j1 + j2);
         trk_update(P, tc, Xc, (float)(k + 1) * dtc);
       }
+      if (Hook::active) hook.coarse_end(k + 1, Xf, Xc, 0.0f, 0.0f, tf.acc, tf.tb >= 0.0f);
       continue;
     }
     // fine step 1
@@ -171,34 +198,40 @@ __device__ __forceinline__ void coupled_path(const SimParams &P, int n_coarse, X
     const float m0 = fine_vol<S1>(vf0, rng, ff0, P, 0, Z0a, caphits, fallbacks);
     float m1 = 0.0f;
     if (NF == 2) m1 = fine_vol<S2>(vf1, rng, ff1, P, 1, Z1a, caphits, fallbacks);
-    float r1;
+    float r1, d1;
     if (NF == 1) {
       r1 = sqrt_approx(ff0.C3 * (vf0 + m0));
-      Xf += fmaf(r1, G1, fmaf(ff0.C2, m0, fmaf(ff0.C1, vf0, ff0.C0)));
+      d1 = fmaf(ff0.C2, m0, fmaf(ff0.C1, vf0, ff0.C0));
     } else {
       r1 = sqrt_approx(fmaf(ff0.C3, vf0 + m0, ff1.C3 * (vf1 + m1)));
-      Xf += fmaf(r1, G1, fmaf(ff1.C2, m1, fmaf(ff1.C1, vf1, fmaf(ff0.C2, m0, fmaf(ff0.C1, vf0, ff0.C0 + ff1.C0)))));
+      d1 = fmaf(ff1.C2, m1, fmaf(ff1.C1, vf1, fmaf(ff0.C2, m0, fmaf(ff0.C1, vf0, ff0.C0 + ff1.C0))));
     }
+    Xf += fmaf(r1, G1, d1);
+    if (Hook::active) hook.fine(r1, G1, d1, vf0, vf1);
     if (PD) {
       if (P.jump_kind) j1 = jump_draw(P, Fc, rng, caphits);
       Xf += j1;
+      if (Hook::active && P.jump_kind) hook.fine_jump(j1);
       trk_update(P, tf, Xf, (float)(2 * k + 1) * dtf);
     }
     // fine step 2
     const float n0 = fine_vol<S1>(m0, rng, ff0, P, 0, Z0b, caphits, fallbacks);
     float n1 = 0.0f;
     if (NF == 2) n1 = fine_vol<S2>(m1, rng, ff1, P, 1, Z1b, caphits, fallbacks);
-    float r2;
+    float r2, d2;
     if (NF == 1) {
       r2 = sqrt_approx(ff0.C3 * (m0 + n0));
-      Xf += fmaf(r2, G2, fmaf(ff0.C2, n0, fmaf(ff0.C1, m0, ff0.C0)));
+      d2 = fmaf(ff0.C2, n0, fmaf(ff0.C1, m0, ff0.C0));
     } else {
       r2 = sqrt_approx(fmaf(ff0.C3, m0 + n0, ff1.C3 * (m1 + n1)));
-      Xf += fmaf(r2, G2, fmaf(ff1.C2, n1, fmaf(ff1.C1, m1, fmaf(ff0.C2, n0, fmaf(ff0.C1, m0, ff0.C0 + ff1.C0)))));
+      d2 = fmaf(ff1.C2, n1, fmaf(ff1.C1, m1, fmaf(ff0.C2, n0, fmaf(ff0.C1, m0, ff0.C0 + ff1.C0))));
     }
+    Xf += fmaf(r2, G2, d2);
+    if (Hook::active) hook.fine(r2, G2, d2, m0, m1);
     if (PD) {
       if (P.jump_kind) j2 = jump_draw(P, Fc, rng, caphits);
       Xf += j2;
+      if (Hook::active && P.jump_kind) hook.fine_jump(j2);
       trk_update(P, tf, Xf, (float)(2 * k + 2) * dtf);
     }
     // coarse step
@@ -206,22 +239,28 @@ __device__ __forceinline__ void coupled_path(const SimParams &P, int n_coarse, X
     float c1n = 0.0f;
     if (NF == 2) c1n = S2 == SCH_NV ? nv_step(vc1, (Z1a + Z1b) * 0.70710678118654752f, fc1) : n1;
     if (r1 + r2 > 1e-15f) Gc = (r1 * G1 + r2 * G2) * rsqrtf(fmaf(r1, r1, r2 * r2));
+    float rc, dc;
     if (NF == 1) {
-      const float rc = sqrt_approx(fc0.C3 * (vc0 + c0n));
-      Xc += fmaf(rc, Gc, fmaf(fc0.C2, c0n, fmaf(fc0.C1, vc0, fc0.C0)));
+      rc = sqrt_approx(fc0.C3 * (vc0 + c0n));
+      dc = fmaf(fc0.C2, c0n, fmaf(fc0.C1, vc0, fc0.C0));
     } else {
-      const float rc = sqrt_approx(fmaf(fc0.C3, vc0 + c0n, fc1.C3 * (vc1 + c1n)));
-      Xc += fmaf(rc, Gc, fmaf(fc1.C2, c1n, fmaf(fc1.C1, vc1, fmaf(fc0.C2, c0n, fmaf(fc0.C1, vc0, fc0.C0 + fc1.C0)))));
+      rc = sqrt_approx(fmaf(fc0.C3, vc0 + c0n, fc1.C3 * (vc1 + c1n)));
+      dc = fmaf(fc1.C2, c1n, fmaf(fc1.C1, vc1, fmaf(fc0.C2, c0n, fmaf(fc0.C1, vc0, fc0.C0 + fc1.C0))));
     }
+    Xc += fmaf(rc, Gc, dc);
+    if (Hook::active) hook.coarse(rc, Gc, dc, vc0, vc1);
     vf0 = n0;
     vf1 = n1;
     vc0 = c0n;
     vc1 = c1n;
     if (PD) {
       Xc += j1 + j2;
+      if (Hook::active && P.jump_kind) hook.coarse_jump(j1 + j2);
       trk_update(P, tc, Xc, (float)(k + 1) * dtc);
     }
+    if (Hook::active) hook.coarse_end(k + 1, Xf, Xc, vf0, vf1, PD ? tf.acc : 0.0f, PD && tf.tb >= 0.0f);
   }
+  if (Hook::active) hook.finish();
   if (PD) {
     trk_final(P, tf, Xf, dtf, of);
     trk_final(P, tc, Xc, dtc, oc);

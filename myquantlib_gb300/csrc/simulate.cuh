@@ -107,8 +107,8 @@ struct NoHook {
   // log-spot increment of the step: root * G + drift, G ~ N(0,1) independent of the variances
   __device__ __forceinline__ void diffusion(float, float, float) {}
   __device__ __forceinline__ void jump(float) {}
-  // after step k (1-based): log-spot, variances, tracker accumulator
-  __device__ __forceinline__ void step_end(int, float, float, float, float) {}
+  // after step k (1-based): log-spot, variances, tracker accumulator, base barrier hit so far
+  __device__ __forceinline__ void step_end(int, float, float, float, float, bool) {}
   __device__ __forceinline__ void finish() {}
 };
 
@@ -197,7 +197,7 @@ __device__ __forceinline__ void sim_path_h(const SimParams &P, const ScenarioCon
           default: break;
         }
       }
-      if (Hook::active) hook.step_end(k + 1, X, va, vb, acc);
+      if (Hook::active) hook.step_end(k + 1, X, va, vb, acc, tb >= 0.0f);
     }
     if (!PD && (NF > 0 || Hook::active) && P.jump_kind) {
       const float J = jump_draw(P, C, rng, caphits);

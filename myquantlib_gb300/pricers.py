@@ -494,6 +494,21 @@ class Engine:
         _abi.check(self.lib.myql_cv_price(self.handle, C.byref(job.c), C.byref(cfg), C.byref(res)))
         return res
 
+    def mlmc_cv_price(self, job: "_Job", mlmc_cfg: "_abi.MlmcConfigC", cv_cfg: "_abi.CvConfigC | None"):
+        """MLMC with the control variate on every level -> (result, plain level variances)."""
+        res = _abi.MlmcResultC()
+        pv = np.zeros(_abi.MLMC_MAX_LEVELS)
+        _abi.check(self.lib.myql_mlmc_cv_price(self.handle, C.byref(job.c), C.byref(mlmc_cfg),
+                                               C.byref(cv_cfg) if cv_cfg is not None else None, C.byref(res),
+                                               _ptr(pv)))
+        return res, pv
+
+    def mlmc_cv_level(self, job: "_Job", mlmc_cfg: "_abi.MlmcConfigC", level: int, dN: int) -> np.ndarray:
+        out = np.zeros(4)
+        _abi.check(self.lib.myql_mlmc_cv_level(self.handle, C.byref(job.c), C.byref(mlmc_cfg), level, dN,
+                                               _ptr(out)))
+        return out
+
     def paths(self, job: "_Job") -> np.ndarray:
         nsc, nf = C.c_uint32(), C.c_uint32()
         _abi.check(self.lib.myql_mc_paths(self.handle, C.byref(job.c), None, 0, C.byref(nsc),

@@ -101,3 +101,46 @@ def test_mlmc_european_against_fourier(engine):
     assert abs(g.price - four) < 4 * g.price_std_err + cfg.epsilon / np.sqrt(2.0), (g.price, four)
     # the level differences decay (weak order estimate positive)
     assert g.alpha_estimated > 0.3
+
+
+# ---------------------------------------------------------------- MLMC with the neural control variate
+def cv_cfg_c(iterations=200, pilot=1 << 16):
+    return m.pricers.ControlVariateConfig(hedge_every=1, iterations=iterations, pilot_paths=pilot,
+                                          batch_paths=4096, learning_rate=3e-3, seed=7).c()
+
+
+@pytest.mark.parametrize("name", ["c5_do_put", "heston_eur"])
+def test_mlmc_cv_levels_unbiased_and_reduced(engine, name):
+    j = CASES[name]()
+    cfg = mlmc_cfg(0.01, L_max=8, streams=4096)
+    train = CASES[name]()
+    train.c.config.time_steps = 32
+    engine.cv_train(train, cv_cfg_c())
+    dN = 1 << 16
+    ratios = []
+    for level in (0, 2, 4):
+        s = engine.mlmc_cv_level(j, cfg, level, dN)
+        my, mz = s[0] / dN, s[2] / dN
+        vy, vz = max(s[1] / dN - my * my, 0.0), max(s[3] / dN - mz * mz, 0.0)
+        # E[C] = 0: the corrected and plain level means differ by mean(C), whose SE is
+        # at most (sd(Y) + sd(Y - C)) / sqrt(dN)
+        bound = 4.0 * (np.sqrt(vy) + np.sqrt(vz)) / np.sqrt(dN)
+        assert abs(mz - my) < bound + 1e-9, (level, my, mz, bound)
+        ratios.append(vy / max(vz, 1e-30))
+    assert ratios[0] > 3.0, ratios  # the plain level (one step here) gains most
+
+
+def test_mlmc_cv_price_against_plain_mlmc(engine, oracle_lib):
+    j = CASES["c5_do_put"]()
+    cfg = mlmc_cfg(0.01, L_max=8)
+    plain = run_mlmc(engine, j, cfg)
+    res, plain_var = engine.mlmc_cv_price(j, cfg, cv_cfg_c())
+    se = np.hypot(res.price_std_err, plain.price_std_err)
+    assert abs(res.price - plain.price) < 4 * se + cfg.epsilon, (res.price, plain.price, se)
+    r = oracle_lib.mlmc_price(j, cfg, oracle_lib.LAYOUT_REFERENCE, 8)
+    assert abs(res.price - r.price) < 4 * np.hypot(res.price_std_err, r.price_std_err) + cfg.epsilon
+    n = res.n_levels
+    v_cv = np.array([res.var_diffs[l] for l in range(n)])
+    assert v_cv[0] < plain_var[0] / 3.0, (v_cv[0], plain_var[0])
+    # fewer level-0 paths for the same target accuracy
+    assert res.paths_per_level[0] < plain.paths_per_level[0]

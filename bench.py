@@ -471,6 +471,60 @@ def run_cv(args) -> dict:
             "time_to_se": res, "clocks": clk.summary()}
 
 
+def run_mlmc(args) -> dict:
+    """MLMC down-and-out put (Heston kappa 2, theta .04, sigma .5, rho -.7, v0 .04, SchemeNV,
+    K 100, B 80, T 1; levels 2..10, dt = T / 2^l; target RMSE 1e-3 x price): plain MLMC
+    against MLMC with the neural control variate on every level (training included), both
+    through the public API, wall-clock."""
+    import myquantlib_gb300 as m
+    from myquantlib_gb300 import _abi
+    if int(os.environ.get("RANK", "0")) != 0:
+        return {}
+    eng = m.Engine(0)
+    model = m.HestonModel(m.HestonParams(2.0, 0.04, 0.5, -0.7, 0.04))
+    job = m.make_job(model, m.HestonStepper(m.SchemeNV, m.TrackerBarrier), m.DownAndOutPut(100.0, 80.0, 1.0),
+                     m.GreekMode.NONE, m.MonteCarloConfig(num_paths=1 << 20, time_steps=1024), 100.0, 0.02, 0.0)
+    raw, _ = eng.price(job)
+    price = float(raw[0, 0])
+
+    def cfg(eps):
+        c = _abi.MlmcConfigC()
+        c.epsilon, c.L_min, c.L_max, c.N0, c.base_steps = eps, 2, 10, 10000, 1
+        c.alpha, c.beta, c.adaptive_rates, c.seed, c.fd_bump, c.n_streams = 2.0, 1.0, 1, 42, 1e-4, 0
+        return c
+
+    cvc = m.pricers.ControlVariateConfig(hedge_every=1, iterations=200, pilot_paths=1 << 16, batch_paths=4096,
+                                         learning_rate=3e-3, seed=7).c()
+    eps = 1e-3 * price
+    # warm-up (tables, streams, first launches)
+    eng.mlmc_cv_price(job, cfg(20 * eps), cvc)
+    res_plain = _abi.MlmcResultC()
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        _abi.check(eng.lib.myql_mlmc_price(eng.handle, m.pricers.C.byref(job.c), m.pricers.C.byref(cfg(eps)),
+                                           m.pricers.C.byref(res_plain)))
+        t_plain = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        res_cv, plain_var = eng.mlmc_cv_price(job, cfg(eps), cvc)
+        t_cv = time.perf_counter() - t0
+    nl = res_cv.n_levels
+    return {"metric": "time-to-RMSE (s) MLMC + neural CV vs plain MLMC", "value": t_cv, "unit": "s", "n_gpus": 1,
+            "steps": 1, "warmup": 1, "ms_per_step": t_cv * 1e3, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 paths, fp64 level sums, bf16 MLP", "data": "synthetic",
+            "config": {"workload": "MLMC Heston down-and-out put, SchemeNV, levels 2..10", "epsilon": eps,
+                       "price": price},
+            "plain": {"s": t_plain, "price": res_plain.price, "se": res_plain.price_std_err,
+                      "levels": int(res_plain.n_levels),
+                      "paths_per_level": [int(res_plain.paths_per_level[l]) for l in range(res_plain.n_levels)],
+                      "path_steps": int(res_plain.total_steps)},
+            "cv": {"s": t_cv, "price": res_cv.price, "se": res_cv.price_std_err, "levels": int(nl),
+                   "paths_per_level": [int(res_cv.paths_per_level[l]) for l in range(nl)],
+                   "variance_ratio_per_level": [float(plain_var[l] / max(res_cv.var_diffs[l], 1e-300))
+                                                for l in range(nl)],
+                   "path_steps": int(res_cv.total_steps)},
+            "speedup": t_plain / t_cv, "clocks": clk.summary()}
+
+
 def run_ncu_cv_case() -> None:
     """A small control-variate case for ncu: 2^16 pilot paths, 40 Adam steps, 2^18 priced paths."""
     import myquantlib_gb300 as m
@@ -498,7 +552,7 @@ def main():
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
     ap.add_argument("--cpu-paths", type=int, default=8192, help="paths of the smaller CPU-baseline sample")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
-    ap.add_argument("--workload", choices=["strip", "batch", "cv"], default="strip",
+    ap.add_argument("--workload", choices=["strip", "batch", "cv", "mlmc"], default="strip",
                     help="strip: the Bates Full-Greeks strip (headline); batch: uneven requests in one launch; "
                          "cv: time-to-relative-SE of the neural control variate against plain MC")
     ap.add_argument("--batch-jobs", type=int, default=4096)
@@ -516,7 +570,7 @@ def main():
     if args.impl == "reference":
         line = run_reference(args)
     else:
-        line = {"batch": run_batch, "cv": run_cv}.get(args.workload, run_engine)(args)
+        line = {"batch": run_batch, "cv": run_cv, "mlmc": run_mlmc}.get(args.workload, run_engine)(args)
     if line:
         print(json.dumps(line), flush=True)
 

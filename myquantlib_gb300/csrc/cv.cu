@@ -311,30 +311,38 @@ namespace myql {
 myql_status cv_level_eval(CtxBase *ctx, MlmcCvParams &Q, int klass, uint64_t dN, double *sums4) {
   CvState &S = state(ctx);
   if (!S.init) return set_error(MYQL_ERR_INVALID_ARG, "no control-variate network in this context");
-  const uint64_t pbs = (dN + 127) / 128, nh = (uint64_t)Q.n_hedge;
-  if (pbs * nh * kCvTileBytes > (8ull << 30)) return set_error(MYQL_ERR_TOO_LARGE, "MLMC batch above 8 GiB of features");
+  // chunks of a multiple of the streams in use (every stream continues its own paths)
+  // with at most ~2 GiB of features
+  const uint64_t U = Q.M.n_used, nh = (uint64_t)Q.n_hedge;
+  uint64_t chunk = (2ull << 30) / (nh * (kCvTileBytes / 128 + 4));
+  chunk = std::max<uint64_t>(U, chunk / U * U);
+  chunk = std::min<uint64_t>(chunk, dN);
+  const uint64_t pbs = (chunk + 127) / 128;
   cudaError_t e = S.feat.ensure(pbs * nh * kCvTileBytes);
   if (e == cudaSuccess) e = S.dM.ensure(pbs * nh * 128 * 4);
   if (e == cudaSuccess) e = S.Y.ensure(pbs * 128 * 4);
   if (e == cudaSuccess) e = S.cv.ensure(pbs * 128 * 4);
+  if (e == cudaSuccess) e = cudaMemsetAsync(S.sums.p, 0, 32, ctx->stream);
   if (e != cudaSuccess) return cuda_status(e, "MLMC control-variate buffers");
   Q.feat = (uint8_t *)S.feat.p;
   Q.dM = (float *)S.dM.p;
   Q.Y = (float *)S.Y.p;
-  Q.M.dN = dN;
-  e = launch_mlmc_cv_level(Q, klass, ctx->stream);
-  if (e != cudaSuccess) return cuda_status(e, "MLMC control-variate level launch");
-  ctx->launches++;
-  myql_status s = forward(ctx, S, (const uint8_t *)S.feat.p, (const float *)S.dM.p, dN, (uint32_t)nh,
-                          (float *)S.cv.p, nullptr);
-  if (s != MYQL_OK) return s;
+  for (uint64_t done = 0; done < dN; done += chunk) {
+    const uint64_t n = std::min(chunk, dN - done);
+    Q.M.dN = n;
+    e = launch_mlmc_cv_level(Q, klass, ctx->stream);
+    if (e != cudaSuccess) return cuda_status(e, "MLMC control-variate level launch");
+    myql_status s = forward(ctx, S, (const uint8_t *)S.feat.p, (const float *)S.dM.p, n, (uint32_t)nh,
+                            (float *)S.cv.p, nullptr);
+    if (s != MYQL_OK) return s;
+    e = launch_cv_reduce((const float *)S.Y.p, (const float *)S.cv.p, n, (double *)S.sums.p, ctx->stream);
+    if (e != cudaSuccess) return cuda_status(e, "MLMC control-variate reduction");
+    ctx->launches += 2;
+  }
   double h4[4] = {0, 0, 0, 0};
-  e = cudaMemsetAsync(S.sums.p, 0, 32, ctx->stream);
-  if (e == cudaSuccess) e = launch_cv_reduce((const float *)S.Y.p, (const float *)S.cv.p, dN, (double *)S.sums.p, ctx->stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(h4, S.sums.p, 32, cudaMemcpyDeviceToHost, ctx->stream);
+  e = cudaMemcpyAsync(h4, S.sums.p, 32, cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_status(e, "MLMC control-variate sums");
-  ctx->launches++;
   for (int i = 0; i < 4; ++i) sums4[i] += h4[i];
   return MYQL_OK;
 }

@@ -23,6 +23,7 @@
 // the whole block leave its tile loop, waits (bounded) for its own bulk
 // copies in flight and frees its TMEM.
 #include <algorithm>
+#include <atomic>
 
 #include "cv.cuh"
 
@@ -55,45 +56,6 @@ __device__ __forceinline__ void epi_hidden(uint32_t tm_row, const float *bias, u
           make_uint4(w[0], w[1], w[2], w[3]);
     }
   }
-}
-
-// inference variant of epi_hidden: the SiLU in packed BF16
-__device__ __forceinline__ void epi_hidden_bf16(uint32_t tm_row, const float *bias, uint8_t *H, uint32_t row,
-                                                int c0, int c1) {
-#pragma unroll 1
-  for (int c = c0; c < c1; ++c) {
-    float v[32];
-    tc::tmem_ld32(tm_row + (uint32_t)(c * 32), v);
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      uint32_t w[4];
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const int k = c * 32 + q * 8 + 2 * e;
-        w[e] = tc::silu2_bf16(v[q * 8 + 2 * e] + bias[k], v[q * 8 + 2 * e + 1] + bias[k + 1]);
-      }
-      *reinterpret_cast<uint4 *>(H + tc::img128_offset(row, (uint32_t)(c * 32 + q * 8), 128)) =
-          make_uint4(w[0], w[1], w[2], w[3]);
-    }
-  }
-}
-
-// inference variant of epi_out: SiLU in packed BF16, the dot product in FP32
-__device__ __forceinline__ float epi_out_bf16(uint32_t tm_row, const float *vec, int c0, int c1) {
-  float g = c0 == 0 ? vec[kVecB4] : 0.0f;
-#pragma unroll 1
-  for (int c = c0; c < c1; ++c) {
-    float v[32];
-    tc::tmem_ld32(tm_row + (uint32_t)(c * 32), v);
-#pragma unroll
-    for (int i = 0; i < 32; i += 2) {
-      const int k = c * 32 + i;
-      const float2 h = tc::bf16x2_to_float2(tc::silu2_bf16(v[i] + vec[kVecB3 + k], v[i + 1] + vec[kVecB3 + k + 1]));
-      g = fmaf(h.x, vec[kVecW4 + k], g);
-      g = fmaf(h.y, vec[kVecW4 + k + 1], g);
-    }
-  }
-  return g;
 }
 
 // output layer over columns [32 c0, 32 c1): sum_k silu(z3_k + b3_k) w4_k (+ b4 when c0 == 0)
@@ -249,21 +211,21 @@ __global__ void __launch_bounds__(kFwdThreads, 2) cv_mlp_kernel(const __grid_con
     }
     if (__syncthreads_or(!ok)) { err = true; break; }
     if (!block_wait(&bar_mma, phase)) { err = true; break; }
-    epi_hidden_bf16(tm_row, vec + kVecB1, sH, row, c0, c1);
+    epi_hidden(tm_row, vec + kVecB1, sH, row, c0, c1);
     block_sync_async();
     if (tid == 0) {
       mma_k128(tm, sH, sW2, 128, 0u);
       tc::mma_commit(&bar_mma);
     }
     if (!block_wait(&bar_mma, phase)) { err = true; break; }
-    epi_hidden_bf16(tm_row, vec + kVecB2, sH, row, c0, c1);
+    epi_hidden(tm_row, vec + kVecB2, sH, row, c0, c1);
     block_sync_async();
     if (tid == 0) {
       mma_k128(tm, sH, sW3, 128, 0u);
       tc::mma_commit(&bar_mma);
     }
     if (!block_wait(&bar_mma, phase)) { err = true; break; }
-    const float gpart = epi_out_bf16(tm_row, vec, c0, c1);
+    const float gpart = epi_out(tm_row, vec, c0, c1);
     if (half == 1) part[row] = gpart;
     tc::fence_before_sync();
     __syncthreads();
@@ -658,27 +620,38 @@ cudaError_t launch_cv_beta(const float *Y, const float *dM, unsigned long long n
 static constexpr uint32_t kFwdSmem = kImgFwdBytes + 32768u + 2u * kCvTileBytes + 1024u;
 static constexpr uint32_t kBwdSmem = 196608u + 1024u;
 
+// Function attributes are set once per device (a bit per device ordinal).
+static bool attr_needed(std::atomic<unsigned long long> &done) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev >= 64) return true;
+  return (done.load() >> dev & 1ull) == 0;
+}
+static void attr_set(std::atomic<unsigned long long> &done) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess && dev < 64) done.fetch_or(1ull << dev);
+}
+
 cudaError_t launch_cv_mlp(const CvMlpParams &P, unsigned int blocks, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
+  static std::atomic<unsigned long long> attr{0};
+  if (attr_needed(attr)) {
     cudaError_t e = cudaFuncSetAttribute(dev::cv_mlp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem);
     // two blocks per SM (2 x ~113 KB) need the full shared-memory carveout
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(dev::cv_mlp_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
                                (int)cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return e;
-    attr = true;
+    attr_set(attr);
   }
   dev::cv_mlp_kernel<<<blocks, dev::kFwdThreads, kFwdSmem, st>>>(P);
   return cudaGetLastError();
 }
 
 cudaError_t launch_cv_bwd(const CvMlpParams &P, unsigned int blocks, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
+  static std::atomic<unsigned long long> attr{0};
+  if (attr_needed(attr)) {
     cudaError_t e = cudaFuncSetAttribute(dev::cv_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem);
     if (e != cudaSuccess) return e;
-    attr = true;
+    attr_set(attr);
   }
   dev::cv_bwd_kernel<<<blocks, dev::kBwdThreads, kBwdSmem, st>>>(P);
   return cudaGetLastError();

@@ -164,20 +164,6 @@ __device__ __forceinline__ float silu(float z) {
   const float h = 0.5f * z;
   return fmaf(h, tanh_fast(h), h);
 }
-// Two SiLUs in packed BF16 (inference epilogues, whose activations are stored in
-// BF16 anyway): h = z / 2, silu = h + h tanh(h), one tanh.approx.bf16x2 per pair.
-__device__ __forceinline__ uint32_t silu2_bf16(float za, float zb) {
-  __nv_bfloat162 h = __floats2bfloat162_rn(0.5f * za, 0.5f * zb);
-  uint32_t hu = *reinterpret_cast<uint32_t *>(&h), tu;
-  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(tu) : "r"(hu));
-  const __nv_bfloat162 t = *reinterpret_cast<__nv_bfloat162 *>(&tu);
-  const __nv_bfloat162 r = __hfma2(h, t, h);
-  return *reinterpret_cast<const uint32_t *>(&r);
-}
-__device__ __forceinline__ float2 bf16x2_to_float2(uint32_t u) {
-  return make_float2(__uint_as_float(u << 16), __uint_as_float(u & 0xFFFF0000u));
-}
-
 // d silu / dz = s (1 + z (1 - s)), s = sigmoid(z) = 0.5 (1 + tanh(z / 2))
 __device__ __forceinline__ float silu_grad(float z) {
   const float s = fmaf(0.5f, tanh_fast(0.5f * z), 0.5f);

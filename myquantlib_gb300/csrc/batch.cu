@@ -45,10 +45,35 @@ struct BatchState : ExtState {
   std::map<uint64_t, DevBuf> seed_tables;  // seed -> [4][kDefaultStreams] states
   cudaGraphExec_t graph = nullptr;
   uint64_t graph_key = 0;
-  std::map<uint64_t, unsigned int> tuned_blocks;  // shape signature -> persistent grid
+  std::map<uint64_t, unsigned int> tuned_blocks;  // (segment class, shape) -> persistent grid
+  static constexpr int kSide = 4;                  // side streams of the concurrent class kernels
+  cudaStream_t side[kSide] = {};
+  cudaEvent_t fork = nullptr, join[kSide] = {};
+  cudaError_t ensure_streams() {
+    if (fork) return cudaSuccess;
+    cudaError_t e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+    for (int i = 0; i < kSide && e == cudaSuccess; ++i) {
+      e = cudaStreamCreateWithFlags(&side[i], cudaStreamNonBlocking);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&join[i], cudaEventDisableTiming);
+    }
+    return e;
+  }
   ~BatchState() {
     if (graph) cudaGraphExecDestroy(graph);
+    for (int i = 0; i < kSide; ++i) {
+      if (side[i]) cudaStreamDestroy(side[i]);
+      if (join[i]) cudaEventDestroy(join[i]);
+    }
+    if (fork) cudaEventDestroy(fork);
   }
+};
+
+// Items of one kernel class (klass, path dependence): [begin, end) of the sorted list.
+struct Segment {
+  int klass;
+  bool pd;
+  uint64_t begin, end;
+  unsigned int blocks;
 };
 
 uint64_t mix(uint64_t h, uint64_t v) { return (h ^ v) * 0x100000001b3ull + (h >> 29); }
@@ -142,6 +167,7 @@ extern "C" myql_status myql_mc_price_batch(myql_ctx *ctx_, const myql_mc_job *jo
   unsigned int *hs = (unsigned int *)B.h_slots.p;
   std::vector<double> strikes(n_jobs);
   std::vector<double> cost(total_items);
+  std::vector<int> seg_key(total_items);  // 2 klass + path dependence
   uint64_t item = 0;
   uint64_t signature = 0;
   // NCI tables: a later job may grow (reallocate) a table an earlier job of the
@@ -180,13 +206,25 @@ extern "C" myql_status myql_mc_price_batch(myql_ctx *ctx_, const myql_mc_job *jo
       hi[item].job = (unsigned int)j;
       hi[item].stream0 = (unsigned int)(k * kBatchItemStreams);
       cost[item] = per_stream;
+      seg_key[item] = 2 * J.klass + (pl.path_dep ? 1 : 0);
     }
-    signature = mix(signature, (uint64_t)J.klass * 1315423911ull + pl.steps);
+    signature = mix(signature, (uint64_t)J.klass * 1315423911ull + pl.steps * 2 + (pl.path_dep ? 1 : 0));
   }
-  // longest items first; slot = item index in job order (finalize sums slots in order)
+  // grouped by kernel class, longest items first within a class; slot = item index in
+  // job order (finalize sums slots in order)
   std::vector<uint64_t> order(total_items);
   std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(), [&](uint64_t a, uint64_t b) { return cost[a] > cost[b]; });
+  std::stable_sort(order.begin(), order.end(), [&](uint64_t a, uint64_t b) {
+    return seg_key[a] != seg_key[b] ? seg_key[a] < seg_key[b] : cost[a] > cost[b];
+  });
+  std::vector<Segment> segs;
+  for (uint64_t k = 0; k < total_items; ++k) {
+    const int key = seg_key[order[k]];
+    if (segs.empty() || 2 * segs.back().klass + (segs.back().pd ? 1 : 0) != key)
+      segs.push_back({key / 2, (key & 1) != 0, k, k, 0u});
+    segs.back().end = k + 1;
+  }
+  if (segs.size() > 64) return set_error(MYQL_ERR_TOO_LARGE, "too many kernel classes");
   {
     std::vector<BatchItem> tmp(hi, hi + total_items);
     for (uint64_t k = 0; k < total_items; ++k) {
@@ -197,73 +235,102 @@ extern "C" myql_status myql_mc_price_batch(myql_ctx *ctx_, const myql_mc_job *jo
   e = cudaMemcpyAsync(ctx->strikes.p, strikes.data(), n_jobs * sizeof(double), cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return cuda_status(e, "batch strikes");
 
-  BatchParams P;
-  P.jobs = (const BatchJob *)B.d_jobs.p;
-  P.items = (const BatchItem *)B.d_items.p;
-  P.item_slot = (const unsigned int *)B.d_slots.p;
-  P.n_items = total_items;
-  P.counter = (unsigned int *)B.d_counter.p;
-  P.partials = (double *)B.d_partials.p;
+  e = B.ensure_streams();
+  if (e != cudaSuccess) return cuda_status(e, "batch streams");
+  auto params_of = [&](const Segment &g, size_t gi) {
+    BatchParams P;
+    P.jobs = (const BatchJob *)B.d_jobs.p;
+    P.items = (const BatchItem *)B.d_items.p;
+    P.item_slot = (const unsigned int *)B.d_slots.p;
+    P.item_begin = g.begin;
+    P.item_end = g.end;
+    P.counter = (unsigned int *)B.d_counter.p + gi;
+    P.partials = (double *)B.d_partials.p;
+    return P;
+  };
 
-  // ---- autotune the persistent grid once per batch shape
-  const int occ = batch_blocks_per_sm();
+  // ---- autotune the persistent grid of each class segment once per batch shape:
+  // candidates on the segment's leading (most expensive) items
   signature = mix(signature, n_jobs);
-  unsigned int blocks = (unsigned int)(occ * ctx->sm_count);
-  auto tuned = B.tuned_blocks.find(signature);
-  if (tuned != B.tuned_blocks.end()) {
-    blocks = tuned->second;
-  } else if (total_items > (uint64_t)8 * occ * ctx->sm_count) {
-    // candidates on the leading (most expensive) items of this batch
-    const unsigned int cands[3] = {(unsigned int)(occ * ctx->sm_count),
-                                   (unsigned int)std::max(1, occ / 2) * (unsigned int)ctx->sm_count,
-                                   (unsigned int)ctx->sm_count};
-    BatchParams T = P;
-    T.n_items = std::min<uint64_t>(total_items, (uint64_t)4 * occ * ctx->sm_count);
-    e = cudaMemcpyAsync(B.d_jobs.p, hj, n_jobs * sizeof(BatchJob), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(B.d_items.p, hi, T.n_items * sizeof(BatchItem), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(B.d_slots.p, hs, T.n_items * sizeof(unsigned int), cudaMemcpyHostToDevice, st);
-    float best = 1e30f;
-    for (int c = 0; c < 3 && e == cudaSuccess; ++c) {
-      e = cudaMemsetAsync(B.d_counter.p, 0, 4, st);
-      if (e == cudaSuccess) e = cudaEventRecord(ctx->ev0, st);
-      if (e == cudaSuccess) e = launch_batch(T, cands[c], st);
-      if (e == cudaSuccess) e = cudaEventRecord(ctx->ev1, st);
-      if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev1);
-      float ms = 0.0f;
-      cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-      ctx->launches++;
-      if (ms < best) {
-        best = ms;
-        blocks = cands[c];
-      }
+  bool uploaded = false;
+  for (size_t gi = 0; gi < segs.size(); ++gi) {
+    Segment &g = segs[gi];
+    const int occ = batch_blocks_per_sm(g.klass, g.pd);
+    const uint64_t n = g.end - g.begin;
+    g.blocks = (unsigned int)std::min<uint64_t>(n, (uint64_t)occ * ctx->sm_count);
+    const uint64_t tkey = mix(signature, 2 * g.klass + (g.pd ? 1 : 0));
+    auto tuned = B.tuned_blocks.find(tkey);
+    if (tuned != B.tuned_blocks.end()) {
+      g.blocks = tuned->second;
+      continue;
     }
-    if (e != cudaSuccess) return cuda_status(e, "batch autotune");
-    B.tuned_blocks[signature] = blocks;
+    if (n > (uint64_t)8 * occ * ctx->sm_count) {
+      if (!uploaded) {
+        e = cudaMemcpyAsync(B.d_jobs.p, hj, n_jobs * sizeof(BatchJob), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(B.d_items.p, hi, total_items * sizeof(BatchItem), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(B.d_slots.p, hs, total_items * sizeof(unsigned int), cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) return cuda_status(e, "batch autotune upload");
+        uploaded = true;
+      }
+      const unsigned int cands[3] = {(unsigned int)(occ * ctx->sm_count),
+                                     (unsigned int)std::max(1, occ / 2) * (unsigned int)ctx->sm_count,
+                                     (unsigned int)ctx->sm_count};
+      BatchParams T = params_of(g, gi);
+      T.item_end = g.begin + std::min<uint64_t>(n, (uint64_t)4 * occ * ctx->sm_count);
+      float best = 1e30f;
+      for (int c = 0; c < 3 && e == cudaSuccess; ++c) {
+        e = cudaMemsetAsync(T.counter, 0, 4, st);
+        if (e == cudaSuccess) e = cudaEventRecord(ctx->ev0, st);
+        if (e == cudaSuccess) e = launch_batch(T, g.klass, g.pd, cands[c], st);
+        if (e == cudaSuccess) e = cudaEventRecord(ctx->ev1, st);
+        if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev1);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+        ctx->launches++;
+        if (ms < best) {
+          best = ms;
+          g.blocks = cands[c];
+        }
+      }
+      if (e != cudaSuccess) return cuda_status(e, "batch autotune");
+    }
+    B.tuned_blocks[tkey] = g.blocks;
   }
 
-  // ---- the batch itself, through a CUDA graph per shape
-  uint64_t key = mix(mix(signature, total_items), blocks);
+  // ---- the batch itself, through a CUDA graph per shape: the class kernels run
+  // concurrently on side streams between the uploads and the finalize
+  uint64_t key = mix(signature, total_items);
+  for (const Segment &g : segs) key = mix(mix(key, g.end), g.blocks);
   for (const void *ptr : {B.h_jobs.p, B.h_items.p, B.h_slots.p, B.h_out.p, B.d_jobs.p, B.d_items.p, B.d_slots.p,
                           B.d_partials.p, B.d_out.p, B.d_counter.p})
     key = mix(key, (uint64_t)(uintptr_t)ptr);
   if (!B.graph || B.graph_key != key) {
     if (B.graph) cudaGraphExecDestroy(B.graph);
     B.graph = nullptr;
-    cudaGraph_t g = nullptr;
+    cudaGraph_t gr = nullptr;
     e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) e = cudaMemcpyAsync(B.d_jobs.p, B.h_jobs.p, n_jobs * sizeof(BatchJob), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(B.d_items.p, B.h_items.p, total_items * sizeof(BatchItem), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(B.d_slots.p, B.h_slots.p, total_items * sizeof(unsigned int), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(B.d_counter.p, 0, 4, st);
-    if (e == cudaSuccess) e = launch_batch(P, blocks, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.d_counter.p, 0, segs.size() * 4, st);
+    if (e == cudaSuccess) e = cudaEventRecord(B.fork, st);
+    const int ns = (int)std::min<size_t>(segs.size(), (size_t)BatchState::kSide);
+    for (int i = 0; i < ns && e == cudaSuccess; ++i) e = cudaStreamWaitEvent(B.side[i], B.fork, 0);
+    for (size_t gi = 0; gi < segs.size() && e == cudaSuccess; ++gi)
+      e = launch_batch(params_of(segs[gi], gi), segs[gi].klass, segs[gi].pd, segs[gi].blocks,
+                       B.side[gi % BatchState::kSide]);
+    for (int i = 0; i < ns && e == cudaSuccess; ++i) {
+      e = cudaEventRecord(B.join[i], B.side[i]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(st, B.join[i], 0);
+    }
     if (e == cudaSuccess)
       e = launch_batch_finalize((const BatchJob *)B.d_jobs.p, (unsigned int)n_jobs, (const double *)B.d_partials.p,
                                 (double *)B.d_out.p, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(B.h_out.p, B.d_out.p, n_jobs * 2 * kQ * sizeof(double), cudaMemcpyDeviceToHost, st);
-    cudaError_t e2 = cudaStreamEndCapture(st, &g);
+    cudaError_t e2 = cudaStreamEndCapture(st, &gr);
     if (e == cudaSuccess) e = e2;
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&B.graph, g, 0);
-    if (g) cudaGraphDestroy(g);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&B.graph, gr, 0);
+    if (gr) cudaGraphDestroy(gr);
     if (e != cudaSuccess) {
       B.graph = nullptr;
       return cuda_status(e, "batch graph capture");
@@ -275,7 +342,7 @@ extern "C" myql_status myql_mc_price_batch(myql_ctx *ctx_, const myql_mc_job *jo
   if (e == cudaSuccess) e = cudaEventRecord(ctx->ev1, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_status(e, "batch run");
-  ctx->launches += 2;
+  ctx->launches += (uint32_t)segs.size() + 1;
   const double *ho = (const double *)B.h_out.p;
   for (size_t j = 0; j < n_jobs; ++j) {
     // [quantity][value, se] -> the myql_mc_price layout [2q + (0|1)][strike]

@@ -36,11 +36,13 @@ struct BatchItem {
   unsigned int stream0;  // first stream of the item
 };
 
+// One segment of the item list: the items of one kernel class, cost-sorted;
+// its persistent blocks pull items [item_begin, item_end) through `counter`.
 struct BatchParams {
   const BatchJob *jobs;
-  const BatchItem *items;  // cost-sorted
-  const unsigned int *item_slot;  // partial slot of each sorted item (= its index within the job order)
-  unsigned long long n_items;
+  const BatchItem *items;
+  const unsigned int *item_slot;  // partial slot of each item (= its index within the job order)
+  unsigned long long item_begin, item_end;
   unsigned int *counter;
   double *partials;        // [slot][kBatchQ][2]
 };
@@ -121,9 +123,58 @@ inline int batch_class(int nf, int s1, int s2) {
   return 4 + (s1 - 1) * 3 + (s2 - 1);
 }
 
-cudaError_t launch_batch(const BatchParams &B, unsigned int blocks, cudaStream_t st);
+// Persistent kernel of one class (klass, path dependence) over one segment; each
+// class is its own instantiation with its own register allocation.
+cudaError_t launch_batch(const BatchParams &B, int klass, bool pd, unsigned int blocks, cudaStream_t st);
 cudaError_t launch_batch_finalize(const BatchJob *jobs, unsigned int n_jobs, const double *partials,
                                   double *outs, cudaStream_t st);
-int batch_blocks_per_sm();
+int batch_blocks_per_sm(int klass, bool pd);
+
+namespace dev {
+
+// Persistent: every block loops pulling items of its segment until it is empty.
+template <int NF, int S1, int S2, bool PD>
+__global__ void __launch_bounds__(kSimBlock) batch_kernel(const BatchParams B) {
+  __shared__ unsigned int item_sh;
+  __shared__ double red[kSimBlock / 32][kBatchQ][2];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  unsigned int caphits = 0, fallbacks = 0;
+  unsigned int *status = nullptr;
+  const unsigned long long n = B.item_end - B.item_begin;
+  for (;;) {
+    if (threadIdx.x == 0) item_sh = atomicAdd(B.counter, 1u);
+    __syncthreads();
+    const unsigned long long k = item_sh;
+    __syncthreads();
+    if (k >= n) break;
+    const unsigned long long it = B.item_begin + k;
+    const BatchItem I = B.items[it];
+    const BatchJob &J = B.jobs[I.job];
+    status = J.sim.status;
+    double acc[kBatchQ][2] = {{0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}};
+    batch_item<NF, S1, S2, PD>(J, I.stream0, acc, caphits, fallbacks);
+#pragma unroll
+    for (int q = 0; q < kBatchQ; ++q)
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        double v = acc[q][c];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red[warp][q][c] = v;
+      }
+    __syncthreads();
+    if (threadIdx.x < kBatchQ * 2) {
+      const int q = threadIdx.x >> 1, c = threadIdx.x & 1;
+      double t = 0.0;
+      for (int w = 0; w < kSimBlock / 32; ++w) t += red[w][q][c];
+      B.partials[((size_t)B.item_slot[it] * kBatchQ + q) * 2 + c] = t;
+    }
+  }
+  if (status && (caphits || fallbacks)) {
+    if (caphits) atomicAdd(status, caphits);
+    if (fallbacks) atomicAdd(status + 1, fallbacks);
+  }
+}
+
+}  // namespace dev
 
 }  // namespace myql

@@ -534,6 +534,18 @@ def run_ncu_cv_case() -> None:
     eng.cv_price(cv_jobs(m, "asian", 1 << 18)[0], cfg)
 
 
+def run_ncu_batch_case() -> None:
+    """A small batched case for ncu: the first 256 uneven requests at up to 2^16 paths, priced twice."""
+    import myquantlib_gb300 as m
+    from myquantlib_gb300 import workloads
+    eng = m.Engine(0)
+    rq = workloads.uneven_requests(256, max_log2_paths=16.0)
+    jobs = [m.make_job(r.model, m.stepper_for(r.model, r.instrument, r.scheme), r.instrument, r.mode, r.cfg,
+                       r.S0, r.r, r.q) for r in rq]
+    for _ in range(2):
+        eng.price_batch(jobs)
+
+
 def run_ncu_case(full: bool = False) -> None:
     """One maturity (T = 1) of the workload, priced twice, for an ncu capture: 2^18 paths (a few
     hundred MB on the device), or the full 2^22 paths for one-pass metrics."""
@@ -564,6 +576,8 @@ def main():
     if args.ncu_case or args.ncu_full:
         if args.workload == "cv":
             run_ncu_cv_case()
+        elif args.workload == "batch":
+            run_ncu_batch_case()
         else:
             run_ncu_case(full=args.ncu_full)
         return

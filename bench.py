@@ -138,7 +138,7 @@ def read_traffic() -> float | None:
     p = ROOT / "profiles" / "simulate_kernel_bates_nci_traffic.md"
     if p.exists():
         for line in p.read_text().splitlines():
-            if line.startswith("dram_bytes_per_launch:"):
+            if line.startswith("dram_bytes_per_launch:"):  # the T = 1 request (2^22 paths)
                 return float(line.split(":", 1)[1])
     return None
 

@@ -395,6 +395,16 @@ myql_status myql_mlmc_cv_price(myql_ctx *ctx, const myql_mc_job *job, const myql
 myql_status myql_mlmc_cv_level(myql_ctx *ctx, const myql_mc_job *job, const myql_mlmc_config *mlmc,
                                uint32_t level, uint64_t dN, double *sums4);
 
+/* FP64 Gil-Pelaez prices of a European instrument (every model; vanilla,
+ * cash- and asset-or-nothing payoffs), the oracle of the Monte Carlo prices:
+ * FourierPricer (pricers/fourier/FourierPricer.hpp) with the characteristic
+ * exponents of CFPolicies.hpp and AffineTraits.hpp, integrated by 256-panel
+ * Gauss-Legendre quadrature on the GPU.  greek_mode Essential adds delta and
+ * gamma, Full every Greek, as FP64 central differences of these prices.
+ * out: MYQL_OUT_DOUBLES(n_strikes) doubles in the myql_mc_price layout
+ * (standard errors 0).  The job's schemes and Monte Carlo settings are ignored. */
+myql_status myql_fourier_price(myql_ctx *ctx, const myql_mc_job *job, int32_t greek_mode, double *out);
+
 /* One-tile tcgen05 GEMM D[128][N] = A[128][K] * B[N][K]^T with the operands
  * rounded to BF16 and FP32 accumulation, through the shared-memory operand
  * layouts and descriptors the control-variate MLP kernels use: mode 0 K = 16,

@@ -148,6 +148,7 @@ _SIGS = {
                                      C.POINTER(MlmcResultC), C.POINTER(C.c_double)]),
     "myql_mlmc_cv_level": (C.c_int, [C.c_void_p, C.POINTER(McJobC), C.POINTER(MlmcConfigC), C.c_uint32,
                                      C.c_uint64, C.POINTER(C.c_double)]),
+    "myql_fourier_price": (C.c_int, [C.c_void_p, C.POINTER(McJobC), C.c_int32, C.POINTER(C.c_double)]),
     "myql_probe_mma": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                  C.POINTER(C.c_float)]),
 }

@@ -509,6 +509,12 @@ class Engine:
                                                _ptr(out)))
         return out
 
+    def fourier(self, job: "_Job", mode: "GreekMode | int" = 0) -> np.ndarray:
+        """FP64 Gil-Pelaez oracle of a European job -> (2Q, n) rows (standard errors 0)."""
+        out = np.zeros(2 * _abi.Q_COUNT * job.n_strikes, dtype=np.float64)
+        _abi.check(self.lib.myql_fourier_price(self.handle, C.byref(job.c), int(mode), _ptr(out)))
+        return out.reshape(2 * _abi.Q_COUNT, job.n_strikes)
+
     def paths(self, job: "_Job") -> np.ndarray:
         nsc, nf = C.c_uint32(), C.c_uint32()
         _abi.check(self.lib.myql_mc_paths(self.handle, C.byref(job.c), None, 0, C.byref(nsc),

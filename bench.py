@@ -316,6 +316,23 @@ def run_engine(args) -> dict:
             "e2e": {"value": e2e, "unit": "paths*steps/s", "h2d_bytes_per_step": 8 * nk * len(jobs),
                     "d2h_bytes_per_step": 8 * 2 * 10 * nk * len(jobs)},
             "gpu_launches": launches_per_step * args.steps, "roofline": roof, "clocks": clk.summary()}
+    # every price and Greek of the strip against the FP64 Gil-Pelaez oracle (z = error / SE)
+    try:
+        zmax = {}
+        for j in jobs:
+            raw, _ = eng.price(j)
+            four = eng.fourier(j, m.GreekMode.FULL)
+            for qi, name in enumerate(m._abi.Q_NAMES):
+                se = raw[2 * qi + 1]
+                ok = se > 0
+                if not ok.any():
+                    continue
+                z = np.abs(raw[2 * qi][ok] - four[2 * qi][ok]) / se[ok]
+                zmax[name] = max(zmax.get(name, 0.0), float(z.max()))
+        line["fourier_check"] = {"max_abs_z": zmax, "options": len(jobs) * nk,
+                                 "oracle": "FP64 Gil-Pelaez on the GPU (myql_fourier_price)"}
+    except Exception as exc:  # the oracle is a report, not the measurement
+        line["fourier_check"] = {"error": str(exc)}
     if world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_reference(args)
     return line

@@ -15,7 +15,7 @@ FOURIER = json.loads((Path(__file__).resolve().parent / "golden" / "reference_fo
 
 @pytest.mark.parametrize("spec", FOURIER, ids=[s["name"] for s in FOURIER])
 def test_fourier_matches_reference(engine, spec):
-    j = jobspec.make_job(dict(spec, mode="full"))
+    j = jobspec.make_job(dict(spec, mode="full", schemes=["Exact", "Exact"]))  # schemes are ignored
     got = engine.fourier(j, m.GreekMode.FULL)
     want = spec["fourier"]
     for q in range(10):

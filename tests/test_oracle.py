@@ -14,6 +14,7 @@ import pyrng
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 MC_SPECS = json.loads((GOLDEN / "reference_mc.json").read_text())
+FOURIER_SPECS = json.loads((GOLDEN / "reference_fourier.json").read_text())
 
 
 @pytest.mark.parametrize("spec", MC_SPECS, ids=[s["name"] for s in MC_SPECS])
@@ -112,3 +113,23 @@ def test_reference_seed_layout_first_draws():
     s = pyrng.seed_state(42 + 999983)
     o, _ = pyrng.next_out(s)
     assert o == golden["seed42_thread1_first"]
+
+
+def test_reference_put_theta_is_not_its_price_derivative(oracle_lib):
+    """The reference's FourierPricer reports a put theta that is not the T-derivative of
+    its own put price (the call side is consistent).  Recorded because the GPU engine's
+    Monte Carlo theta and its Fourier oracle follow the derivative."""
+    if not oracle_lib.reference_available():
+        pytest.skip("reference library not built here")
+    spec = [s for s in FOURIER_SPECS if s["name"] == "heston_put_k95_t05"][0]
+
+    def ref(T):
+        s = json.loads(json.dumps(spec))
+        s["instrument"]["T"] = T
+        return np.asarray(oracle_lib.ref_fourier(jobspec.make_job(dict(s, mode="full", schemes=["Exact"]))))
+
+    h = 1e-5
+    base = ref(0.5)
+    dPdT = (ref(0.5 + h)[0] - ref(0.5 - h)[0]) / (2 * h)
+    assert base[5] == pytest.approx(5.316764368677, rel=1e-9)   # the reported theta
+    assert dPdT == pytest.approx(4.154394, rel=1e-6)             # the derivative of its price

@@ -297,7 +297,7 @@ def run_engine(args) -> dict:
     xu_ach = XU_PER_STEP * sim / (sim_ms / 1e3)
     alu_frac, xu_frac = alu_ach / alu_peak, xu_ach / xu_peak
     bound = "alu" if alu_frac >= xu_frac else "xu"
-    roof = {"bound": bound, "kernel": "simulate_kernel<1,NCI,-,European>",
+    roof = {"bound": bound, "kernel": "simulate_lockstep_kernel<1,NCI,-,5 scenarios>",
             "achieved": (alu_ach if bound == "alu" else xu_ach) / 1e9,
             "peak": (alu_peak if bound == "alu" else xu_peak) / 1e9, "unit": "Gop/s",
             "frac": max(alu_frac, xu_frac),

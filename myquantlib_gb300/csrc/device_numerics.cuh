@@ -158,12 +158,13 @@ __device__ __forceinline__ float log1p_m(float w) {
 // checked with Temme's uniform expansion when it lies within 2*Delta of an
 // integer; below 10 an explicit summation.  FP32 throughout; the summation
 // runs in plain (unscaled) form, which is exact up to FP32 rounding of the CDF.
-static __device__ __noinline__ int poisson_inv(float lam, unsigned long long x, unsigned int cap,
-                                        unsigned int &caphits) {
-  const float U = u01_bits(x);
+// U = u01_bits(x) and, where lam > 4, W = inv_normal_bits(x) depend on the draw
+// alone: callers that invert one draw for several means compute them once.
+static __device__ __noinline__ int poisson_core(float lam, float U, float W,
+                                                unsigned long long x, unsigned int cap,
+                                                unsigned int &caphits) {
   float X = 0.0f;
   if (lam > 4.0f) {
-    const float W = inv_normal_bits(x);
     const float rl = sqrt_approx(lam);
     const float li = 1.0f / lam;
     float S, Del;
@@ -286,6 +287,12 @@ static __device__ __noinline__ int poisson_inv(float lam, unsigned long long x, 
     X = (float)n;
   }
   return (int)X;
+}
+
+__device__ __forceinline__ int poisson_inv(float lam, unsigned long long x, unsigned int cap,
+                                           unsigned int &caphits) {
+  const float W = lam > 4.0f ? inv_normal_bits(x) : 0.0f;
+  return poisson_core(lam, u01_bits(x), W, x, cap, caphits);
 }
 
 // Poisson draw by sequential inversion, as boost::random::poisson_distribution

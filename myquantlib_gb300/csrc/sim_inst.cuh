@@ -6,6 +6,14 @@ namespace myql {
 template <int NF, int S1, int S2>
 cudaError_t launch_sim_t(const SimParams &P, bool path_dep, cudaStream_t stream) {
   const unsigned int grid = (P.n_streams + kSimBlock - 1) / kSimBlock;
+  if constexpr (NF >= 1 && S1 != dev::SCH_EXACT && S2 != dev::SCH_EXACT) {
+    // Full Greeks of a European: every simulated scenario in lockstep
+    constexpr int n_sc_full = NF == 2 ? 9 : 7;
+    if (!path_dep && P.n_sc == n_sc_full) {
+      dev::simulate_lockstep_kernel<NF, S1, S2, n_sc_full - 2><<<grid, kSimBlock, 0, stream>>>(P);
+      return cudaGetLastError();
+    }
+  }
   if (path_dep)
     dev::simulate_kernel<NF, S1, S2, true><<<grid, kSimBlock, 0, stream>>>(P);
   else

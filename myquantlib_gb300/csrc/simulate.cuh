@@ -21,28 +21,40 @@ namespace dev {
 
 enum { SCH_NONE = 0, SCH_NV = 1, SCH_EXACT = 2, SCH_NCI = 3 };
 
-// Chi-squared quantile of the SchemeNCI table (VolSchemes.hpp:334-370): cubic
-// Hermite cell of row N on the U grid, or the tail grid for U >= 0.999.
-__device__ __forceinline__ float nci_quantile(const NciTable &tab, int N,
-                                              unsigned long long x2,
-                                              unsigned long long u999,
-                                              unsigned int &fallbacks) {
-  if (N < tab.rows) {
-    if (x2 < u999) {
-      const unsigned long long hi = __umul64hi(x2, tab.pos_scale);  // U*inv_dx * 2^50
-      int i = (int)(hi >> 50);
-      i = min(i, kNciGrid - 2);
-      const float t = (float)((unsigned int)(hi >> 26) & 0xFFFFFFu) * 5.9604644775390625e-8f;
-      const float4 c = __ldg(tab.main + (size_t)N * (kNciGrid - 1) + i);
-      return fmaf(fmaf(fmaf(c.w, t, c.z), t, c.y), t, c.x);
-    }
+// Cell of a draw x2 on the SchemeNCI table's U grid (VolSchemes.hpp:334-370):
+// the cubic Hermite cell and its fraction on the main grid, or on the tail grid
+// for U >= 0.999.  It depends on the draw alone, not on the table row.
+struct NciPos {
+  int i;
+  float t;
+  bool tail;
+};
+
+__device__ __forceinline__ NciPos nci_pos(const NciTable &tab, unsigned long long x2,
+                                          unsigned long long u999) {
+  NciPos p;
+  p.tail = x2 >= u999;
+  if (!p.tail) {
+    const unsigned long long hi = __umul64hi(x2, tab.pos_scale);  // U*inv_dx * 2^50
+    p.i = min((int)(hi >> 50), kNciGrid - 2);
+    p.t = (float)((unsigned int)(hi >> 26) & 0xFFFFFFu) * 5.9604644775390625e-8f;
+  } else {
     const float w = -__logf(u01c_bits(x2));
     float pos = (w - tab.tail_w0) * tab.tail_inv_dw;
     pos = fminf(fmaxf(pos, 0.0f), (float)(kNciTail - 1) - 1e-3f);
-    const int i = (int)pos;
-    const float t = pos - (float)i;
-    const float4 c = __ldg(tab.tail + (size_t)N * (kNciTail - 1) + i);
-    return fmaf(fmaf(fmaf(c.w, t, c.z), t, c.y), t, c.x);
+    p.i = (int)pos;
+    p.t = pos - (float)p.i;
+  }
+  return p;
+}
+
+// Chi-squared quantile of row N (d + 2N degrees of freedom) at the cell p of x2.
+__device__ __forceinline__ float nci_row(const NciTable &tab, int N, const NciPos &p,
+                                         unsigned long long x2, unsigned int &fallbacks) {
+  if (N < tab.rows) {
+    const float4 c = p.tail ? __ldg(tab.tail + (size_t)N * (kNciTail - 1) + p.i)
+                            : __ldg(tab.main + (size_t)N * (kNciGrid - 1) + p.i);
+    return fmaf(fmaf(fmaf(c.w, p.t, c.z), p.t, c.y), p.t, c.x);
   }
   // Beyond the table (dof >= d + 2*rows): Wilson-Hilferty cube.
   ++fallbacks;
@@ -51,6 +63,13 @@ __device__ __forceinline__ float nci_quantile(const NciTable &tab, int N,
   const float h = 2.0f / (9.0f * nu);
   const float b = 1.0f - h + z * sqrtf(h);
   return fmaxf(nu * b * b * b, 0.0f);
+}
+
+__device__ __forceinline__ float nci_quantile(const NciTable &tab, int N,
+                                              unsigned long long x2,
+                                              unsigned long long u999,
+                                              unsigned int &fallbacks) {
+  return nci_row(tab, N, nci_pos(tab, x2, u999), x2, fallbacks);
 }
 
 // One step of the CIR variance under scheme SCH (VolSchemes.hpp evolve()).
@@ -270,6 +289,140 @@ __global__ void __launch_bounds__(kSimBlock) simulate_kernel(const __grid_consta
       }
       if (sc == 0) rng = r;
     }
+  }
+  P.states[s] = rng.a;
+  P.states[(size_t)S + s] = rng.b;
+  P.states[2 * (size_t)S + s] = rng.c;
+  P.states[3 * (size_t)S + s] = rng.d;
+  if (caphits) atomicAdd(P.status, caphits);
+  if (fallbacks) atomicAdd(P.status + 1, fallbacks);
+}
+
+// ---------------------------------------------------------------------------
+// Scenario lockstep (GreekMode::Full, European instruments, NV / NCI factors).
+//
+// Under these schemes a step consumes the same draws in every scenario (one for
+// the spot Gaussian, one per NV factor, two per NCI factor) and the jump of a
+// European path is drawn once after the last step, so the replays of a path
+// read the same random numbers step by step.  One thread then advances all
+// simulated scenarios of its path together: the draws, the spot Gaussian, the
+// Poisson draw's U and W and the chi-squared table cell are computed once per
+// step, and only the parts that depend on a scenario's variance and constants
+// run per scenario.  Every scenario's arithmetic is the per-scenario kernel's,
+// so its record is bit-identical.
+
+// Simulated scenarios of a European Full request in lockstep order: base,
+// v0 (or factor-0 v0) up / down, T up / down, then factor-1 v0 up / down.
+__host__ __device__ constexpr int lockstep_sc(int j) { return j < 5 ? j : j + 2; }
+
+// The per-step draws of one factor, shared by every scenario.
+template <int SCH>
+struct FactorDraws {
+  float Z = 0.0f;                 // NV: Gaussian of the variance step
+  unsigned long long xp = 0, x2 = 0;  // NCI: Poisson and chi-squared draws
+  float U = 0.0f, W = 0.0f;       // NCI: uniform and Gaussian of xp
+  NciPos pos{};                   // NCI: table cell of x2
+};
+
+template <int SCH>
+__device__ __forceinline__ void factor_draws(FactorDraws<SCH> &d, Xo &rng, const SimParams &P,
+                                             int fi) {
+  if (SCH == SCH_NV) {
+    d.Z = inv_normal_bits(draw(rng));
+  } else if (SCH == SCH_NCI) {
+    d.xp = draw(rng);
+    d.U = u01_bits(d.xp);
+    d.W = inv_normal_bits(d.xp);
+    d.x2 = draw(rng);
+    d.pos = nci_pos(P.nci[fi], d.x2, P.nci_u999);
+  }
+}
+
+// evolve<SCH> (above) with the step's draws given.
+template <int SCH>
+__device__ __forceinline__ float evolve_drawn(float v, const FactorDraws<SCH> &d,
+                                              const FactorConst &f, const SimParams &P, int fi,
+                                              unsigned int &caphits, unsigned int &fallbacks) {
+  if (SCH == SCH_NV) {
+    const float root = sqrt_approx(fmaf(f.w0, v, f.w1)) + f.w2 * d.Z;
+    return fmaf(f.w0 * root, root, f.w1);
+  } else {
+    const float lam = f.w0 * v;
+    const int N = poisson_core(lam, d.U, lam > 4.0f ? d.W : 0.0f, d.xp, P.loop_cap, caphits);
+    return nci_row(P.nci[fi], N, d.pos, d.x2, fallbacks) * f.w2;
+  }
+}
+
+template <int NF, int S1, int S2, int NSIM>
+__global__ void __launch_bounds__(kSimBlock) simulate_lockstep_kernel(
+    const __grid_constant__ SimParams P) {
+  static_assert(NF >= 1 && S1 != SCH_EXACT && S2 != SCH_EXACT, "lockstep needs NV/NCI factors");
+  const unsigned int s = blockIdx.x * kSimBlock + threadIdx.x;
+  const unsigned int S = P.n_streams;
+  if (s >= S) return;
+  Xo rng;
+  rng.a = P.states[s];
+  rng.b = P.states[(size_t)S + s];
+  rng.c = P.states[2 * (size_t)S + s];
+  rng.d = P.states[3 * (size_t)S + s];
+  unsigned int caphits = 0, fallbacks = 0;
+  const int n = P.n_steps;
+  for (unsigned long long i = P.path_begin + s; i < P.path_end; i += S) {
+    const size_t col = (size_t)(i - P.rec_offset);
+    float X[NSIM], va[NSIM], vb[NSIM];
+#pragma unroll
+    for (int j = 0; j < NSIM; ++j) {
+      X[j] = 0.0f;
+      va[j] = P.sc[lockstep_sc(j)].f[0].v0;
+      vb[j] = P.sc[lockstep_sc(j)].f[1].v0;
+    }
+    for (int k = 0; k < n; ++k) {
+      const float G = inv_normal_bits(draw(rng));
+      FactorDraws<S1> da;
+      FactorDraws<S2> db;
+      factor_draws<S1>(da, rng, P, 0);
+      if (NF == 2) factor_draws<S2>(db, rng, P, 1);
+#pragma unroll
+      for (int j = 0; j < NSIM; ++j) {
+        const ScenarioConst &C = P.sc[lockstep_sc(j)];
+        if (NF == 1) {
+          const FactorConst &f = C.f[0];
+          const float vn = evolve_drawn<S1>(va[j], da, f, P, 0, caphits, fallbacks);
+          const float root = sqrt_approx(f.C3 * (va[j] + vn));
+          const float drift = fmaf(f.C2, vn, fmaf(f.C1, va[j], f.C0));
+          X[j] += fmaf(root, G, drift);
+          va[j] = vn;
+        } else {
+          const FactorConst &f0 = C.f[0];
+          const FactorConst &f1 = C.f[1];
+          const float van = evolve_drawn<S1>(va[j], da, f0, P, 0, caphits, fallbacks);
+          const float vbn = evolve_drawn<S2>(vb[j], db, f1, P, 1, caphits, fallbacks);
+          const float root = sqrt_approx(fmaf(f0.C3, va[j] + van, f1.C3 * (vb[j] + vbn)));
+          const float drift = fmaf(f1.C2, vbn, fmaf(f1.C1, vb[j], fmaf(f0.C2, van,
+                                   fmaf(f0.C1, va[j], f0.C0 + f1.C0))));
+          X[j] += fmaf(root, G, drift);
+          va[j] = van;
+          vb[j] = vbn;
+        }
+      }
+    }
+    // One jump over each scenario's (bumped) maturity, drawn from the state after
+    // the last step; the base scenario's draws advance the stream.
+    if (P.jump_kind) {
+      Xo after = rng;
+#pragma unroll
+      for (int j = 0; j < NSIM; ++j) {
+        Xo r = after;
+        X[j] += jump_draw(P, P.sc[lockstep_sc(j)], r, caphits);
+        if (j == 0) rng = r;
+      }
+    }
+    const size_t F = (size_t)P.n_fields;
+#pragma unroll
+    for (int j = 0; j < NSIM; ++j)
+      P.records[(size_t)lockstep_sc(j) * F * P.rec_stride + col] = X[j];
+    P.records[(size_t)SC_RUP * F * P.rec_stride + col] = X[0] + P.sc[SC_RUP].x_shift;
+    P.records[(size_t)SC_RDN * F * P.rec_stride + col] = X[0] + P.sc[SC_RDN].x_shift;
   }
   P.states[s] = rng.a;
   P.states[(size_t)S + s] = rng.b;

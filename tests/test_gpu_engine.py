@@ -2,6 +2,7 @@
 bit-exact jump-ahead streams, the device samplers against the oracle, the FP64
 chi-squared tables against scipy, size edge cases, determinism, chunking and
 host-side fault injection (loop caps), which faults no GPU."""
+import dataclasses
 import json
 from pathlib import Path
 
@@ -169,3 +170,59 @@ def test_arith_asian_one_step_equals_half_european(engine):
         100.0, 0.02, 0.0, m.EuropeanOption(100.0, 1.0))
     # same path: avg = (S0 + S_T)/2, payoff = max(S_T - (2K - S0), 0)/2 = max(S_T - K,0)/2 at K=S0
     assert abs(a.price - 0.5 * e.price) < 1e-4 * e.price
+
+
+_H_NCI = m.HestonParams(2.0, 0.05, 0.9, -0.6, 0.05)   # sigma^2 > 4 kappa theta: NCI only
+_H_NV = m.HestonParams(1.5, 0.04, 0.3, -0.7, 0.04)
+_H_NV2 = m.HestonParams(0.5, 0.04, 0.2, -0.3, 0.03)
+_MJ = m.MertonParams(0.5, -0.1, 0.15)
+_KJ = m.KouParams(0.8, 0.4, 10.0, 5.0)
+LOCKSTEP = {
+    "bates_nci": (m.BatesModel(_H_NCI, _MJ), m.BatesStepper(m.SchemeNCI)),
+    "heston_nv": (m.HestonModel(_H_NV), m.HestonStepper(m.SchemeNV)),
+    "bateskou_nci": (m.BatesKouModel(_H_NV, _KJ), m.BatesKouStepper(m.SchemeNCI)),
+    "dbates_nci_nv": (m.DoubleBatesModel(_H_NCI, _H_NV2, _MJ), m.DoubleBatesStepper(m.SchemeNCI, m.SchemeNV)),
+    "dheston_nv_nci": (m.DoubleHestonModel(_H_NV, _H_NCI), m.DoubleHestonStepper(m.SchemeNV, m.SchemeNCI)),
+}
+
+
+@pytest.mark.parametrize("name", list(LOCKSTEP))
+def test_full_greek_scenarios_equal_single_scenario_runs(engine, name):
+    """Full Greeks of a European advance every bumped scenario of a path in lockstep
+    on shared draws.  Each scenario's records must be bit-identical to a request
+    that prices that bumped scenario alone (MonteCarloPricer.hpp:302-410 replays
+    the path from rng_start for each bump)."""
+    model, stepper = LOCKSTEP[name]
+    # one path per stream: a stream continues from the base scenario's end state, and a
+    # bumped scenario priced alone continues from its own, which differs once its jump
+    # count (and so its draw count) differs from the base's
+    cfg = m.MonteCarloConfig(num_paths=6000, time_steps=40, seed=7, n_streams=6000)
+    T, S0, r, q = 0.75, 100.0, 0.02, 0.01
+    full = m.make_job(model, stepper, m.EuropeanOption([90.0, 100.0, 110.0], T), m.GreekMode.FULL,
+                      cfg, S0, r, q)
+    g = engine.paths(full)
+    nf = model.num_variance_factors
+    assert g.shape[0] == (9 if nf == 2 else 7)
+
+    def single(mod, t):
+        j = m.make_job(mod, stepper, m.EuropeanOption([100.0], t), m.GreekMode.NONE, cfg, S0, r, q)
+        return engine.paths(j)[0]
+
+    def bump_v0(f, s):
+        if nf == 1:
+            return dataclasses.replace(model, heston=dataclasses.replace(model.heston, v0=model.heston.v0 + s * cfg.vol_bump))
+        key = "heston1" if f == 0 else "heston2"
+        h = getattr(model, key)
+        return dataclasses.replace(model, **{key: dataclasses.replace(h, v0=h.v0 + s * cfg.vol_bump)})
+
+    np.testing.assert_array_equal(g[0], single(model, T))
+    np.testing.assert_array_equal(g[1], single(bump_v0(0, +1), T))
+    np.testing.assert_array_equal(g[2], single(bump_v0(0, -1), T))
+    np.testing.assert_array_equal(g[3], single(model, T + cfg.t_bump))
+    np.testing.assert_array_equal(g[4], single(model, T - cfg.t_bump))
+    if nf == 2:
+        np.testing.assert_array_equal(g[7], single(bump_v0(1, +1), T))
+        np.testing.assert_array_equal(g[8], single(bump_v0(1, -1), T))
+    # rate bumps: the base path shifted by (r' - r) T
+    np.testing.assert_allclose(g[5], g[0] + np.float32(cfg.r_bump * T), rtol=0, atol=2e-6)
+    np.testing.assert_allclose(g[6], g[0] - np.float32(cfg.r_bump * T), rtol=0, atol=2e-6)

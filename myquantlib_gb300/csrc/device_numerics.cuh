@@ -160,133 +160,258 @@ __device__ __forceinline__ float log1p_m(float w) {
 // runs in plain (unscaled) form, which is exact up to FP32 rounding of the CDF.
 // U = u01_bits(x) and, where lam > 4, W = inv_normal_bits(x) depend on the draw
 // alone: callers that invert one draw for several means compute them once.
+// The common regimes (central estimate, summation) are inline; the tail solve
+// and the near-integer check, taken by a few lanes in a thousand, are out of
+// line so that the inlined path stays small.
+
+// Normal-asymptotic estimate S and its error window Del, lambda > 4, |W| < 3.
+__device__ __forceinline__ void poisson_central(float lam, float W, float &S, float &Del) {
+  const float rl = sqrt_approx(lam);
+  const float li = rcp_approx(lam);
+  const float S1 = rl * W + (1.0f / 3.0f + (1.0f / 6.0f) * W * W) *
+                                (1.0f - W * (1.0f / 12.0f) * rcp_approx(rl));
+  Del = fmaf(fmaf(1.0f / 160.0f, W * W, 1.0f / 80.0f), W * W, 1.0f / 40.0f) * li;
+  S = __fadd_rn(lam, S1 + Del);  // never contracted with the caller's product
+}
+
+// Tail estimate (|W| >= 3): Newton on sqrt(2((1-R) + R log R)) = W / sqrt(lambda);
+// quadratic convergence reaches FP32 resolution in a few steps, so a fixed
+// small budget replaces the FP64 tolerance loop.  Returns (S, Del).
+static __device__ __noinline__ float2 poisson_newton(float lam, float W) {
+  const float s = W / sqrt_approx(lam);
+  float R = fmaxf(1.0f + s, 0.1f), R2;
+  for (int it = 0; it < 12; ++it) {
+    R2 = R;
+    const float T = log1pf(R - 1.0f);
+    float S2 = sqrtf(2.0f * xlogx_m1(R - 1.0f));
+    if (R < 1.0f) S2 = -S2;
+    R = R2 - (S2 - s) * S2 / T;
+    if (R < 0.1f * R2) R = 0.1f * R2;
+    if (fabsf(R - R2) <= 2e-7f * R) break;
+  }
+  const float T = log1pf(R - 1.0f);
+  float S = lam * R + __logf(sqrtf(2.0f * R * xlogx_m1(R - 1.0f)) / fabsf(R - 1.0f)) / T;
+  S = S - 0.0218f / (S + 0.065f * lam);
+  const float Del = 0.01f / S;
+  return make_float2(S + Del, Del);
+}
+
+// floor(S) = X lies within 2 Del of an integer: decide between X - 1 and X
+// from the CDF at X - 1.
+static __device__ __noinline__ float poisson_check(float lam, float X, float U,
+                                                   unsigned long long x) {
+  const float li = 1.0f / lam;
+  if (X > 0.5f * lam && X < 2.0f * lam) {
+    // Temme's uniform asymptotic expansion of the CDF at X - 1 (TOMS 955).
+    const float Xi = 1.0f / X;
+    float Eta = sqrtf(2.0f * xlogx_m1(X * li - 1.0f) / (X * li));
+    if (X > lam) Eta = -Eta;
+    float B1 = 8.0995211567045583e-16f, B0;
+    float T = B1;
+    B0 = -1.9752288294349411e-15f;  T = B0 + T * Eta;
+    B1 = -5.1391118342426808e-16f + 25.0f * B1 * Xi;  T = B1 + T * Eta;
+    B0 = 2.8534893807047458e-14f + 24.0f * B0 * Xi;   T = B0 + T * Eta;
+    B1 = -1.3923887224181616e-13f + 23.0f * B1 * Xi;  T = B1 + T * Eta;
+    B0 = 3.3717632624009806e-13f + 22.0f * B0 * Xi;   T = B0 + T * Eta;
+    B1 = 1.1004392031956284e-13f + 21.0f * B1 * Xi;   T = B1 + T * Eta;
+    B0 = -5.0276692801141763e-12f + 20.0f * B0 * Xi;  T = B0 + T * Eta;
+    B1 = 2.4361948020667402e-11f + 19.0f * B1 * Xi;   T = B1 + T * Eta;
+    B0 = -5.8307721325504166e-11f + 18.0f * B0 * Xi;  T = B0 + T * Eta;
+    B1 = -2.5514193994946487e-11f + 17.0f * B1 * Xi;  T = B1 + T * Eta;
+    B0 = 9.1476995822367933e-10f + 16.0f * B0 * Xi;   T = B0 + T * Eta;
+    B1 = -4.3820360184533521e-09f + 15.0f * B1 * Xi;  T = B1 + T * Eta;
+    B0 = 1.0261809784240299e-08f + 14.0f * B0 * Xi;   T = B0 + T * Eta;
+    B1 = 6.7078535434015332e-09f + 13.0f * B1 * Xi;   T = B1 + T * Eta;
+    B0 = -1.7665952736826086e-07f + 12.0f * B0 * Xi;  T = B0 + T * Eta;
+    B1 = 8.2967113409530833e-07f + 11.0f * B1 * Xi;   T = B1 + T * Eta;
+    B0 = -1.8540622107151585e-06f + 10.0f * B0 * Xi;  T = B0 + T * Eta;
+    B1 = -2.1854485106799979e-06f + 9.0f * B1 * Xi;   T = B1 + T * Eta;
+    B0 = 3.9192631785224383e-05f + 8.0f * B0 * Xi;    T = B0 + T * Eta;
+    B1 = -0.00017875514403292177f + 7.0f * B1 * Xi;   T = B1 + T * Eta;
+    B0 = 0.00035273368606701921f + 6.0f * B0 * Xi;    T = B0 + T * Eta;
+    B1 = 0.0011574074074074078f + 5.0f * B1 * Xi;     T = B1 + T * Eta;
+    B0 = -0.014814814814814815f + 4.0f * B0 * Xi;     T = B0 + T * Eta;
+    B1 = 0.083333333333333329f + 3.0f * B1 * Xi;      T = B1 + T * Eta;
+    B0 = -0.33333333333333331f + 2.0f * B0 * Xi;      T = B0 + T * Eta;
+    T = T / (1.0f + B1 * Xi);
+    T = T * __expf(-0.5f * X * Eta * Eta) * rsqrtf(2.0f * 3.14159265358979f * X);
+    if (X < lam) {
+      T += 0.5f * erfcf(Eta * sqrtf(0.5f * X));
+      if (T > U) X -= 1.0f;
+    } else {
+      T -= 0.5f * erfcf(-Eta * sqrtf(0.5f * X));
+      if (T > -u01c_bits(x)) X -= 1.0f;
+    }
+  } else {
+    // Stirling-corrected ratio, then a 50-term summation (tails only).
+    float Xi = 1.0f / X;
+    float T = -(691.0f / 360360.0f);
+    T = (1.0f / 1188.0f) + T * Xi * Xi;
+    T = -(1.0f / 1680.0f) + T * Xi * Xi;
+    T = (1.0f / 1260.0f) + T * Xi * Xi;
+    T = -(1.0f / 360.0f) + T * Xi * Xi;
+    T = (1.0f / 12.0f) + T * Xi * Xi;
+    T = T * Xi;
+    T = (X - lam) - X * __logf(X * li) - T;
+    if (X < lam) {
+      const float E = __expf(-0.5f * T);
+      float Ssum = 1.0f - E * (U * E) * sqrtf(2.0f * 3.14159265358979f * Xi) * lam;
+      float Tt = 1.0f, Xr = X;
+      for (int i = 1; i < 50; ++i) {
+        Xr -= 1.0f;
+        Tt *= Xr * li;
+        Ssum += Tt;
+      }
+      if (Ssum > 0.0f) X -= 1.0f;
+    } else {
+      const float E = __expf(-0.5f * T);
+      float Ssum = 1.0f - E * (u01c_bits(x) * E) * sqrtf(2.0f * 3.14159265358979f * X);
+      float Xr = X;
+      for (int i = 0; i < 50; ++i) {
+        Xr += 1.0f;
+        Ssum = Ssum * Xr * li + 1.0f;
+      }
+      if (Ssum < 0.0f) X -= 1.0f;
+    }
+  }
+  return X;
+}
+
+// Explicit summation of the CDF from 0: p_n = p_{n-1} * (lam * (1/n)), F_n = F_{n-1} + p_n,
+// until U <= F_n.  A second exit, p_n < 5e-8 F_n (F has stopped moving), guards
+// the deep upper tail.  It cannot fire first when U < 1 - 1e-5: it needs the
+// remaining mass below ~3e-7 while FP32 rounding of F stays under ~3e-6, so F_n
+// already exceeds U there.  Such draws take a loop without it.
+constexpr float kPoissonUFast = 0.99999f;
+
+__device__ __forceinline__ float poisson_sum(float lam, float U, unsigned int cap,
+                                             unsigned int &caphits) {
+  float p = __expf(-lam);
+  float F = p;
+  unsigned int n = 0;
+  const bool fast = U < kPoissonUFast;
+  while (U > F) {
+    if (++n > cap) {
+      ++caphits;
+      break;
+    }
+    const float nf = (float)n;
+    p *= lam * rcp_approx(nf);
+    F += p;
+    if (!fast && p < F * 5.0e-8f) break;
+  }
+  return (float)n;
+}
+
+__device__ __forceinline__ int poisson_eval(float lam, float U, float W, unsigned long long x,
+                                            unsigned int cap, unsigned int &caphits) {
+  float X = 0.0f;
+  if (lam > 4.0f) {
+    float S, Del;
+    if (fabsf(W) < 3.0f) {
+      poisson_central(lam, W, S, Del);
+    } else {
+      const float2 sd = poisson_newton(lam, W);
+      S = sd.x;
+      Del = sd.y;
+    }
+    X = floorf(S);
+    if (S > 10.0f && S < X + 2.0f * Del) X = poisson_check(lam, X, U, x);
+  }
+  if (X < 10.0f) X = poisson_sum(lam, U, cap, caphits);
+  return (int)X;
+}
+
+// poisson_eval for NS means on one draw (the bumped scenarios of one path):
+// each N[j] equals poisson_eval(lam[j], U, W, x), where W = inv_normal_bits(x)
+// is computed only if some mean exceeds 4.  The central estimates run as
+// straight-line code and the summations share one loop, so the scenarios'
+// arithmetic interleaves and the loop overhead is paid once.
+template <int NS>
+__device__ __forceinline__ void poisson_eval_n(const float (&lam)[NS], float U,
+                                               unsigned long long x, unsigned int cap,
+                                               unsigned int &caphits, int (&N)[NS]) {
+  float X[NS];
+  bool big = false;
+#pragma unroll
+  for (int j = 0; j < NS; ++j) {
+    X[j] = 0.0f;
+    big |= lam[j] > 4.0f;
+  }
+  if (big) {
+    const float W = inv_normal_bits(x);
+    float S[NS], Del[NS];
+    if (fabsf(W) < 3.0f) {
+#pragma unroll
+      for (int j = 0; j < NS; ++j) poisson_central(lam[j], W, S[j], Del[j]);
+    } else {
+#pragma unroll
+      for (int j = 0; j < NS; ++j) {
+        S[j] = Del[j] = 0.0f;
+        if (lam[j] > 4.0f) {
+          const float2 sd = poisson_newton(lam[j], W);
+          S[j] = sd.x;
+          Del[j] = sd.y;
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+      if (lam[j] > 4.0f) {
+        X[j] = floorf(S[j]);
+        if (S[j] > 10.0f && S[j] < X[j] + 2.0f * Del[j]) X[j] = poisson_check(lam[j], X[j], U, x);
+      }
+    }
+  }
+  float p[NS], F[NS];
+  bool act[NS];
+  bool any = false;
+#pragma unroll
+  for (int j = 0; j < NS; ++j) {
+    const bool small = X[j] < 10.0f;
+    p[j] = __expf(-lam[j]);
+    F[j] = p[j];
+    act[j] = small && U > F[j];
+    if (small) X[j] = 0.0f;
+    any |= act[j];
+  }
+  // poisson_sum for every scenario in one loop.  A scenario's p and F are dead
+  // once it has exited, so the terms are computed without branches.
+  const bool fast = U < kPoissonUFast;
+  unsigned int n = 0;
+  while (any) {
+    if (++n > cap) {
+#pragma unroll
+      for (int j = 0; j < NS; ++j) {
+        if (act[j]) {
+          ++caphits;
+          X[j] = (float)n;
+        }
+      }
+      break;
+    }
+    const float nf = (float)n;
+    const float r = rcp_approx(nf);
+    any = false;
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+      p[j] *= lam[j] * r;
+      F[j] += p[j];
+      const bool go = U > F[j] && (fast || !(p[j] < F[j] * 5.0e-8f));
+      X[j] = act[j] && !go ? nf : X[j];
+      act[j] = act[j] && go;
+      any |= act[j];
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < NS; ++j) N[j] = (int)X[j];
+}
+
+// One out-of-line copy for the kernels that invert one mean per draw.
 static __device__ __noinline__ int poisson_core(float lam, float U, float W,
                                                 unsigned long long x, unsigned int cap,
                                                 unsigned int &caphits) {
-  float X = 0.0f;
-  if (lam > 4.0f) {
-    const float rl = sqrt_approx(lam);
-    const float li = 1.0f / lam;
-    float S, Del;
-    if (fabsf(W) < 3.0f) {
-      S = rl * W + (1.0f / 3.0f + (1.0f / 6.0f) * W * W) * (1.0f - W / (12.0f * rl));
-      Del = fmaf(fmaf(1.0f / 160.0f, W * W, 1.0f / 80.0f), W * W, 1.0f / 40.0f) * li;
-      S = lam + (S + Del);
-    } else {
-      // Newton on sqrt(2((1-R) + R log R)) = W / sqrt(lambda); quadratic
-      // convergence reaches FP32 resolution in a few steps, so a fixed small
-      // budget replaces the FP64 tolerance loop.
-      const float s = W / rl;
-      float R = fmaxf(1.0f + s, 0.1f), R2;
-      for (int it = 0; it < 12; ++it) {
-        R2 = R;
-        const float T = log1pf(R - 1.0f);
-        float S2 = sqrtf(2.0f * xlogx_m1(R - 1.0f));
-        if (R < 1.0f) S2 = -S2;
-        R = R2 - (S2 - s) * S2 / T;
-        if (R < 0.1f * R2) R = 0.1f * R2;
-        if (fabsf(R - R2) <= 2e-7f * R) break;
-      }
-      const float T = log1pf(R - 1.0f);
-      S = lam * R + __logf(sqrtf(2.0f * R * xlogx_m1(R - 1.0f)) / fabsf(R - 1.0f)) / T;
-      S = S - 0.0218f / (S + 0.065f * lam);
-      Del = 0.01f / S;
-      S = S + Del;
-    }
-    X = floorf(S);
-    if (S > 10.0f && S < X + 2.0f * Del) {
-      if (X > 0.5f * lam && X < 2.0f * lam) {
-        // Temme's uniform asymptotic expansion of the CDF at X - 1 (TOMS 955).
-        const float Xi = 1.0f / X;
-        float Eta = sqrtf(2.0f * xlogx_m1(X * li - 1.0f) / (X * li));
-        if (X > lam) Eta = -Eta;
-        float B1 = 8.0995211567045583e-16f, B0;
-        float T = B1;
-        B0 = -1.9752288294349411e-15f;  T = B0 + T * Eta;
-        B1 = -5.1391118342426808e-16f + 25.0f * B1 * Xi;  T = B1 + T * Eta;
-        B0 = 2.8534893807047458e-14f + 24.0f * B0 * Xi;   T = B0 + T * Eta;
-        B1 = -1.3923887224181616e-13f + 23.0f * B1 * Xi;  T = B1 + T * Eta;
-        B0 = 3.3717632624009806e-13f + 22.0f * B0 * Xi;   T = B0 + T * Eta;
-        B1 = 1.1004392031956284e-13f + 21.0f * B1 * Xi;   T = B1 + T * Eta;
-        B0 = -5.0276692801141763e-12f + 20.0f * B0 * Xi;  T = B0 + T * Eta;
-        B1 = 2.4361948020667402e-11f + 19.0f * B1 * Xi;   T = B1 + T * Eta;
-        B0 = -5.8307721325504166e-11f + 18.0f * B0 * Xi;  T = B0 + T * Eta;
-        B1 = -2.5514193994946487e-11f + 17.0f * B1 * Xi;  T = B1 + T * Eta;
-        B0 = 9.1476995822367933e-10f + 16.0f * B0 * Xi;   T = B0 + T * Eta;
-        B1 = -4.3820360184533521e-09f + 15.0f * B1 * Xi;  T = B1 + T * Eta;
-        B0 = 1.0261809784240299e-08f + 14.0f * B0 * Xi;   T = B0 + T * Eta;
-        B1 = 6.7078535434015332e-09f + 13.0f * B1 * Xi;   T = B1 + T * Eta;
-        B0 = -1.7665952736826086e-07f + 12.0f * B0 * Xi;  T = B0 + T * Eta;
-        B1 = 8.2967113409530833e-07f + 11.0f * B1 * Xi;   T = B1 + T * Eta;
-        B0 = -1.8540622107151585e-06f + 10.0f * B0 * Xi;  T = B0 + T * Eta;
-        B1 = -2.1854485106799979e-06f + 9.0f * B1 * Xi;   T = B1 + T * Eta;
-        B0 = 3.9192631785224383e-05f + 8.0f * B0 * Xi;    T = B0 + T * Eta;
-        B1 = -0.00017875514403292177f + 7.0f * B1 * Xi;   T = B1 + T * Eta;
-        B0 = 0.00035273368606701921f + 6.0f * B0 * Xi;    T = B0 + T * Eta;
-        B1 = 0.0011574074074074078f + 5.0f * B1 * Xi;     T = B1 + T * Eta;
-        B0 = -0.014814814814814815f + 4.0f * B0 * Xi;     T = B0 + T * Eta;
-        B1 = 0.083333333333333329f + 3.0f * B1 * Xi;      T = B1 + T * Eta;
-        B0 = -0.33333333333333331f + 2.0f * B0 * Xi;      T = B0 + T * Eta;
-        T = T / (1.0f + B1 * Xi);
-        T = T * __expf(-0.5f * X * Eta * Eta) * rsqrtf(2.0f * 3.14159265358979f * X);
-        if (X < lam) {
-          T += 0.5f * erfcf(Eta * sqrtf(0.5f * X));
-          if (T > U) X -= 1.0f;
-        } else {
-          T -= 0.5f * erfcf(-Eta * sqrtf(0.5f * X));
-          if (T > -u01c_bits(x)) X -= 1.0f;
-        }
-      } else {
-        // Stirling-corrected ratio, then a 50-term summation (tails only).
-        float Xi = 1.0f / X;
-        float T = -(691.0f / 360360.0f);
-        T = (1.0f / 1188.0f) + T * Xi * Xi;
-        T = -(1.0f / 1680.0f) + T * Xi * Xi;
-        T = (1.0f / 1260.0f) + T * Xi * Xi;
-        T = -(1.0f / 360.0f) + T * Xi * Xi;
-        T = (1.0f / 12.0f) + T * Xi * Xi;
-        T = T * Xi;
-        T = (X - lam) - X * __logf(X * li) - T;
-        if (X < lam) {
-          const float E = __expf(-0.5f * T);
-          float Ssum = 1.0f - E * (U * E) * sqrtf(2.0f * 3.14159265358979f * Xi) * lam;
-          float Tt = 1.0f, Xr = X;
-          for (int i = 1; i < 50; ++i) {
-            Xr -= 1.0f;
-            Tt *= Xr * li;
-            Ssum += Tt;
-          }
-          if (Ssum > 0.0f) X -= 1.0f;
-        } else {
-          const float E = __expf(-0.5f * T);
-          float Ssum = 1.0f - E * (u01c_bits(x) * E) * sqrtf(2.0f * 3.14159265358979f * X);
-          float Xr = X;
-          for (int i = 0; i < 50; ++i) {
-            Xr += 1.0f;
-            Ssum = Ssum * Xr * li + 1.0f;
-          }
-          if (Ssum < 0.0f) X -= 1.0f;
-        }
-      }
-    }
-  }
-  if (X < 10.0f) {
-    // explicit summation of the CDF from 0
-    float p = __expf(-lam);
-    float F = p;
-    unsigned int n = 0;
-    while (U > F) {
-      if (++n > cap) {
-        ++caphits;
-        break;
-      }
-      p *= __fdividef(lam, (float)n);  // n <= cap: approximate division, 2 ulp
-      F += p;
-      if (p < F * 5.0e-8f) break;  // F has stopped moving: deep upper tail
-    }
-    X = (float)n;
-  }
-  return (int)X;
+  return poisson_eval(lam, U, W, x, cap, caphits);
 }
 
 __device__ __forceinline__ int poisson_inv(float lam, unsigned long long x, unsigned int cap,

@@ -48,21 +48,32 @@ __device__ __forceinline__ NciPos nci_pos(const NciTable &tab, unsigned long lon
   return p;
 }
 
-// Chi-squared quantile of row N (d + 2N degrees of freedom) at the cell p of x2.
-__device__ __forceinline__ float nci_row(const NciTable &tab, int N, const NciPos &p,
-                                         unsigned long long x2, unsigned int &fallbacks) {
-  if (N < tab.rows) {
-    const float4 c = p.tail ? __ldg(tab.tail + (size_t)N * (kNciTail - 1) + p.i)
-                            : __ldg(tab.main + (size_t)N * (kNciGrid - 1) + p.i);
-    return fmaf(fmaf(fmaf(c.w, p.t, c.z), p.t, c.y), p.t, c.x);
-  }
-  // Beyond the table (dof >= d + 2*rows): Wilson-Hilferty cube.
-  ++fallbacks;
+// Hermite cell of row N (clamped to the table) at the position p.
+__device__ __forceinline__ float4 nci_cell(const NciTable &tab, int N, const NciPos &p) {
+  const size_t row = (size_t)min(N, tab.rows - 1);
+  return p.tail ? __ldg(tab.tail + row * (kNciTail - 1) + p.i)
+                : __ldg(tab.main + row * (kNciGrid - 1) + p.i);
+}
+
+__device__ __forceinline__ float nci_cubic(const float4 &c, float t) {
+  return fmaf(fmaf(fmaf(c.w, t, c.z), t, c.y), t, c.x);
+}
+
+// Wilson-Hilferty cube for rows beyond the table (dof >= d + 2*rows).
+__device__ __forceinline__ float nci_beyond(const NciTable &tab, int N, unsigned long long x2) {
   const float nu = tab.d + 2.0f * (float)N;
   const float z = inv_normal_bits(x2);
   const float h = 2.0f / (9.0f * nu);
   const float b = 1.0f - h + z * sqrtf(h);
   return fmaxf(nu * b * b * b, 0.0f);
+}
+
+// Chi-squared quantile of row N (d + 2N degrees of freedom) at the cell p of x2.
+__device__ __forceinline__ float nci_row(const NciTable &tab, int N, const NciPos &p,
+                                         unsigned long long x2, unsigned int &fallbacks) {
+  if (N < tab.rows) return nci_cubic(nci_cell(tab, N, p), p.t);
+  ++fallbacks;
+  return nci_beyond(tab, N, x2);
 }
 
 __device__ __forceinline__ float nci_quantile(const NciTable &tab, int N,
@@ -318,10 +329,10 @@ __host__ __device__ constexpr int lockstep_sc(int j) { return j < 5 ? j : j + 2;
 // The per-step draws of one factor, shared by every scenario.
 template <int SCH>
 struct FactorDraws {
-  float Z = 0.0f;                 // NV: Gaussian of the variance step
+  float Z = 0.0f;                     // NV: Gaussian of the variance step
   unsigned long long xp = 0, x2 = 0;  // NCI: Poisson and chi-squared draws
-  float U = 0.0f, W = 0.0f;       // NCI: uniform and Gaussian of xp
-  NciPos pos{};                   // NCI: table cell of x2
+  float U = 0.0f;                     // NCI: uniform of xp
+  NciPos pos{};                       // NCI: table cell of x2
 };
 
 template <int SCH>
@@ -332,24 +343,45 @@ __device__ __forceinline__ void factor_draws(FactorDraws<SCH> &d, Xo &rng, const
   } else if (SCH == SCH_NCI) {
     d.xp = draw(rng);
     d.U = u01_bits(d.xp);
-    d.W = inv_normal_bits(d.xp);
     d.x2 = draw(rng);
     d.pos = nci_pos(P.nci[fi], d.x2, P.nci_u999);
   }
 }
 
-// evolve<SCH> (above) with the step's draws given.
-template <int SCH>
-__device__ __forceinline__ float evolve_drawn(float v, const FactorDraws<SCH> &d,
-                                              const FactorConst &f, const SimParams &P, int fi,
-                                              unsigned int &caphits, unsigned int &fallbacks) {
+// evolve<SCH> (above) of one factor for every scenario, with the step's draws
+// given: the Poisson inversions of all scenarios first, then all their table
+// gathers (independent loads in flight together), then the cubic cells.
+template <int SCH, int NS>
+__device__ __forceinline__ void evolve_lockstep(const float (&v)[NS], float (&vn)[NS],
+                                                const FactorDraws<SCH> &d, const SimParams &P,
+                                                int fi, unsigned int &caphits,
+                                                unsigned int &fallbacks) {
   if (SCH == SCH_NV) {
-    const float root = sqrt_approx(fmaf(f.w0, v, f.w1)) + f.w2 * d.Z;
-    return fmaf(f.w0 * root, root, f.w1);
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+      const FactorConst &f = P.sc[lockstep_sc(j)].f[fi];
+      const float root = sqrt_approx(fmaf(f.w0, v[j], f.w1)) + f.w2 * d.Z;
+      vn[j] = fmaf(f.w0 * root, root, f.w1);
+    }
   } else {
-    const float lam = f.w0 * v;
-    const int N = poisson_core(lam, d.U, lam > 4.0f ? d.W : 0.0f, d.xp, P.loop_cap, caphits);
-    return nci_row(P.nci[fi], N, d.pos, d.x2, fallbacks) * f.w2;
+    float lam[NS];
+    int N[NS];
+#pragma unroll
+    for (int j = 0; j < NS; ++j) lam[j] = P.sc[lockstep_sc(j)].f[fi].w0 * v[j];
+    poisson_eval_n<NS>(lam, d.U, d.xp, P.loop_cap, caphits, N);
+    const NciTable &tab = P.nci[fi];
+    float4 c[NS];
+#pragma unroll
+    for (int j = 0; j < NS; ++j) c[j] = nci_cell(tab, N[j], d.pos);
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+      float q = nci_cubic(c[j], d.pos.t);
+      if (N[j] >= tab.rows) {
+        ++fallbacks;
+        q = nci_beyond(tab, N[j], d.x2);
+      }
+      vn[j] = q * P.sc[lockstep_sc(j)].f[fi].w2;
+    }
   }
 }
 
@@ -382,12 +414,15 @@ __global__ void __launch_bounds__(kSimBlock) simulate_lockstep_kernel(
       FactorDraws<S2> db;
       factor_draws<S1>(da, rng, P, 0);
       if (NF == 2) factor_draws<S2>(db, rng, P, 1);
+      float van[NSIM], vbn[NSIM];
+      evolve_lockstep<S1, NSIM>(va, van, da, P, 0, caphits, fallbacks);
+      if (NF == 2) evolve_lockstep<S2, NSIM>(vb, vbn, db, P, 1, caphits, fallbacks);
 #pragma unroll
       for (int j = 0; j < NSIM; ++j) {
         const ScenarioConst &C = P.sc[lockstep_sc(j)];
         if (NF == 1) {
           const FactorConst &f = C.f[0];
-          const float vn = evolve_drawn<S1>(va[j], da, f, P, 0, caphits, fallbacks);
+          const float vn = van[j];
           const float root = sqrt_approx(f.C3 * (va[j] + vn));
           const float drift = fmaf(f.C2, vn, fmaf(f.C1, va[j], f.C0));
           X[j] += fmaf(root, G, drift);
@@ -395,14 +430,12 @@ __global__ void __launch_bounds__(kSimBlock) simulate_lockstep_kernel(
         } else {
           const FactorConst &f0 = C.f[0];
           const FactorConst &f1 = C.f[1];
-          const float van = evolve_drawn<S1>(va[j], da, f0, P, 0, caphits, fallbacks);
-          const float vbn = evolve_drawn<S2>(vb[j], db, f1, P, 1, caphits, fallbacks);
-          const float root = sqrt_approx(fmaf(f0.C3, va[j] + van, f1.C3 * (vb[j] + vbn)));
-          const float drift = fmaf(f1.C2, vbn, fmaf(f1.C1, vb[j], fmaf(f0.C2, van,
+          const float root = sqrt_approx(fmaf(f0.C3, va[j] + van[j], f1.C3 * (vb[j] + vbn[j])));
+          const float drift = fmaf(f1.C2, vbn[j], fmaf(f1.C1, vb[j], fmaf(f0.C2, van[j],
                                    fmaf(f0.C1, va[j], f0.C0 + f1.C0))));
           X[j] += fmaf(root, G, drift);
-          va[j] = van;
-          vb[j] = vbn;
+          va[j] = van[j];
+          vb[j] = vbn[j];
         }
       }
     }

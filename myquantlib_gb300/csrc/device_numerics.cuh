@@ -153,11 +153,14 @@ __device__ __forceinline__ float log1p_m(float w) {
 
 // Inverse Poisson CDF: smallest N with F_lambda(N) >= U, U = x * 2^-64.
 // Follows the structure of Giles' algorithm (ACM TOMS 955), as used by
-// Numerics::poissinvcdf (math/Numerics.hpp:49-272): for lambda > 4 a
-// normal-asymptotic estimate (with a Newton solve in the tails) whose floor is
-// checked with Temme's uniform expansion when it lies within 2*Delta of an
-// integer; below 10 an explicit summation.  FP32 throughout; the summation
-// runs in plain (unscaled) form, which is exact up to FP32 rounding of the CDF.
+// Numerics::poissinvcdf (math/Numerics.hpp:49-272): a normal-asymptotic
+// estimate (with a Newton solve in the tails) whose floor is checked with
+// Temme's uniform expansion when it lies within 2*Delta of an integer, and an
+// explicit summation for small means and small tail estimates.  Giles sums
+// for every estimate below 10; here a central estimate below 10 is final
+// outside its window and decided by a short sum inside it (kPoissonAsymMin
+// below).  FP32 throughout; the summation runs in plain (unscaled) form,
+// which is exact up to FP32 rounding of the CDF.
 // U = u01_bits(x) and, where lam > 4, W = inv_normal_bits(x) depend on the draw
 // alone: callers that invert one draw for several means compute them once.
 // The common regimes (central estimate, summation) are inline; the tail solve
@@ -277,78 +280,117 @@ static __device__ __noinline__ float poisson_check(float lam, float X, float U,
   return X;
 }
 
-// Explicit summation of the CDF from 0: p_n = p_{n-1} * (lam * (1/n)), F_n = F_{n-1} + p_n,
-// until U <= F_n.  A second exit, p_n < 5e-8 F_n (F has stopped moving), guards
-// the deep upper tail.  It cannot fire first when U < 1 - 1e-5: it needs the
-// remaining mass below ~3e-7 while FP32 rounding of F stays under ~3e-6, so F_n
-// already exceeds U there.  Such draws take a loop without it.
+// Explicit summation of the CDF from 0: p_n = p_{n-1} * (lam * (1/n)), F_n = F_{n-1} + p_n.
+// Full summation (tgt = kPoissonSumAll) returns the first n with U <= F_n.  A
+// second exit, p_n < 5e-8 F_n (F has stopped moving), guards the deep upper
+// tail; it cannot fire first when U < 1 - 1e-5, because it needs the remaining
+// mass below ~3e-7 while FP32 rounding of F stays under ~3e-6, so F_n already
+// exceeds U there, and such draws skip it.  A decision (tgt = X - 1 >= 0)
+// returns X - 1 if U <= F_{X-1}, else X.
 constexpr float kPoissonUFast = 0.99999f;
+constexpr float kPoissonSumAll = 1.0e30f;
 
-__device__ __forceinline__ float poisson_sum(float lam, float U, unsigned int cap,
+// Means above this use the normal-asymptotic estimate S of Giles' algorithm.
+// For them S is increasing in W on |W| < 3, and at every step of the CDF
+// (U = F(n), checked for every n and means in (1, 40] on a grid of 1/10000)
+// S(W(U)) lies in [n + 1, n + 1 + 2 Del): so floor(S) is the inverse outside
+// the window [X, X + 2 Del), and X - 1 or X inside it.  Giles sums the CDF
+// whenever X < 10; here only the window cases are decided by a short sum
+// (to X - 1), which gives the same N.
+constexpr float kPoissonAsymMin = 2.5f;
+
+// Giles' estimate (mean above kPoissonAsymMin) and how to finish: done (X is
+// the answer), or a summation with target tgt (see poisson_sum).
+__device__ __forceinline__ bool poisson_finish(float lam, float S, float Del, bool central,
+                                               float U, unsigned long long x, float &X,
+                                               float &tgt) {
+  X = floorf(S);
+  const bool win = S < X + 2.0f * Del;
+  if (win && S > 10.0f) {
+    X = poisson_check(lam, X, U, x);
+    tgt = kPoissonSumAll;
+    return !central && X < 10.0f;
+  }
+  if (central) {
+    tgt = X - 1.0f;
+    return win && X >= 1.0f;
+  }
+  tgt = kPoissonSumAll;
+  return X < 10.0f;  // tail estimates below 10: Giles' summation
+}
+
+__device__ __forceinline__ float poisson_sum(float lam, float U, float tgt, unsigned int cap,
                                              unsigned int &caphits) {
+  const bool fast = U < kPoissonUFast;
+  const bool all = tgt >= kPoissonSumAll;
   float p = __expf(-lam);
   float F = p;
+  float nf = 0.0f;
   unsigned int n = 0;
-  const bool fast = U < kPoissonUFast;
-  while (U > F) {
+  for (;;) {
+    if (all ? (!(U > F) || (!fast && p < F * 5.0e-8f)) : nf >= tgt)
+      return all ? nf : (U <= F ? nf : nf + 1.0f);
     if (++n > cap) {
       ++caphits;
-      break;
+      return (float)n;
     }
-    const float nf = (float)n;
+    nf = (float)n;
     p *= lam * rcp_approx(nf);
     F += p;
-    if (!fast && p < F * 5.0e-8f) break;
   }
-  return (float)n;
 }
 
 __device__ __forceinline__ int poisson_eval(float lam, float U, float W, unsigned long long x,
                                             unsigned int cap, unsigned int &caphits) {
-  float X = 0.0f;
-  if (lam > 4.0f) {
+  float X = 0.0f, tgt = kPoissonSumAll;
+  bool sum = true;
+  if (lam > kPoissonAsymMin) {
     float S, Del;
-    if (fabsf(W) < 3.0f) {
+    const bool central = fabsf(W) < 3.0f;
+    if (central) {
       poisson_central(lam, W, S, Del);
     } else {
       const float2 sd = poisson_newton(lam, W);
       S = sd.x;
       Del = sd.y;
     }
-    X = floorf(S);
-    if (S > 10.0f && S < X + 2.0f * Del) X = poisson_check(lam, X, U, x);
+    sum = poisson_finish(lam, S, Del, central, U, x, X, tgt);
   }
-  if (X < 10.0f) X = poisson_sum(lam, U, cap, caphits);
+  if (sum) X = poisson_sum(lam, U, tgt, cap, caphits);
   return (int)X;
 }
 
 // poisson_eval for NS means on one draw (the bumped scenarios of one path):
 // each N[j] equals poisson_eval(lam[j], U, W, x), where W = inv_normal_bits(x)
-// is computed only if some mean exceeds 4.  The central estimates run as
+// is computed only if some mean needs it.  The central estimates run as
 // straight-line code and the summations share one loop, so the scenarios'
 // arithmetic interleaves and the loop overhead is paid once.
 template <int NS>
 __device__ __forceinline__ void poisson_eval_n(const float (&lam)[NS], float U,
                                                unsigned long long x, unsigned int cap,
                                                unsigned int &caphits, int (&N)[NS]) {
-  float X[NS];
+  float X[NS], tgt[NS];
+  bool act[NS];
   bool big = false;
 #pragma unroll
   for (int j = 0; j < NS; ++j) {
     X[j] = 0.0f;
-    big |= lam[j] > 4.0f;
+    tgt[j] = kPoissonSumAll;
+    act[j] = true;
+    big |= lam[j] > kPoissonAsymMin;
   }
   if (big) {
     const float W = inv_normal_bits(x);
+    const bool central = fabsf(W) < 3.0f;
     float S[NS], Del[NS];
-    if (fabsf(W) < 3.0f) {
+    if (central) {
 #pragma unroll
       for (int j = 0; j < NS; ++j) poisson_central(lam[j], W, S[j], Del[j]);
     } else {
 #pragma unroll
       for (int j = 0; j < NS; ++j) {
         S[j] = Del[j] = 0.0f;
-        if (lam[j] > 4.0f) {
+        if (lam[j] > kPoissonAsymMin) {
           const float2 sd = poisson_newton(lam[j], W);
           S[j] = sd.x;
           Del[j] = sd.y;
@@ -356,30 +398,35 @@ __device__ __forceinline__ void poisson_eval_n(const float (&lam)[NS], float U,
       }
     }
 #pragma unroll
-    for (int j = 0; j < NS; ++j) {
-      if (lam[j] > 4.0f) {
-        X[j] = floorf(S[j]);
-        if (S[j] > 10.0f && S[j] < X[j] + 2.0f * Del[j]) X[j] = poisson_check(lam[j], X[j], U, x);
-      }
-    }
+    for (int j = 0; j < NS; ++j)
+      if (lam[j] > kPoissonAsymMin)
+        act[j] = poisson_finish(lam[j], S[j], Del[j], central, U, x, X[j], tgt[j]);
   }
+  // poisson_sum for every scenario that needs one, in one loop.  A scenario's
+  // p and F are dead once it has finished, so the terms are computed without
+  // branches.
+  const bool fast = U < kPoissonUFast;
   float p[NS], F[NS];
-  bool act[NS];
   bool any = false;
 #pragma unroll
   for (int j = 0; j < NS; ++j) {
-    const bool small = X[j] < 10.0f;
     p[j] = __expf(-lam[j]);
     F[j] = p[j];
-    act[j] = small && U > F[j];
-    if (small) X[j] = 0.0f;
-    any |= act[j];
   }
-  // poisson_sum for every scenario in one loop.  A scenario's p and F are dead
-  // once it has exited, so the terms are computed without branches.
-  const bool fast = U < kPoissonUFast;
+  float nf = 0.0f;
   unsigned int n = 0;
-  while (any) {
+  for (;;) {
+    any = false;
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+      const bool all = tgt[j] >= kPoissonSumAll;
+      const bool stop = all ? (!(U > F[j]) || (!fast && p[j] < F[j] * 5.0e-8f)) : nf >= tgt[j];
+      const float res = all ? nf : (U <= F[j] ? nf : nf + 1.0f);
+      X[j] = act[j] && stop ? res : X[j];
+      act[j] = act[j] && !stop;
+      any |= act[j];
+    }
+    if (!any) break;
     if (++n > cap) {
 #pragma unroll
       for (int j = 0; j < NS; ++j) {
@@ -390,17 +437,12 @@ __device__ __forceinline__ void poisson_eval_n(const float (&lam)[NS], float U,
       }
       break;
     }
-    const float nf = (float)n;
+    nf = (float)n;
     const float r = rcp_approx(nf);
-    any = false;
 #pragma unroll
     for (int j = 0; j < NS; ++j) {
       p[j] *= lam[j] * r;
       F[j] += p[j];
-      const bool go = U > F[j] && (fast || !(p[j] < F[j] * 5.0e-8f));
-      X[j] = act[j] && !go ? nf : X[j];
-      act[j] = act[j] && go;
-      any |= act[j];
     }
   }
 #pragma unroll
@@ -416,7 +458,7 @@ static __device__ __noinline__ int poisson_core(float lam, float U, float W,
 
 __device__ __forceinline__ int poisson_inv(float lam, unsigned long long x, unsigned int cap,
                                            unsigned int &caphits) {
-  const float W = lam > 4.0f ? inv_normal_bits(x) : 0.0f;
+  const float W = lam > kPoissonAsymMin ? inv_normal_bits(x) : 0.0f;
   return poisson_core(lam, u01_bits(x), W, x, cap, caphits);
 }
 

@@ -65,6 +65,30 @@ def test_device_inverse_poisson(engine, oracle_lib):
     assert np.all(np.abs(got - want) <= 1)
 
 
+
+def test_device_inverse_poisson_at_cdf_steps(engine):
+    """U placed 1e-5 on either side of every step F(n) of the CDF, for means on both
+    sides of the summation / asymptotic-estimate boundary: the inversion must be the
+    exact quantile there, where a wrong floor of the estimate would show."""
+    lams, xs, want = [], [], []
+    for lam in np.linspace(0.05, 30.0, 600):
+        n = np.arange(0, int(lam + 8.0 * np.sqrt(lam) + 10))
+        F = stats.poisson.cdf(n, lam)
+        for d in (-1e-5, 1e-5):
+            U = F + d
+            # keep points at least 2e-6 from every step: nearer ones are within FP32
+            # rounding of the summed CDF
+            gap = np.min(np.abs(U[:, None] - F[None, :]), axis=1)
+            U = U[(U > 1e-7) & (U < 1.0 - 1e-7) & (gap > 2e-6)]
+            lams.append(np.full(U.size, lam))
+            xs.append(np.floor(U * 2.0**64).astype(np.uint64))
+            want.append(stats.poisson.ppf(U, lam))
+    lam, x, want = np.concatenate(lams), np.concatenate(xs), np.concatenate(want)
+    got = engine.sampler(1, x, lam).astype(np.float64)
+    bad = got != want
+    assert not bad.any(), (int(bad.sum()), lam[bad][:5], x[bad][:5] / 2.0**64, got[bad][:5], want[bad][:5])
+
+
 def test_device_chi2_quantile(engine):
     rng = np.random.default_rng(9)
     dof = np.concatenate([[0.494] * 6, rng.uniform(0.05, 2500, 200)])

@@ -68,6 +68,12 @@ __device__ __forceinline__ float rcp_approx(float x) {
   return r;
 }
 
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 // Inverse normal CDF of p = x * 2^-64, FP32.
 // Central region p in [6.2e-4, 1 - 6.2e-4] (w <= 6 below):
 //   z = (p - 1/2) * R(w),  w = -log(4 p (1 - p)),
@@ -169,10 +175,11 @@ __device__ __forceinline__ float log1p_m(float w) {
 
 // Normal-asymptotic estimate S and its error window Del, lambda > 4, |W| < 3.
 __device__ __forceinline__ void poisson_central(float lam, float W, float &S, float &Del) {
-  const float rl = sqrt_approx(lam);
-  const float li = rcp_approx(lam);
+  const float ir = rsqrt_approx(lam);  // 1/sqrt(lam): sqrt(lam) = lam * ir, 1/lam = ir^2
+  const float rl = lam * ir;
+  const float li = ir * ir;
   const float S1 = rl * W + (1.0f / 3.0f + (1.0f / 6.0f) * W * W) *
-                                (1.0f - W * (1.0f / 12.0f) * rcp_approx(rl));
+                                (1.0f - W * (1.0f / 12.0f) * ir);
   Del = fmaf(fmaf(1.0f / 160.0f, W * W, 1.0f / 80.0f), W * W, 1.0f / 40.0f) * li;
   S = __fadd_rn(lam, S1 + Del);  // never contracted with the caller's product
 }
@@ -281,12 +288,12 @@ static __device__ __noinline__ float poisson_check(float lam, float X, float U,
 }
 
 // Explicit summation of the CDF from 0: p_n = p_{n-1} * (lam * (1/n)), F_n = F_{n-1} + p_n.
-// Full summation (tgt = kPoissonSumAll) returns the first n with U <= F_n.  A
-// second exit, p_n < 5e-8 F_n (F has stopped moving), guards the deep upper
-// tail; it cannot fire first when U < 1 - 1e-5, because it needs the remaining
-// mass below ~3e-7 while FP32 rounding of F stays under ~3e-6, so F_n already
-// exceeds U there, and such draws skip it.  A decision (tgt = X - 1 >= 0)
-// returns X - 1 if U <= F_{X-1}, else X.
+// It returns the first n with U <= F_n, or lim if that comes first (lim = X
+// decides between X - 1 and X; kPoissonSumAll sums without limit).  A second
+// exit, p_n < 5e-8 F_n (F has stopped moving), guards the deep upper tail; it
+// cannot fire first when U < 1 - 1e-5, because it needs the remaining mass
+// below ~3e-7 while FP32 rounding of F stays under ~3e-6, so F_n already
+// exceeds U there, and such draws skip it.
 constexpr float kPoissonUFast = 0.99999f;
 constexpr float kPoissonSumAll = 1.0e30f;
 
@@ -300,36 +307,33 @@ constexpr float kPoissonSumAll = 1.0e30f;
 constexpr float kPoissonAsymMin = 2.5f;
 
 // Giles' estimate (mean above kPoissonAsymMin) and how to finish: done (X is
-// the answer), or a summation with target tgt (see poisson_sum).
+// the answer), or a summation with limit lim (see poisson_sum).
 __device__ __forceinline__ bool poisson_finish(float lam, float S, float Del, bool central,
                                                float U, unsigned long long x, float &X,
-                                               float &tgt) {
+                                               float &lim) {
   X = floorf(S);
   const bool win = S < X + 2.0f * Del;
+  lim = kPoissonSumAll;
   if (win && S > 10.0f) {
     X = poisson_check(lam, X, U, x);
-    tgt = kPoissonSumAll;
     return !central && X < 10.0f;
   }
   if (central) {
-    tgt = X - 1.0f;
+    lim = X;
     return win && X >= 1.0f;
   }
-  tgt = kPoissonSumAll;
   return X < 10.0f;  // tail estimates below 10: Giles' summation
 }
 
-__device__ __forceinline__ float poisson_sum(float lam, float U, float tgt, unsigned int cap,
+__device__ __forceinline__ float poisson_sum(float lam, float U, float lim, unsigned int cap,
                                              unsigned int &caphits) {
   const bool fast = U < kPoissonUFast;
-  const bool all = tgt >= kPoissonSumAll;
   float p = __expf(-lam);
   float F = p;
   float nf = 0.0f;
   unsigned int n = 0;
   for (;;) {
-    if (all ? (!(U > F) || (!fast && p < F * 5.0e-8f)) : nf >= tgt)
-      return all ? nf : (U <= F ? nf : nf + 1.0f);
+    if (!(U > F) || nf >= lim || (!fast && p < F * 5.0e-8f)) return nf;
     if (++n > cap) {
       ++caphits;
       return (float)n;
@@ -342,7 +346,7 @@ __device__ __forceinline__ float poisson_sum(float lam, float U, float tgt, unsi
 
 __device__ __forceinline__ int poisson_eval(float lam, float U, float W, unsigned long long x,
                                             unsigned int cap, unsigned int &caphits) {
-  float X = 0.0f, tgt = kPoissonSumAll;
+  float X = 0.0f, lim = kPoissonSumAll;
   bool sum = true;
   if (lam > kPoissonAsymMin) {
     float S, Del;
@@ -354,9 +358,9 @@ __device__ __forceinline__ int poisson_eval(float lam, float U, float W, unsigne
       S = sd.x;
       Del = sd.y;
     }
-    sum = poisson_finish(lam, S, Del, central, U, x, X, tgt);
+    sum = poisson_finish(lam, S, Del, central, U, x, X, lim);
   }
-  if (sum) X = poisson_sum(lam, U, tgt, cap, caphits);
+  if (sum) X = poisson_sum(lam, U, lim, cap, caphits);
   return (int)X;
 }
 
@@ -369,13 +373,13 @@ template <int NS>
 __device__ __forceinline__ void poisson_eval_n(const float (&lam)[NS], float U,
                                                unsigned long long x, unsigned int cap,
                                                unsigned int &caphits, int (&N)[NS]) {
-  float X[NS], tgt[NS];
+  float X[NS], lim[NS];
   bool act[NS];
   bool big = false;
 #pragma unroll
   for (int j = 0; j < NS; ++j) {
     X[j] = 0.0f;
-    tgt[j] = kPoissonSumAll;
+    lim[j] = kPoissonSumAll;
     act[j] = true;
     big |= lam[j] > kPoissonAsymMin;
   }
@@ -400,49 +404,57 @@ __device__ __forceinline__ void poisson_eval_n(const float (&lam)[NS], float U,
 #pragma unroll
     for (int j = 0; j < NS; ++j)
       if (lam[j] > kPoissonAsymMin)
-        act[j] = poisson_finish(lam[j], S[j], Del[j], central, U, x, X[j], tgt[j]);
+        act[j] = poisson_finish(lam[j], S[j], Del[j], central, U, x, X[j], lim[j]);
   }
-  // poisson_sum for every scenario that needs one, in one loop.  A scenario's
-  // p and F are dead once it has finished, so the terms are computed without
-  // branches.
-  const bool fast = U < kPoissonUFast;
-  float p[NS], F[NS];
   bool any = false;
 #pragma unroll
-  for (int j = 0; j < NS; ++j) {
-    p[j] = __expf(-lam[j]);
-    F[j] = p[j];
-  }
-  float nf = 0.0f;
-  unsigned int n = 0;
-  for (;;) {
+  for (int j = 0; j < NS; ++j) any |= act[j];
+  if (any && !(U < kPoissonUFast)) {
+    // deep upper tail (one draw in 1e5): the scalar summation with its tail exit
+#pragma unroll
+    for (int j = 0; j < NS; ++j)
+      if (act[j]) X[j] = poisson_sum(lam[j], U, lim[j], cap, caphits);
     any = false;
+  }
+  if (any) {
+    // poisson_sum for every scenario that needs one, in one loop.  A
+    // scenario's p and F are dead once it has finished, so the terms are
+    // computed without branches.
+    float p[NS], F[NS];
 #pragma unroll
     for (int j = 0; j < NS; ++j) {
-      const bool all = tgt[j] >= kPoissonSumAll;
-      const bool stop = all ? (!(U > F[j]) || (!fast && p[j] < F[j] * 5.0e-8f)) : nf >= tgt[j];
-      const float res = all ? nf : (U <= F[j] ? nf : nf + 1.0f);
-      X[j] = act[j] && stop ? res : X[j];
-      act[j] = act[j] && !stop;
-      any |= act[j];
+      p[j] = __expf(-lam[j]);
+      F[j] = p[j];
     }
-    if (!any) break;
-    if (++n > cap) {
+    float nf = 0.0f;
+    unsigned int n = 0;
+    for (;;) {
+      any = false;
 #pragma unroll
       for (int j = 0; j < NS; ++j) {
-        if (act[j]) {
-          ++caphits;
-          X[j] = (float)n;
-        }
+        const bool stop = !(U > F[j]) || nf >= lim[j];
+        X[j] = act[j] && stop ? nf : X[j];
+        act[j] = act[j] && !stop;
+        any |= act[j];
       }
-      break;
-    }
-    nf = (float)n;
-    const float r = rcp_approx(nf);
+      if (!any) break;
+      if (++n > cap) {
 #pragma unroll
-    for (int j = 0; j < NS; ++j) {
-      p[j] *= lam[j] * r;
-      F[j] += p[j];
+        for (int j = 0; j < NS; ++j) {
+          if (act[j]) {
+            ++caphits;
+            X[j] = (float)n;
+          }
+        }
+        break;
+      }
+      nf = (float)n;
+      const float r = rcp_approx(nf);
+#pragma unroll
+      for (int j = 0; j < NS; ++j) {
+        p[j] *= lam[j] * r;
+        F[j] += p[j];
+      }
     }
   }
 #pragma unroll

@@ -17,13 +17,14 @@
 namespace myql {
 namespace dev {
 
-template <class FLD>
+template <int SPEC, class FLD>
 __device__ __forceinline__ PathView make_view(const PayoffParams &P, FLD fld, int sc) {
   PathView v;
   const float X = fld(sc, 0);
   v.S = P.S0 * __expf(X);
   v.Y = 0.0f;
   v.hit[0] = v.hit[1] = v.hit[2] = -1.0f;
+  if (SPEC == 1) return v;
   switch (P.tracker) {
     case TRK_GEO_ASIAN: v.Y = P.S0 * __expf(fmaf(P.avg_c1[sc], fld(sc, 1), P.avg_c0[sc])); break;
     case TRK_ARITH_ASIAN: v.Y = P.S0 * fmaf(P.avg_c1[sc], fld(sc, 1), P.avg_c0[sc]); break;
@@ -46,11 +47,11 @@ __device__ __forceinline__ PathView make_view(const PayoffParams &P, FLD fld, in
 
 // Per-path estimators of every quantity for strike K (MonteCarloPricer.hpp:261-276
 // and :316-409), from the increments of each scenario.
-template <class FLD>
+template <int SPEC, class FLD>
 __device__ __forceinline__ void path_quantities(const PayoffParams &P, FLD fld, float K,
                                                 float (&q)[kQ]) {
   const bool bumps = P.mode != 0;
-  const Tri b = scenario_tri(P, make_view(P, fld, 0), K, bumps);
+  const Tri b = scenario_tri<SPEC>(P, make_view<SPEC>(P, fld, 0), K, bumps);
   q[0] = b.v;
   if (!bumps) return;
   q[1] = (b.dp - b.dm) * P.inv_2h;
@@ -58,27 +59,28 @@ __device__ __forceinline__ void path_quantities(const PayoffParams &P, FLD fld, 
   if (P.mode == 1) return;
   const int nv = P.n_factors >= 2 ? 2 : 1;
   for (int fct = 0; fct < nv; ++fct) {
-    const Tri u = scenario_tri(P, make_view(P, fld, fct == 0 ? SC_VUP0 : SC_VUP1), K, true);
-    const Tri d = scenario_tri(P, make_view(P, fld, fct == 0 ? SC_VDN0 : SC_VDN1), K, true);
+    const Tri u = scenario_tri<SPEC>(P, make_view<SPEC>(P, fld, fct == 0 ? SC_VUP0 : SC_VUP1), K, true);
+    const Tri d = scenario_tri<SPEC>(P, make_view<SPEC>(P, fld, fct == 0 ? SC_VDN0 : SC_VDN1), K, true);
     q[fct == 0 ? 3 : 4] = (u.v - d.v) * P.vega_c[fct];
     q[fct == 0 ? 7 : 8] = ((u.dp - u.dm) - (d.dp - d.dm)) * P.vanna_c[fct];
   }
   {
-    const Tri u = scenario_tri(P, make_view(P, fld, SC_TUP), K, true);
-    const Tri d = scenario_tri(P, make_view(P, fld, SC_TDN), K, true);
+    const Tri u = scenario_tri<SPEC>(P, make_view<SPEC>(P, fld, SC_TUP), K, true);
+    const Tri d = scenario_tri<SPEC>(P, make_view<SPEC>(P, fld, SC_TDN), K, true);
     q[5] = ((u.v - d.v) + (u.v * P.dfm1_tup - d.v * P.dfm1_tdn)) * P.theta_c;
     const float du = u.dp - u.dm, dd = d.dp - d.dm;
     q[9] = ((du - dd) + (du * P.dfm1_tup - dd * P.dfm1_tdn)) * P.charm_c;
   }
   {
-    const Tri u = scenario_tri(P, make_view(P, fld, SC_RUP), K, false);
-    const Tri d = scenario_tri(P, make_view(P, fld, SC_RDN), K, false);
+    const Tri u = scenario_tri<SPEC>(P, make_view<SPEC>(P, fld, SC_RUP), K, false);
+    const Tri d = scenario_tri<SPEC>(P, make_view<SPEC>(P, fld, SC_RDN), K, false);
     q[6] = ((u.v - d.v) + (u.v * P.dfm1_rup - d.v * P.dfm1_rdn)) * P.rho_c;
   }
 }
 
 __device__ __forceinline__ int active_q(int mode) { return mode == 0 ? 1 : (mode == 1 ? 3 : kQ); }
 
+template <int SPEC>
 __global__ void __launch_bounds__(kPayoffBlock) payoff_reduce_kernel(const __grid_constant__ PayoffParams P) {
   __shared__ float stage[kPayoffBlock / 32][kMaxScenarios * kMaxFields][33];
   __shared__ double red[kPayoffBlock / 32][2 * kQ][32];
@@ -100,7 +102,7 @@ __global__ void __launch_bounds__(kPayoffBlock) payoff_reduce_kernel(const __gri
       float q[kQ];
 #pragma unroll
       for (int k = 0; k < kQ; ++k) q[k] = 0.0f;
-      path_quantities(P, fld, K, q);
+      path_quantities<SPEC>(P, fld, K, q);
 #pragma unroll
       for (int k = 0; k < kQ; ++k) {
         s1[k] += q[k];
@@ -135,9 +137,9 @@ __global__ void __launch_bounds__(kPayoffBlock) payoff_reduce_kernel(const __gri
   const int kidx = blockIdx.y * 32 + lane;
   const bool kvalid = kidx < P.n_strikes;
   const float K = kvalid ? (float)P.strikes[kidx] : 0.0f;
-  double d1[kQ], d2[kQ];
+  // FP64 running sums per (warp, quantity, lane) in shared memory
 #pragma unroll
-  for (int q = 0; q < kQ; ++q) d1[q] = d2[q] = 0.0;
+  for (int q = 0; q < 2 * kQ; ++q) red[warp][q][lane] = 0.0;
   const int nsf = P.n_sc * F;
   const unsigned long long per_warp = (unsigned long long)P.tile_paths / (kPayoffBlock / 32);
   const unsigned long long w0 = t0 + (unsigned long long)warp * per_warp;
@@ -156,7 +158,7 @@ __global__ void __launch_bounds__(kPayoffBlock) payoff_reduce_kernel(const __gri
         float q[kQ];
 #pragma unroll
         for (int k = 0; k < kQ; ++k) q[k] = 0.0f;
-        path_quantities(P, fld, K, q);
+        path_quantities<SPEC>(P, fld, K, q);
 #pragma unroll
         for (int k = 0; k < kQ; ++k) {
           s1[k] += q[k];
@@ -166,15 +168,12 @@ __global__ void __launch_bounds__(kPayoffBlock) payoff_reduce_kernel(const __gri
     }
 #pragma unroll
     for (int q = 0; q < kQ; ++q) {
-      d1[q] += (double)s1[q];
-      d2[q] += (double)s2[q];
+      if (q < nq) {
+        red[warp][2 * q][lane] += (double)s1[q];
+        red[warp][2 * q + 1][lane] += (double)s2[q];
+      }
     }
     __syncwarp();
-  }
-#pragma unroll
-  for (int q = 0; q < kQ; ++q) {
-    red[warp][2 * q][lane] = d1[q];
-    red[warp][2 * q + 1][lane] = d2[q];
   }
   __syncthreads();
   if (warp == 0 && kvalid) {
@@ -214,7 +213,10 @@ __global__ void finalize_kernel(const FinalizeParams P) {
 cudaError_t launch_payoff(const PayoffParams &P, unsigned long long n_tiles, cudaStream_t stream) {
   if (n_tiles == 0) return cudaSuccess;
   const dim3 grid((unsigned int)n_tiles, P.n_strikes == 1 ? 1u : (unsigned int)((P.n_strikes + 31) / 32));
-  dev::payoff_reduce_kernel<<<grid, kPayoffBlock, 0, stream>>>(P);
+  if (P.kind == 0 && P.payoff == 0 && P.tracker == TRK_EUROPEAN)
+    dev::payoff_reduce_kernel<1><<<grid, kPayoffBlock, 0, stream>>>(P);
+  else
+    dev::payoff_reduce_kernel<0><<<grid, kPayoffBlock, 0, stream>>>(P);
   return cudaGetLastError();
 }
 

@@ -45,10 +45,13 @@ __device__ __forceinline__ float smooth_incr(float x, float c, float phi0) {
 // One payoff of Payoffs.hpp (call/put applied through the sign of y):
 // y0 = +-(spot - strike) at s = 0, b = its change per unit bump,
 // x = the spot-like argument (asset-or-nothing pays x * (1 + s * eps_rel)).
+// SPEC = 1 compiles the vanilla European case alone (the strip workloads);
+// SPEC = 0 dispatches on the request's runtime kind, tracker and payoff.
+template <int SPEC = 0>
 __device__ __forceinline__ Tri payoff_tri(const PayoffParams &P, float y0, float b, float x,
                                           bool smooth, bool bumps) {
   Tri r;
-  if (P.payoff == 0) {
+  if (SPEC == 1 || P.payoff == 0) {
     r.v = fmaxf(y0, 0.0f);
     if (bumps) {
       r.dp = ramp_incr(y0, b);
@@ -93,9 +96,11 @@ struct PathView {
   float hit[3];
 };
 
+template <int SPEC = 0>
 __device__ __forceinline__ Tri scenario_tri(const PayoffParams &P, const PathView &v, float K,
                                             bool bumps) {
   const float sgn = P.option_type == 0 ? 1.0f : -1.0f;
+  if (SPEC == 1) return payoff_tri<1>(P, sgn * (v.S - K), sgn * v.S * P.eps_rel, v.S, false, bumps);
   float x, d0, slope;
   switch (P.kind) {
     case 1:  // Asian (Asian.hpp:114-121)

@@ -195,26 +195,30 @@ static __device__ __noinline__ float2 poisson_newton(float lam, float W) {
     const float T = log1pf(R - 1.0f);
     float S2 = sqrtf(2.0f * xlogx_m1(R - 1.0f));
     if (R < 1.0f) S2 = -S2;
-    R = R2 - (S2 - s) * S2 / T;
+    R = R2 - (S2 - s) * S2 * rcp_approx(T);  // the step only: the root is set by S2
     if (R < 0.1f * R2) R = 0.1f * R2;
     if (fabsf(R - R2) <= 2e-7f * R) break;
   }
   const float T = log1pf(R - 1.0f);
-  float S = lam * R + __logf(sqrtf(2.0f * R * xlogx_m1(R - 1.0f)) / fabsf(R - 1.0f)) / T;
-  S = S - 0.0218f / (S + 0.065f * lam);
-  const float Del = 0.01f / S;
+  // O(1) corrections to lam * R: approximate divisions are far inside Del
+  float S = lam * R + __logf(sqrt_approx(2.0f * R * xlogx_m1(R - 1.0f)) * rcp_approx(fabsf(R - 1.0f))) *
+                          rcp_approx(T);
+  S = S - 0.0218f * rcp_approx(S + 0.065f * lam);
+  const float Del = 0.01f * rcp_approx(S);
   return make_float2(S + Del, Del);
 }
 
 // floor(S) = X lies within 2 Del of an integer: decide between X - 1 and X
 // from the CDF at X - 1.
+// The decision compares a CDF value with U, so approximate reciprocals and
+// square roots (relative error ~1e-7) change it only for U within ~1e-7 of it.
 static __device__ __noinline__ float poisson_check(float lam, float X, float U,
                                                    unsigned long long x) {
-  const float li = 1.0f / lam;
+  const float li = rcp_approx(lam);
   if (X > 0.5f * lam && X < 2.0f * lam) {
     // Temme's uniform asymptotic expansion of the CDF at X - 1 (TOMS 955).
-    const float Xi = 1.0f / X;
-    float Eta = sqrtf(2.0f * xlogx_m1(X * li - 1.0f) / (X * li));
+    const float Xi = rcp_approx(X);
+    float Eta = sqrt_approx(2.0f * xlogx_m1(X * li - 1.0f) * rcp_approx(X * li));
     if (X > lam) Eta = -Eta;
     float B1 = 8.0995211567045583e-16f, B0;
     float T = B1;
@@ -243,18 +247,18 @@ static __device__ __noinline__ float poisson_check(float lam, float X, float U,
     B0 = -0.014814814814814815f + 4.0f * B0 * Xi;     T = B0 + T * Eta;
     B1 = 0.083333333333333329f + 3.0f * B1 * Xi;      T = B1 + T * Eta;
     B0 = -0.33333333333333331f + 2.0f * B0 * Xi;      T = B0 + T * Eta;
-    T = T / (1.0f + B1 * Xi);
-    T = T * __expf(-0.5f * X * Eta * Eta) * rsqrtf(2.0f * 3.14159265358979f * X);
+    T = T * rcp_approx(1.0f + B1 * Xi);
+    T = T * __expf(-0.5f * X * Eta * Eta) * rsqrt_approx(2.0f * 3.14159265358979f * X);
     if (X < lam) {
-      T += 0.5f * erfcf(Eta * sqrtf(0.5f * X));
+      T += 0.5f * erfcf(Eta * sqrt_approx(0.5f * X));
       if (T > U) X -= 1.0f;
     } else {
-      T -= 0.5f * erfcf(-Eta * sqrtf(0.5f * X));
+      T -= 0.5f * erfcf(-Eta * sqrt_approx(0.5f * X));
       if (T > -u01c_bits(x)) X -= 1.0f;
     }
   } else {
     // Stirling-corrected ratio, then a 50-term summation (tails only).
-    float Xi = 1.0f / X;
+    float Xi = rcp_approx(X);
     float T = -(691.0f / 360360.0f);
     T = (1.0f / 1188.0f) + T * Xi * Xi;
     T = -(1.0f / 1680.0f) + T * Xi * Xi;
@@ -265,7 +269,7 @@ static __device__ __noinline__ float poisson_check(float lam, float X, float U,
     T = (X - lam) - X * __logf(X * li) - T;
     if (X < lam) {
       const float E = __expf(-0.5f * T);
-      float Ssum = 1.0f - E * (U * E) * sqrtf(2.0f * 3.14159265358979f * Xi) * lam;
+      float Ssum = 1.0f - E * (U * E) * sqrt_approx(2.0f * 3.14159265358979f * Xi) * lam;
       float Tt = 1.0f, Xr = X;
       for (int i = 1; i < 50; ++i) {
         Xr -= 1.0f;
@@ -275,7 +279,7 @@ static __device__ __noinline__ float poisson_check(float lam, float X, float U,
       if (Ssum > 0.0f) X -= 1.0f;
     } else {
       const float E = __expf(-0.5f * T);
-      float Ssum = 1.0f - E * (u01c_bits(x) * E) * sqrtf(2.0f * 3.14159265358979f * X);
+      float Ssum = 1.0f - E * (u01c_bits(x) * E) * sqrt_approx(2.0f * 3.14159265358979f * X);
       float Xr = X;
       for (int i = 0; i < 50; ++i) {
         Xr += 1.0f;

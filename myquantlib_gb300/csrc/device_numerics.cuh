@@ -189,7 +189,8 @@ __device__ __forceinline__ void poisson_central(float lam, float W, float &S, fl
 // small budget replaces the FP64 tolerance loop.  Returns (S, Del).
 static __device__ __noinline__ float2 poisson_newton(float lam, float W) {
   const float s = W / sqrt_approx(lam);
-  float R = fmaxf(1.0f + s, 0.1f), R2;
+  // start from the inverse series R = 1 + s + s^2/6 - s^3/72 + O(s^4) of the equation
+  float R = fmaxf(1.0f + s * (1.0f + s * (1.0f / 6.0f - s * (1.0f / 72.0f))), 0.1f), R2;
   for (int it = 0; it < 12; ++it) {
     R2 = R;
     const float T = log1pf(R - 1.0f);

@@ -133,9 +133,9 @@ def read_peaks() -> dict:
 
 
 def read_traffic() -> float | None:
-    """DRAM bytes (read + write) of one full-size simulate_kernel launch (T = 1, 2^22 paths),
-    from the ncu summary committed under profiles/ (a `dram_bytes_per_launch: N` line)."""
-    p = ROOT / "profiles" / "simulate_kernel_bates_nci_traffic.md"
+    """DRAM bytes (read + write) of one full-size simulate_lockstep_kernel launch (T = 1, 2^22
+    paths), from the ncu summary committed under profiles/ (a `dram_bytes_per_launch: N` line)."""
+    p = ROOT / "profiles" / "simulate_lockstep_bates_nci_traffic.md"
     if p.exists():
         for line in p.read_text().splitlines():
             if line.startswith("dram_bytes_per_launch:"):  # the T = 1 request (2^22 paths)

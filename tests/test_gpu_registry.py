@@ -19,7 +19,7 @@ RECORDS = [
     {"model": "BatesKou", "heston1": [1.5, 0.04, 0.3, -0.7, 0.04], "kou": [0.8, 0.4, 10.0, 5.0],
      "instrument": "UpAndOut", "option_type": "Call", "strikes": [100.0], "maturity": 1.0, "barrier": 130.0,
      "r": 0.02, "paths": 1 << 15, "steps": 100, "mode": "Essential", "scheme": "Exact"},
-    {"model": "DoubleHeston", "heston1": [1.5, 0.04, 0.3, -0.7, 0.04], "heston2": [0.5, 0.02, 0.2, -0.3, 0.03],
+    {"model": "DoubleHeston", "heston1": [1.5, 0.04, 0.3, -0.7, 0.04], "heston2": [0.5, 0.03, 0.2, -0.3, 0.03],
      "instrument": "LookbackFloating", "option_type": "Put", "maturity": 0.5, "r": 0.01,
      "paths": 1 << 15, "steps": 32, "scheme": "NV"},
     {"model": "Bates", "heston1": [2.0, 0.05, 0.9, -0.6, 0.05], "merton": [0.5, -0.1, 0.15],

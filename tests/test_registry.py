@@ -75,7 +75,7 @@ RECORDS = [
     {"model": "Bates", "heston1": [2.0, 0.05, 0.9, -0.6, 0.05], "merton": [0.5, -0.1, 0.15],
      "instrument": "Vanilla", "option_type": "Call", "strikes": [90.0, 100.0, 110.0], "maturity": 1.0,
      "S0": 100.0, "r": 0.02, "q": 0.01, "paths": 65536, "steps": 50, "seed": 7, "mode": "Essential"},
-    {"model": "DoubleHeston", "heston1": [1.5, 0.04, 0.3, -0.7, 0.04], "heston2": [0.5, 0.02, 0.2, -0.3, 0.03],
+    {"model": "DoubleHeston", "heston1": [1.5, 0.04, 0.3, -0.7, 0.04], "heston2": [0.5, 0.03, 0.2, -0.3, 0.03],
      "instrument": "ArithAsian", "option_type": "Put", "strikes": [100.0], "maturity": 2.0,
      "S0": 100.0, "r": 0.02, "paths": 16384, "steps": 64, "scheme": "NV"},
     {"model": "BatesKou", "heston1": [1.5, 0.04, 0.3, -0.7, 0.04], "kou": [0.8, 0.4, 10.0, 5.0],
@@ -85,7 +85,7 @@ RECORDS = [
 ]
 CSV = """model,kappa,theta,sigma,rho,v0,kappa2,theta2,sigma2,rho2,v02,jump_lambda,merton_mu,merton_delta,kou_p_up,kou_eta1,kou_eta2,instrument,option_type,strikes,maturity,barrier,rebate,S0,r,q,paths,steps,seed,mode,scheme,t_bump
 Bates,2.0,0.05,0.9,-0.6,0.05,,,,,,0.5,-0.1,0.15,,,,Vanilla,Call,90;100;110,1.0,,,100,0.02,0.01,65536,50,7,Essential,,
-DoubleHeston,1.5,0.04,0.3,-0.7,0.04,0.5,0.02,0.2,-0.3,0.03,,,,,,,ArithAsian,Put,100,2.0,,,100,0.02,,16384,64,,,NV,
+DoubleHeston,1.5,0.04,0.3,-0.7,0.04,0.5,0.03,0.2,-0.3,0.03,,,,,,,ArithAsian,Put,100,2.0,,,100,0.02,,16384,64,,,NV,
 BatesKou,1.5,0.04,0.3,-0.7,0.04,,,,,,0.8,,,0.4,10.0,5.0,UpAndOut,Call,100,1.0,130,1.0,100,0.03,,32768,100,,Full,Exact,0.001
 """
 

@@ -359,7 +359,8 @@ typedef struct myql_cv_result {
 } myql_cv_result;
 
 /* Pilot simulation + training; the network stays in the context.  res (may be
- * NULL) reports the in-sample estimators on the pilot paths. */
+ * NULL) reports the in-sample estimators on the first min(pilot_paths, 2^17)
+ * pilot paths (res->paths = pilot paths trained on). */
 myql_status myql_cv_train(myql_ctx *ctx, const myql_mc_job *job, const myql_cv_config *cfg,
                           myql_cv_result *res);
 /* Prices job (its own seed, paths and streams) with the context's network. */

@@ -534,11 +534,13 @@ myql_status myql_cv_train(myql_ctx *ctx_, const myql_mc_job *job, const myql_cv_
     if (e != cudaSuccess) return cuda_status(e, "cv_adam launch");
     ctx->launches += 3;
   }
-  // in-sample variance before / after on the whole pilot set
-  s = forward(ctx, S, (const uint8_t *)S.p_feat.p, (const float *)S.p_dM.p, P, nh, (float *)S.p_cv.p, nullptr);
+  // in-sample variance before / after, on the first min(P, 2^17) pilot paths (a diagnostic:
+  // the out-of-sample ratio of myql_cv_price is the one that counts)
+  const uint64_t Pe = std::min<uint64_t>(P, kCvInSamplePaths);
+  s = forward(ctx, S, (const uint8_t *)S.p_feat.p, (const float *)S.p_dM.p, Pe, nh, (float *)S.p_cv.p, nullptr);
   if (s != MYQL_OK) return s;
   e = cudaMemsetAsync(S.sums.p, 0, 32, ctx->stream);
-  if (e == cudaSuccess) e = launch_cv_reduce((const float *)S.p_Y.p, (const float *)S.p_cv.p, P, (double *)S.sums.p, ctx->stream);
+  if (e == cudaSuccess) e = launch_cv_reduce((const float *)S.p_Y.p, (const float *)S.p_cv.p, Pe, (double *)S.sums.p, ctx->stream);
   double sums[4] = {0, 0, 0, 0};
   std::vector<double> losses(std::max(1u, iters), 0.0);
   if (e == cudaSuccess) e = cudaMemcpyAsync(sums, S.sums.p, 32, cudaMemcpyDeviceToHost, ctx->stream);
@@ -549,7 +551,7 @@ myql_status myql_cv_train(myql_ctx *ctx_, const myql_mc_job *job, const myql_cv_
   if (s != MYQL_OK) return s;
   if (res) {
     std::memset(res, 0, sizeof *res);
-    const double n = (double)P;
+    const double n = (double)Pe;
     const double my = sums[0] / n, vy = std::max(sums[1] / n - my * my, 0.0);
     const double mz = sums[2] / n, vz = std::max(sums[3] / n - mz * mz, 0.0);
     res->plain_price = my;

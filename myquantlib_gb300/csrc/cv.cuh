@@ -34,6 +34,7 @@ constexpr int kCvHidden = 128;
 constexpr int kCvIn = 16;
 constexpr int kCvFeatures = 6;
 constexpr uint32_t kCvTileBytes = 128u * kCvIn * 2u;  // 4096
+constexpr uint64_t kCvInSamplePaths = 1ull << 17;  // pilot paths of the in-sample diagnostic
 
 // FP32 parameter blob: W1 [128][16], b1, W2 [128][128], b2, W3 [128][128], b3, w4 [128], b4
 constexpr int kPW1 = 0;

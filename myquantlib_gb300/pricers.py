@@ -723,10 +723,10 @@ class MonteCarloPricer:
 class ControlVariateConfig:
     """Settings of the neural martingale control variate (no counterpart in the reference)."""
     hedge_every: int = 8          # time steps per hedge interval
-    iterations: int = 300         # Adam steps
+    iterations: int = 120         # Adam steps
     pilot_paths: int = 1 << 18    # training paths (independent seed)
-    batch_paths: int = 8192       # paths per Adam step
-    learning_rate: float = 2e-3
+    batch_paths: int = 4096       # paths per Adam step
+    learning_rate: float = 5e-3
     seed: int = 1
 
     def c(self) -> _abi.CvConfigC:

@@ -213,7 +213,7 @@ myql_status simulate_chunks(CtxBase *ctx, CvSimParams C, int klass, uint64_t see
   return MYQL_OK;
 }
 
-// persistent grids: the forward kernel fits two blocks per SM, the backward one
+// persistent grids: one block per SM
 unsigned int mlp_blocks(const CtxBase *ctx, uint64_t n_pb, int per_sm = 1) {
   return (unsigned int)std::max<uint64_t>(1, std::min<uint64_t>(n_pb, (uint64_t)ctx->sm_count * per_sm));
 }
@@ -240,7 +240,9 @@ myql_status forward(CtxBase *ctx, CvState &S, const uint8_t *feat, const float *
   F.n_pb = (unsigned int)((n_paths + 127) / 128);
   F.n_hedge = nh;
   F.status = (unsigned int *)ctx->status.p;
-  cudaError_t e = launch_cv_mlp(F, mlp_blocks(ctx, F.tile_major ? n_pb * nh : n_pb, 2), ctx->stream);
+  // one block per SM, four tile groups per block
+  const uint64_t units = F.tile_major ? n_pb * nh : n_pb;
+  cudaError_t e = launch_cv_mlp(F, mlp_blocks(ctx, (units + 3) / 4), ctx->stream);
   ctx->launches++;
   if (e == cudaSuccess && F.tile_major) {
     e = launch_cv_rowsum(F.gdm, n_paths, nh, cv, ctx->stream);

@@ -1,12 +1,13 @@
 // cv_mlp.cu -- the control variate's MLP on the tcgen05 tensor cores.
 //
-// cv_mlp_kernel (forward, persistent): weights stay in shared memory; feature
-// tiles of 128 rows stream in by bulk copy (double buffered); per tile three
-// MMA chains (K = 16, 128, 128) accumulate FP32 in TMEM, and the four warps
-// turn each accumulator row into SiLU activations (BF16, written back as the
-// next layer's A operand).  The output layer is a per-row FP32 dot product,
-// multiplied by the row's martingale increment and summed per path over the
-// hedge times.
+// cv_mlp_kernel (forward, persistent, one block per SM): weights stay in shared
+// memory; four groups of four warps each run their own 128-row tiles.  Per
+// tile three MMA chains (K = 16, 128, 128) accumulate FP32 in the group's TMEM
+// columns, and the group's warps turn each accumulator row into SiLU
+// activations (BF16, written back as the next layer's A operand) while the
+// other groups' MMAs run.  Feature tiles stream in by bulk copy behind the
+// first layer.  The output layer is a per-row FP32 dot product, multiplied by
+// the row's martingale increment and summed per path over the hedge times.
 //
 // cv_bwd_kernel (training): per tile, the forward pass again (keeping h1, h2
 // in shared memory), then back-propagation of dL/dg = coef_path * dM_row:
@@ -39,11 +40,11 @@ __device__ __forceinline__ uint8_t *align1024(uint8_t *p) {
 __device__ __forceinline__ void epi_hidden(uint32_t tm_row, const float *bias, uint8_t *H, uint32_t row, int c0 = 0,
                                            int c1 = 4) {
 #pragma unroll 1
-  for (int c = c0; c < c1; ++c) {
-    float v[32];
-    tc::tmem_ld32(tm_row + (uint32_t)(c * 32), v);
+  for (int c = c0; c < c1; c += 2) {
+    float v[64];
+    tc::tmem_ld64(tm_row + (uint32_t)(c * 32), v);  // columns [32 c, 32 c + 64): one round trip
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
+    for (int q = 0; q < 8; ++q) {
       uint32_t w[4];
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
@@ -62,11 +63,11 @@ __device__ __forceinline__ void epi_hidden(uint32_t tm_row, const float *bias, u
 __device__ __forceinline__ float epi_out(uint32_t tm_row, const float *vec, int c0 = 0, int c1 = 4) {
   float g = c0 == 0 ? vec[kVecB4] : 0.0f;
 #pragma unroll 1
-  for (int c = c0; c < c1; ++c) {
-    float v[32];
-    tc::tmem_ld32(tm_row + (uint32_t)(c * 32), v);
+  for (int c = c0; c < c1; c += 2) {
+    float v[64];
+    tc::tmem_ld64(tm_row + (uint32_t)(c * 32), v);
 #pragma unroll
-    for (int i = 0; i < 32; ++i) {
+    for (int i = 0; i < 64; ++i) {
       const int k = c * 32 + i;
       g = fmaf(tc::silu(v[i] + vec[kVecB3 + k]), vec[kVecW4 + k], g);
     }
@@ -126,137 +127,170 @@ __device__ __forceinline__ void block_sync_async() {
 }
 
 // ------------------------------------------------------------------ forward
-// 8 warps: warps w and w + 4 read the same TMEM lane quarter (rows 32 (w % 4) ..)
-// and take the low / high 64 columns of every layer.
-constexpr int kFwdThreads = 256;
+// One block per SM: 16 warps in 4 groups of 4.  Group g owns a tile slot:
+// TMEM columns [128 g, 128 g + 128), an activation image H[g] and a feature
+// buffer X[g].  Its warps cover the 128 TMEM lanes (warp w reads lanes
+// 32 (w % 4) ..), so each thread owns one row of the tile and all 128 columns.
+// A group runs its tiles on its own: its elected thread issues the MMAs, the
+// group waits on its own commit barrier and synchronises with a named barrier
+// of 128 threads, so four tiles are in flight per SM and one group's MMAs run
+// under the others' epilogues.  The weights are loaded once per block.
+constexpr int kFwdGroups = 4;
+constexpr int kFwdThreads = 128 * kFwdGroups;
+constexpr uint32_t kFwdH = kImgFwdBytes;                       // H[g] at kFwdH + g * 32 KB
+constexpr uint32_t kFwdX = kFwdH + kFwdGroups * 32768u;         // X[g] at kFwdX + g * 4 KB
+constexpr uint32_t kFwdSmemBytes = kFwdX + kFwdGroups * kCvTileBytes;
 
-__global__ void __launch_bounds__(kFwdThreads, 2) cv_mlp_kernel(const __grid_constant__ CvMlpParams P) {
+__device__ __forceinline__ void group_sync(int id) {
+  asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory");
+}
+// named barrier of one group that also ORs a predicate over its 128 threads
+__device__ __forceinline__ bool group_sync_or(int id, bool pred) {
+  uint32_t r;
+  asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, %2, 128, p;\n\t"
+               "selp.u32 %0, 1, 0, q;\n\t}"
+               : "=r"(r)
+               : "r"((uint32_t)pred), "r"(id)
+               : "memory");
+  return r != 0;
+}
+
+__global__ void __launch_bounds__(kFwdThreads, 1) cv_mlp_kernel(const __grid_constant__ CvMlpParams P) {
   extern __shared__ uint8_t dyn[];
-  __shared__ __align__(8) uint64_t bar_w, bar_x[2], bar_mma;
+  __shared__ __align__(8) uint64_t bar_w, bar_x[kFwdGroups], bar_mma[kFwdGroups];
   __shared__ uint32_t tmem_base;
   __shared__ float vec[kVecCount];
-  __shared__ float part[128];
   uint8_t *sm = align1024(dyn);
-  uint8_t *sW1 = sm + kImgW1, *sW2 = sm + kImgW2, *sW3 = sm + kImgW3, *sH = sm + kImgFwdBytes;
-  uint8_t *sX = sH + 32768;
+  uint8_t *sW1 = sm + kImgW1, *sW2 = sm + kImgW2, *sW3 = sm + kImgW3;
   const int tid = threadIdx.x, warp = tid >> 5;
-  const uint32_t row = (uint32_t)(tid & 127);
-  const int half = warp >> 2;  // column half: [64 half, 64 half + 64)
+  const int grp = warp >> 2, gtid = tid & 127;
+  const bool elected = gtid == 0;
+  const int bar_id = 1 + grp;  // named barrier of the group (0 is __syncthreads)
+  const uint32_t row = (uint32_t)gtid;  // = 32 (warp % 4) + lane
+  uint8_t *sH = sm + kFwdH + (uint32_t)grp * 32768u;
+  uint8_t *sX = sm + kFwdX + (uint32_t)grp * kCvTileBytes;
   for (int i = tid; i < kVecCount; i += kFwdThreads) vec[i] = P.vec[i];
   if (tid == 0) {
     tc::mbar_init(&bar_w, 1);
-    tc::mbar_init(&bar_x[0], 1);
-    tc::mbar_init(&bar_x[1], 1);
-    tc::mbar_init(&bar_mma, 1);
+    for (int g = 0; g < kFwdGroups; ++g) {
+      tc::mbar_init(&bar_x[g], 1);
+      tc::mbar_init(&bar_mma[g], 1);
+    }
     tc::fence_mbar_init();
   }
   if (warp == 0) {
-    tc::tmem_alloc(&tmem_base, 128);
+    tc::tmem_alloc(&tmem_base, 128 * kFwdGroups);
     tc::tmem_relinquish();
   }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  const uint32_t tm = tmem_base;
+  const uint32_t tm = tmem_base + (uint32_t)(grp * 128);
   const uint32_t tm_row = tm + ((uint32_t)((warp & 3) * 32) << 16);
-  const int c0 = 2 * half, c1 = 2 * half + 2;
-  // path-major: whole path blocks per block (per-path sums in registers);
-  // tile-major: tiles round robin over the blocks (per-row products to P.gdm)
+  // path-major: whole path blocks per group (per-path sums in registers);
+  // tile-major: tiles round robin over all groups (per-row products to P.gdm)
+  const unsigned long long G = (unsigned long long)blockIdx.x * kFwdGroups + grp;
+  const unsigned long long NG = (unsigned long long)gridDim.x * kFwdGroups;
   const unsigned long long n_tiles = (unsigned long long)P.n_pb * P.n_hedge;
   unsigned long long total;
   if (P.tile_major) {
-    total = n_tiles > blockIdx.x ? (n_tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    total = n_tiles > G ? (n_tiles - 1 - G) / NG + 1 : 0;
   } else {
-    const unsigned int n_mine = P.n_pb > blockIdx.x ? (P.n_pb - 1 - blockIdx.x) / gridDim.x + 1 : 0;
-    total = (unsigned long long)n_mine * P.n_hedge;
+    const unsigned long long n_mine = P.n_pb > G ? (P.n_pb - 1 - G) / NG + 1 : 0;
+    total = n_mine * P.n_hedge;
   }
   auto tile_of = [&](unsigned long long t) {
-    if (P.tile_major) return (unsigned long long)blockIdx.x + t * gridDim.x;
-    return ((unsigned long long)blockIdx.x + (t / P.n_hedge) * gridDim.x) * P.n_hedge + t % P.n_hedge;
+    if (P.tile_major) return G + t * NG;
+    return (G + (t / P.n_hedge) * NG) * P.n_hedge + t % P.n_hedge;
   };
-  int pending = -1;  // x buffer with a bulk copy in flight (thread 0) and its phase parity
-  uint32_t pending_parity = 0;
+  bool x_pending = false;  // elected thread: a feature copy in flight on bar_x[grp]
+  uint32_t xphase = 0, mphase = 0;
   if (tid == 0) {
     tc::mbar_arrive_expect_tx(&bar_w, kImgFwdBytes);
     tc::bulk_g2s(sm, P.img, kImgFwdBytes, &bar_w);
-    if (total > 0) {
-      tc::mbar_arrive_expect_tx(&bar_x[0], kCvTileBytes);
-      tc::bulk_g2s(sX, P.feat + tile_of(0) * kCvTileBytes, kCvTileBytes, &bar_x[0]);
-      pending = 0;
-    }
   }
-  bool ok = true;
-  if (tid == 0) ok = tc::mbar_wait(&bar_w, 0, kCvWaitNs);
+  if (elected && total > 0) {
+    tc::mbar_arrive_expect_tx(&bar_x[grp], kCvTileBytes);
+    tc::bulk_g2s(sX, P.feat + tile_of(0) * kCvTileBytes, kCvTileBytes, &bar_x[grp]);
+    x_pending = true;
+  }
+  bool ok = tc::mbar_wait(&bar_w, 0, kCvWaitNs);
   bool err = __syncthreads_or(!ok) != 0;
-  uint32_t phase = 0;
   float acc = 0.0f;
+  auto mma_wait = [&]() {
+    const bool w = tc::mbar_wait(&bar_mma[grp], mphase & 1u, kCvWaitNs);
+    ++mphase;
+    const bool bad = group_sync_or(bar_id, !w);
+    tc::fence_after_sync();
+    return !bad;
+  };
+  auto before_mma = [&]() {  // the group's H writes and TMEM reads done before the next MMA
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    group_sync(bar_id);
+    tc::fence_after_sync();
+  };
   for (unsigned long long t = 0; t < total && !err; ++t) {
     const unsigned long long tile = tile_of(t);
     const unsigned int j = (unsigned int)(tile % P.n_hedge);
-    if (tid == 0) {
-      if (t + 1 < total) {
-        const int nb = (int)((t + 1) & 1);
-        tc::mbar_arrive_expect_tx(&bar_x[nb], kCvTileBytes);
-        tc::bulk_g2s(sX + nb * kCvTileBytes, P.feat + tile_of(t + 1) * kCvTileBytes, kCvTileBytes, &bar_x[nb]);
-      }
-      ok = tc::mbar_wait(&bar_x[t & 1], (uint32_t)((t >> 1) & 1), kCvWaitNs);
-      pending = (t + 1 < total) ? (int)((t + 1) & 1) : -1;
-      pending_parity = (uint32_t)(((t + 1) >> 1) & 1);
-      if (ok) {
-        tc::fence_after_sync();
-        tc::mma_bf16(tm, tc::desc_img16(tc::smem_u32(sX + (t & 1) * kCvTileBytes)), tc::desc_img16(tc::smem_u32(sW1)),
-                     tc::idesc_bf16(128, 128), 0u);
-        tc::mma_commit(&bar_mma);
-      }
+    // layer 1: features landed, and the group's last tile left TMEM (its loads done)
+    ok = true;
+    if (elected) {
+      ok = tc::mbar_wait(&bar_x[grp], xphase & 1u, kCvWaitNs);
+      ++xphase;
+      x_pending = !ok;
     }
-    if (__syncthreads_or(!ok)) { err = true; break; }
-    if (!block_wait(&bar_mma, phase)) { err = true; break; }
-    epi_hidden(tm_row, vec + kVecB1, sH, row, c0, c1);
-    block_sync_async();
-    if (tid == 0) {
-      mma_k128(tm, sH, sW2, 128, 0u);
-      tc::mma_commit(&bar_mma);
-    }
-    if (!block_wait(&bar_mma, phase)) { err = true; break; }
-    epi_hidden(tm_row, vec + kVecB2, sH, row, c0, c1);
-    block_sync_async();
-    if (tid == 0) {
-      mma_k128(tm, sH, sW3, 128, 0u);
-      tc::mma_commit(&bar_mma);
-    }
-    if (!block_wait(&bar_mma, phase)) { err = true; break; }
-    const float gpart = epi_out(tm_row, vec, c0, c1);
-    if (half == 1) part[row] = gpart;
     tc::fence_before_sync();
-    __syncthreads();
+    if (group_sync_or(bar_id, !ok)) { err = true; break; }
     tc::fence_after_sync();
-    if (half == 0) {
-      const float g = gpart + part[row];
-      const unsigned long long r = tile * 128ull + row;
-      if (P.g_out) P.g_out[r] = g;
-      if (P.tile_major) {
-        P.gdm[r] = g * P.dM[r];
-      } else {
-        acc = fmaf(g, P.dM[r], acc);
-        if (j == P.n_hedge - 1) {
-          const unsigned long long path = (tile / P.n_hedge) * 128ull + row;
-          if (path < P.n_paths) P.cv[path] = acc;
-          acc = 0.0f;
-        }
+    if (elected) {
+      tc::mma_bf16(tm, tc::desc_img16(tc::smem_u32(sX)), tc::desc_img16(tc::smem_u32(sW1)),
+                   tc::idesc_bf16(128, 128), 0u);
+      tc::mma_commit(&bar_mma[grp]);
+    }
+    if (!mma_wait()) { err = true; break; }
+    // X is free: the group's next features stream in under layers 2 and 3
+    if (elected && t + 1 < total) {
+      tc::mbar_arrive_expect_tx(&bar_x[grp], kCvTileBytes);
+      tc::bulk_g2s(sX, P.feat + tile_of(t + 1) * kCvTileBytes, kCvTileBytes, &bar_x[grp]);
+      x_pending = true;
+    }
+    epi_hidden(tm_row, vec + kVecB1, sH, row);
+    before_mma();
+    if (elected) {
+      mma_k128(tm, sH, sW2, 128, 0u);
+      tc::mma_commit(&bar_mma[grp]);
+    }
+    if (!mma_wait()) { err = true; break; }
+    epi_hidden(tm_row, vec + kVecB2, sH, row);
+    before_mma();
+    if (elected) {
+      mma_k128(tm, sH, sW3, 128, 0u);
+      tc::mma_commit(&bar_mma[grp]);
+    }
+    if (!mma_wait()) { err = true; break; }
+    const float g = epi_out(tm_row, vec);
+    const unsigned long long r = tile * 128ull + row;
+    if (P.g_out) P.g_out[r] = g;
+    if (P.tile_major) {
+      P.gdm[r] = g * P.dM[r];
+    } else {
+      acc = fmaf(g, P.dM[r], acc);
+      if (j == P.n_hedge - 1) {
+        const unsigned long long path = (tile / P.n_hedge) * 128ull + row;
+        if (path < P.n_paths) P.cv[path] = acc;
+        acc = 0.0f;
       }
     }
-    // the next tile's writes of `part` come after its three MMA waits, each a block barrier
   }
-  if (err) {
-    if (tid == 0) {
-      atomicAdd(P.status + 2, 1u);
-      if (pending >= 0) tc::mbar_wait(&bar_x[pending], pending_parity, kCvWaitNs);
-    }
+  if (err && elected) {
+    atomicAdd(P.status + 2, 1u);
+    if (x_pending) tc::mbar_wait(&bar_x[grp], xphase & 1u, kCvWaitNs);
   }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  if (warp == 0) tc::tmem_dealloc(tm, 128);
+  if (warp == 0) tc::tmem_dealloc(tmem_base, 128 * kFwdGroups);
 }
 
 // ------------------------------------------------------------------ backward
@@ -617,7 +651,7 @@ cudaError_t launch_cv_beta(const float *Y, const float *dM, unsigned long long n
   return cudaGetLastError();
 }
 
-static constexpr uint32_t kFwdSmem = kImgFwdBytes + 32768u + 2u * kCvTileBytes + 1024u;
+static constexpr uint32_t kFwdSmem = dev::kFwdSmemBytes + 1024u;
 static constexpr uint32_t kBwdSmem = 196608u + 1024u;
 
 // Function attributes are set once per device (a bit per device ordinal).
@@ -635,7 +669,6 @@ cudaError_t launch_cv_mlp(const CvMlpParams &P, unsigned int blocks, cudaStream_
   static std::atomic<unsigned long long> attr{0};
   if (attr_needed(attr)) {
     cudaError_t e = cudaFuncSetAttribute(dev::cv_mlp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem);
-    // two blocks per SM (2 x ~113 KB) need the full shared-memory carveout
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(dev::cv_mlp_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
                                (int)cudaSharedmemCarveoutMaxShared);

@@ -56,7 +56,9 @@ def network(engine, seed=3):
     return engine.cv_params().astype(np.float64)
 
 
-@pytest.mark.parametrize("n_paths,n_hedge", [(300, 7), (1024, 32)])
+# the first two run tile-major (minibatch sizes); 160037 paths (1251 ragged path blocks,
+# above 8 per SM) run path-major, whole path blocks per tile group
+@pytest.mark.parametrize("n_paths,n_hedge", [(300, 7), (1024, 32), (160037, 1)])
 def test_cv_forward_matches_cpu_mlp(engine, n_paths, n_hedge):
     params = network(engine)
     feats, dM, _ = mlp_problem(1, n_paths, n_hedge)

@@ -420,7 +420,7 @@ def cv_jobs(m, kind: str, paths: int, seed: int = 42):
     return m.make_job(model, stepper, instr, m.GreekMode.NONE, cfg, 100.0, 0.02, 0.0), steps
 
 
-def cv_config(m, kind: str, pilot: int = 1 << 20, iterations: int = 120):
+def cv_config(m, kind: str, pilot: int = 1 << 19, iterations: int = 120):
     kind = kind.split("_")[0]
     return m.pricers.ControlVariateConfig(hedge_every=8 if kind == "asian" else 5, iterations=iterations,
                                           pilot_paths=pilot, batch_paths=4096, learning_rate=5e-3, seed=7).c()

@@ -24,6 +24,8 @@ struct CvState : ExtState {
   DevBuf p_feat, p_dM, p_Y, p_cv;  // pilot set
   DevBuf feat, dM, Y, cv;          // pricing chunk / caller data
   DevBuf gdm;                      // per-row g dM of the tile-major forward
+  DevBuf gpart;                    // per-block gradient slices of the backward
+  DevBuf rpart;                    // per-block residual sums
   bool init = false;
   uint64_t adam_t = 0;
 };
@@ -62,8 +64,9 @@ myql_status upload_params(CtxBase *ctx, CvState &S, const float *p) {
   if (e == cudaSuccess) e = S.grad.ensure(kPCount * 4);
   if (e == cudaSuccess) e = S.img.ensure(kImgBytes);
   if (e == cudaSuccess) e = S.vec.ensure(kVecCount * 4);
-  if (e == cudaSuccess) e = S.loss.ensure(8 * 4096);
+  if (e == cudaSuccess) e = S.loss.ensure(8ull * 4096 * kResidBlocks);  // [iteration][block] loss partials
   if (e == cudaSuccess) e = S.sums.ensure(128);
+  if (e == cudaSuccess) e = S.rpart.ensure(8 * kResidBlocks);
   if (e == cudaSuccess) e = cudaMemcpyAsync(S.params.p, p, kPCount * 4, cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(S.adam_m.p, 0, kPCount * 4, ctx->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(S.adam_v.p, 0, kPCount * 4, ctx->stream);
@@ -264,9 +267,12 @@ myql_status backward(CtxBase *ctx, CvState &S, const uint8_t *feat, const float 
   B.n_pb = (unsigned int)((n_paths + 127) / 128);
   B.n_hedge = nh;
   B.status = (unsigned int *)ctx->status.p;
-  cudaError_t e = cudaMemsetAsync(S.grad.p, 0, kPCount * 4, ctx->stream);
-  if (e == cudaSuccess) e = launch_cv_bwd(B, mlp_blocks(ctx, (uint64_t)B.n_pb * nh), ctx->stream);
-  ctx->launches++;
+  const unsigned int blocks = mlp_blocks(ctx, (uint64_t)B.n_pb * nh);
+  cudaError_t e = S.gpart.ensure((size_t)blocks * kPCount * 4);
+  if (e != cudaSuccess) return cuda_status(e, "control-variate gradient slices");
+  B.gpart = (float *)S.gpart.p;
+  e = launch_cv_bwd(B, blocks, ctx->stream);
+  ctx->launches += 2;
   return cuda_status(e, "cv_bwd launch");
 }
 
@@ -452,14 +458,21 @@ myql_status myql_cv_gradient(myql_ctx *ctx_, const float *feats, const float *dM
                           (float *)S.cv.p, nullptr);
   if (s != MYQL_OK) return s;
   e = launch_cv_resid((const float *)S.Y.p, (const float *)S.cv.p, n_paths, (float *)S.coef.p, (double *)S.loss.p,
-                      (double *)S.sums.p + 6, ctx->stream);
+                      (double *)S.rpart.p, ctx->stream);
   if (e != cudaSuccess) return cuda_status(e, "cv_resid launch");
   s = backward(ctx, S, (const uint8_t *)S.feat.p, (const float *)S.dM.p, n_paths, n_hedge);
   if (s != MYQL_OK) return s;
+  double lp[kResidBlocks];
   e = cudaMemcpyAsync(grad, S.grad.p, kPCount * 4, cudaMemcpyDeviceToHost, ctx->stream);
-  if (e == cudaSuccess && loss) e = cudaMemcpyAsync(loss, S.loss.p, 8, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(lp, S.loss.p, sizeof lp, cudaMemcpyDeviceToHost, ctx->stream);
   if (e != cudaSuccess) return cuda_status(e, "control-variate gradient results");
-  return wait_status(ctx);
+  s = wait_status(ctx);
+  if (s == MYQL_OK && loss) {
+    double t = 0.0;
+    for (unsigned int b = 0; b < kResidBlocks; ++b) t += lp[b];
+    *loss = t;
+  }
+  return s;
 }
 
 myql_status myql_cv_train(myql_ctx *ctx_, const myql_mc_job *job, const myql_cv_config *cfg, myql_cv_result *res) {
@@ -522,7 +535,8 @@ myql_status myql_cv_train(myql_ctx *ctx_, const myql_mc_job *job, const myql_cv_
     float *cvb = (float *)S.p_cv.p + b0 * 128;
     s = forward(ctx, S, f, dm, nb * 128, nh, cvb, nullptr);
     if (s != MYQL_OK) return s;
-    e = launch_cv_resid(Y, cvb, nb * 128, (float *)S.coef.p, loss + it, (double *)S.sums.p + 6, ctx->stream);
+    e = launch_cv_resid(Y, cvb, nb * 128, (float *)S.coef.p, loss + (size_t)it * kResidBlocks, (double *)S.rpart.p,
+                        ctx->stream);
     if (e != cudaSuccess) return cuda_status(e, "cv_resid launch");
     s = backward(ctx, S, f, dm, nb * 128, nh);
     if (s != MYQL_OK) return s;
@@ -544,10 +558,10 @@ myql_status myql_cv_train(myql_ctx *ctx_, const myql_mc_job *job, const myql_cv_
   e = cudaMemsetAsync(S.sums.p, 0, 32, ctx->stream);
   if (e == cudaSuccess) e = launch_cv_reduce((const float *)S.p_Y.p, (const float *)S.p_cv.p, Pe, (double *)S.sums.p, ctx->stream);
   double sums[4] = {0, 0, 0, 0};
-  std::vector<double> losses(std::max(1u, iters), 0.0);
+  std::vector<double> lparts((size_t)std::max(1u, iters) * kResidBlocks, 0.0);
   if (e == cudaSuccess) e = cudaMemcpyAsync(sums, S.sums.p, 32, cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess && iters)
-    e = cudaMemcpyAsync(losses.data(), loss, iters * 8, cudaMemcpyDeviceToHost, ctx->stream);
+    e = cudaMemcpyAsync(lparts.data(), loss, (size_t)iters * kResidBlocks * 8, cudaMemcpyDeviceToHost, ctx->stream);
   if (e != cudaSuccess) return cuda_status(e, "control-variate training results");
   s = wait_status(ctx);
   if (s != MYQL_OK) return s;
@@ -561,8 +575,13 @@ myql_status myql_cv_train(myql_ctx *ctx_, const myql_mc_job *job, const myql_cv_
     res->price = mz;
     res->price_std_err = std::sqrt(vz / n);
     res->variance_ratio = vz > 0.0 ? vy / vz : 0.0;
-    res->initial_loss = iters ? losses[0] : 0.0;
-    res->final_loss = iters ? losses[iters - 1] : 0.0;
+    auto loss_of = [&](uint32_t it) {  // the step's block partials, in order
+      double t = 0.0;
+      for (unsigned int b = 0; b < kResidBlocks; ++b) t += lparts[(size_t)it * kResidBlocks + b];
+      return t;
+    };
+    res->initial_loss = iters ? loss_of(0) : 0.0;
+    res->final_loss = iters ? loss_of(iters - 1) : 0.0;
     res->paths = P;
     res->train_ms = ms_since(t_train);
     res->total_ms = ms_since(t0);

@@ -35,6 +35,7 @@ constexpr int kCvIn = 16;
 constexpr int kCvFeatures = 6;
 constexpr uint32_t kCvTileBytes = 128u * kCvIn * 2u;  // 4096
 constexpr uint64_t kCvInSamplePaths = 1ull << 17;  // pilot paths of the in-sample diagnostic
+constexpr unsigned int kResidBlocks = 64;           // fixed grid of the residual reductions
 
 // FP32 parameter blob: W1 [128][16], b1, W2 [128][128], b2, W3 [128][128], b3, w4 [128], b4
 constexpr int kPW1 = 0;
@@ -87,7 +88,8 @@ struct CvMlpParams {
   float *gdm;           // tile-major forward: per-row g dM, summed per path by cv_rowsum_kernel
   int tile_major;       // forward: 1 = blocks take tiles round robin, 0 = whole path blocks
   const float *coef;    // backward: dL/dC per path
-  float *grad;          // backward: FP32 parameter-blob gradient (accumulated)
+  float *grad;          // backward: FP32 parameter-blob gradient (written by the reduction)
+  float *gpart;         // backward: per-block gradient slices [gridDim.x][kPCount]
   unsigned long long n_paths;
   unsigned int n_pb, n_hedge;
   unsigned int *status;  // [2] += 1 on a wait that ran out
@@ -266,8 +268,8 @@ cudaError_t launch_cv_bwd(const CvMlpParams &P, unsigned int blocks, cudaStream_
 cudaError_t launch_cv_pack(const float *params, uint8_t *img, float *vec, cudaStream_t st);
 cudaError_t launch_cv_adam(float *params, float *m, float *v, const float *grad, float lr, float b1t, float b2t,
                            cudaStream_t st);
-cudaError_t launch_cv_resid(const float *Y, const float *cv, unsigned long long n, float *coef, double *loss_out,
-                            double *acc, cudaStream_t st);
+cudaError_t launch_cv_resid(const float *Y, const float *cv, unsigned long long n, float *coef, double *loss_part,
+                            double *part, cudaStream_t st);
 cudaError_t launch_cv_beta(const float *Y, const float *dM, unsigned long long n, unsigned int n_hedge,
                            double *sums5, cudaStream_t st);
 cudaError_t launch_cv_rowsum(const float *gdm, unsigned long long n_paths, unsigned int n_hedge, float *cv,

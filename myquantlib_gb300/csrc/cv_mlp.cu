@@ -17,8 +17,9 @@
 //   dh1 = dz2 W2                                        dW2 += dz2^T h1
 //   dz1 = dh1 * silu'(z1)  (z1 recomputed)              dW1 += dz1^T x
 // dW2, dW3 accumulate in TMEM over the block's tiles, dW1 in registers, the
-// bias and output-layer gradients through warp reductions; one FP32 atomic add
-// per parameter and block at the end.
+// bias and output-layer gradients through warp reductions.  Each block writes
+// its gradient to its own slice of a partial buffer, and cv_grad_reduce_kernel
+// sums the slices in block order, so the gradient is deterministic.
 //
 // Every mbarrier wait is bounded; a wait that runs out sets status[2], makes
 // the whole block leave its tile loop, waits (bounded) for its own bulk
@@ -490,28 +491,58 @@ __global__ void __launch_bounds__(kBwdThreads, 1) cv_bwd_kernel(const __grid_con
     __syncthreads();
     tc::fence_after_sync();
   }
-  if (!err && total > 0) {
-    // flush: thread (quarter, half) owns output row o = row of dW2, dW3 (TMEM lane o), columns of its half
-    float *gr = P.grad;
+  // flush: this block's gradient to its own slice of P.gpart (plain vector stores;
+  // cv_grad_reduce_kernel sums the slices in a fixed order).  Thread (quarter, half)
+  // owns output row o = row of dW2, dW3 (TMEM lane o), the columns of its half.
+  const bool flush = !err && total > 0;
+  float *gp = P.gpart + (size_t)blockIdx.x * kPCount;
+  if (flush) {
     for (int c = c0; c < c1; ++c) {
       float v[32];
       tc::tmem_ld32(TW3 + lane_off + (uint32_t)(c * 32), v);
-      for (int i = 0; i < 32; ++i) atomicAdd(gr + kPW3 + row * 128 + c * 32 + i, v[i]);
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        *reinterpret_cast<float4 *>(gp + kPW3 + row * 128 + c * 32 + 4 * q) =
+            make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
       tc::tmem_ld32(TW2 + lane_off + (uint32_t)(c * 32), v);
-      for (int i = 0; i < 32; ++i) atomicAdd(gr + kPW2 + row * 128 + c * 32 + i, v[i]);
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        *reinterpret_cast<float4 *>(gp + kPW2 + row * 128 + c * 32 + 4 * q) =
+            make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
     }
-    if (half == 0)
-      for (int i = 0; i < kCvIn; ++i) atomicAdd(gr + kPW1 + row * kCvIn + i, dw1[i]);
+    if (half == 0) {
+#pragma unroll
+      for (int q = 0; q < kCvIn / 4; ++q)
+        *reinterpret_cast<float4 *>(gp + kPW1 + row * kCvIn + 4 * q) =
+            make_float4(dw1[4 * q], dw1[4 * q + 1], dw1[4 * q + 2], dw1[4 * q + 3]);
+    }
+  }
+  // bias and output-layer sums: the four row quarters meet in the (idle) D buffer
+  float *red = reinterpret_cast<float *>(sD);  // [quarter][b1, b2, b3, w4][128], then b4[quarter]
+  const int qt = warp & 3;
+  if (flush) {
     for (int c = c0; c < c1; ++c) {
       const int col = c * 32 + lane;
-      atomicAdd(gr + kPB1 + col, gb1[c - c0]);
-      atomicAdd(gr + kPB2 + col, gb2[c - c0]);
-      atomicAdd(gr + kPB3 + col, gb3[c - c0]);
-      atomicAdd(gr + kPW4 + col, gw4[c - c0]);
+      red[(qt * 4 + 0) * 128 + col] = gb1[c - c0];
+      red[(qt * 4 + 1) * 128 + col] = gb2[c - c0];
+      red[(qt * 4 + 2) * 128 + col] = gb3[c - c0];
+      red[(qt * 4 + 3) * 128 + col] = gw4[c - c0];
     }
     float s = gb4;
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0 && half == 0) atomicAdd(gr + kPB4, s);
+    if (lane == 0 && half == 0) red[2048 + qt] = s;
+  }
+  __syncthreads();
+  if (flush) {
+    const int dst[4] = {kPB1, kPB2, kPB3, kPW4};
+    for (int i = tid; i < 4 * 128; i += kBwdThreads) {
+      const int v = i >> 7, col = i & 127;
+      gp[dst[v] + col] = ((red[(0 * 4 + v) * 128 + col] + red[(1 * 4 + v) * 128 + col]) +
+                          red[(2 * 4 + v) * 128 + col]) + red[(3 * 4 + v) * 128 + col];
+    }
+    if (tid < 4) gp[kPB4 + tid] = tid == 0 ? ((red[2048] + red[2049]) + red[2050]) + red[2051] : 0.0f;
+  } else {
+    for (int i = tid; i < kPCount; i += kBwdThreads) gp[i] = 0.0f;
   }
   if (err && tid == 0) atomicAdd(P.status + 2, 1u);
   tc::fence_before_sync();
@@ -562,26 +593,58 @@ __global__ void cv_adam_kernel(float *p, float *m, float *v, const float *g, flo
 
 // r_p = Y_p - C_p - mean(Y - C); coef_p = dL/dC_p = -2 r_p / n; loss = mean r^2.
 // Pass 1 sums Y - C into acc[0]; pass 2 writes coef and sums r^2 into acc[1].
-__global__ void cv_resid_sum_kernel(const float *Y, const float *cv, unsigned long long n, double *acc) {
-  double s = 0.0;
-  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
-       i += (unsigned long long)gridDim.x * blockDim.x)
-    s += (double)Y[i] - (double)cv[i];
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(acc, s);
+// grad[p] = sum over the backward blocks' slices, block 0 first (deterministic)
+__global__ void cv_grad_reduce_kernel(const float *gpart, unsigned int nb, float *grad) {
+  const unsigned int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= (unsigned int)kPCount) return;
+  float s = 0.0f;
+  for (unsigned int b = 0; b < nb; ++b) s += gpart[(size_t)b * kPCount + p];
+  grad[p] = s;
 }
-__global__ void cv_resid_coef_kernel(const float *Y, const float *cv, unsigned long long n, double *acc,
-                                     float *coef, double *loss) {
-  const double mu = acc[0] / (double)n;
+
+// Deterministic block sum of 256 threads' FP64 values (warp shuffles, then the
+// 8 warp sums in order); the result is valid in thread 0.
+__device__ __forceinline__ double block_sum256(double v) {
+  __shared__ double ws[8];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < 8; ++w) t += ws[w];
+  return t;
+}
+
+// residuals r = Y - cv - mean(Y - cv): kResidBlocks partial sums of Y - cv, then
+// per path the loss gradient coef = -2 r / n and kResidBlocks partial sums of r^2 / n.
+// Fixed grid and fixed summation order: the results do not depend on scheduling.
+__global__ void __launch_bounds__(256) cv_resid_sum_kernel(const float *Y, const float *cv, unsigned long long n,
+                                                           double *part) {
+  double s = 0.0;
+  for (unsigned long long i = blockIdx.x * 256ull + threadIdx.x; i < n; i += (unsigned long long)gridDim.x * 256ull)
+    s += (double)Y[i] - (double)cv[i];
+  const double t = block_sum256(s);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+__global__ void __launch_bounds__(256) cv_resid_coef_kernel(const float *Y, const float *cv, unsigned long long n,
+                                                            const double *part, float *coef, double *loss_part) {
+  __shared__ double mu_s;
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (unsigned int b = 0; b < gridDim.x; ++b) t += part[b];
+    mu_s = t / (double)n;
+  }
+  __syncthreads();
+  const double mu = mu_s;
   double ss = 0.0;
-  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
-       i += (unsigned long long)gridDim.x * blockDim.x) {
+  for (unsigned long long i = blockIdx.x * 256ull + threadIdx.x; i < n; i += (unsigned long long)gridDim.x * 256ull) {
     const double r = (double)Y[i] - (double)cv[i] - mu;
     ss += r * r;
     coef[i] = (float)(-2.0 * r / (double)n);
   }
-  for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(loss, ss / (double)n);
+  const double t = block_sum256(ss);
+  if (threadIdx.x == 0) loss_part[blockIdx.x] = t / (double)n;
 }
 
 // cv[p] = sum_j gdm[row (p, j)] in hedge order (tile-major forward)
@@ -687,6 +750,9 @@ cudaError_t launch_cv_bwd(const CvMlpParams &P, unsigned int blocks, cudaStream_
     attr_set(attr);
   }
   dev::cv_bwd_kernel<<<blocks, dev::kBwdThreads, kBwdSmem, st>>>(P);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  dev::cv_grad_reduce_kernel<<<(kPCount + 255) / 256, 256, 0, st>>>(P.gpart, blocks, P.grad);
   return cudaGetLastError();
 }
 
@@ -701,15 +767,12 @@ cudaError_t launch_cv_adam(float *params, float *m, float *v, const float *grad,
   return cudaGetLastError();
 }
 
-// acc: two doubles of scratch; loss_out is overwritten with mean r^2
-cudaError_t launch_cv_resid(const float *Y, const float *cv, unsigned long long n, float *coef, double *loss_out,
-                            double *acc, cudaStream_t st) {
-  cudaError_t e = cudaMemsetAsync(acc, 0, 8, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(loss_out, 0, 8, st);
-  if (e != cudaSuccess) return e;
-  const unsigned int blocks = (unsigned int)std::min<unsigned long long>(304ull, (n + 255) / 256);
-  dev::cv_resid_sum_kernel<<<blocks, 256, 0, st>>>(Y, cv, n, acc);
-  dev::cv_resid_coef_kernel<<<blocks, 256, 0, st>>>(Y, cv, n, acc, coef, loss_out);
+// part: kResidBlocks doubles of scratch; loss_part: kResidBlocks partial sums of
+// r^2 / n (the loss is their sum, in order)
+cudaError_t launch_cv_resid(const float *Y, const float *cv, unsigned long long n, float *coef, double *loss_part,
+                            double *part, cudaStream_t st) {
+  dev::cv_resid_sum_kernel<<<kResidBlocks, 256, 0, st>>>(Y, cv, n, part);
+  dev::cv_resid_coef_kernel<<<kResidBlocks, 256, 0, st>>>(Y, cv, n, part, coef, loss_part);
   return cudaGetLastError();
 }
 

@@ -70,6 +70,16 @@ def test_cv_forward_matches_cpu_mlp(engine, n_paths, n_hedge):
     assert np.linalg.norm(cv - cv_ref) <= 1e-2 * np.linalg.norm(cv_ref)
 
 
+def test_cv_gradient_is_deterministic(engine):
+    """The backward blocks write per-block gradient slices that one kernel sums in block
+    order: the same data gives the same gradient bit for bit."""
+    network(engine)
+    feats, dM, Y = mlp_problem(3, 4096, 16)
+    l1, g1 = engine.cv_gradient(feats, dM, Y, 4096, 16)
+    l2, g2 = engine.cv_gradient(feats, dM, Y, 4096, 16)
+    assert np.array_equal(g1, g2) and l1 == l2
+
+
 @pytest.mark.parametrize("n_paths,n_hedge", [(300, 8), (2048, 16)])
 def test_cv_gradient_matches_cpu_mlp(engine, n_paths, n_hedge):
     params = network(engine)

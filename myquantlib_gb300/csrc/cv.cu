@@ -26,6 +26,7 @@ struct CvState : ExtState {
   DevBuf gdm;                      // per-row g dM of the tile-major forward
   DevBuf gpart;                    // per-block gradient slices of the backward
   DevBuf rpart;                    // per-block residual sums
+  DevBuf fpart;                    // per-block price / hedge-ratio sums
   bool init = false;
   uint64_t adam_t = 0;
 };
@@ -67,6 +68,7 @@ myql_status upload_params(CtxBase *ctx, CvState &S, const float *p) {
   if (e == cudaSuccess) e = S.loss.ensure(8ull * 4096 * kResidBlocks);  // [iteration][block] loss partials
   if (e == cudaSuccess) e = S.sums.ensure(128);
   if (e == cudaSuccess) e = S.rpart.ensure(8 * kResidBlocks);
+  if (e == cudaSuccess) e = S.fpart.ensure(8 * 5 * kFoldBlocks);
   if (e == cudaSuccess) e = cudaMemcpyAsync(S.params.p, p, kPCount * 4, cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(S.adam_m.p, 0, kPCount * 4, ctx->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(S.adam_v.p, 0, kPCount * 4, ctx->stream);
@@ -343,7 +345,8 @@ myql_status cv_level_eval(CtxBase *ctx, MlmcCvParams &Q, int klass, uint64_t dN,
     myql_status s = forward(ctx, S, (const uint8_t *)S.feat.p, (const float *)S.dM.p, n, (uint32_t)nh,
                             (float *)S.cv.p, nullptr);
     if (s != MYQL_OK) return s;
-    e = launch_cv_reduce((const float *)S.Y.p, (const float *)S.cv.p, n, (double *)S.sums.p, ctx->stream);
+    e = launch_cv_reduce((const float *)S.Y.p, (const float *)S.cv.p, n, (double *)S.sums.p, (double *)S.fpart.p,
+                         ctx->stream);
     if (e != cudaSuccess) return cuda_status(e, "MLMC control-variate reduction");
     ctx->launches += 2;
   }
@@ -508,7 +511,8 @@ myql_status myql_cv_train(myql_ctx *ctx_, const myql_mc_job *job, const myql_cv_
     double m5[5] = {0, 0, 0, 0, 0};
     e = cudaMemsetAsync(S.sums.p, 0, 40, ctx->stream);
     if (e == cudaSuccess)
-      e = launch_cv_beta((const float *)S.p_Y.p, (const float *)S.p_dM.p, P, nh, (double *)S.sums.p, ctx->stream);
+      e = launch_cv_beta((const float *)S.p_Y.p, (const float *)S.p_dM.p, P, nh, (double *)S.sums.p,
+                         (double *)S.fpart.p, ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(m5, S.sums.p, 40, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_status(e, "control-variate constant hedge");
@@ -556,7 +560,8 @@ myql_status myql_cv_train(myql_ctx *ctx_, const myql_mc_job *job, const myql_cv_
   s = forward(ctx, S, (const uint8_t *)S.p_feat.p, (const float *)S.p_dM.p, Pe, nh, (float *)S.p_cv.p, nullptr);
   if (s != MYQL_OK) return s;
   e = cudaMemsetAsync(S.sums.p, 0, 32, ctx->stream);
-  if (e == cudaSuccess) e = launch_cv_reduce((const float *)S.p_Y.p, (const float *)S.p_cv.p, Pe, (double *)S.sums.p, ctx->stream);
+  if (e == cudaSuccess) e = launch_cv_reduce((const float *)S.p_Y.p, (const float *)S.p_cv.p, Pe, (double *)S.sums.p,
+                                                  (double *)S.fpart.p, ctx->stream);
   double sums[4] = {0, 0, 0, 0};
   std::vector<double> lparts((size_t)std::max(1u, iters) * kResidBlocks, 0.0);
   if (e == cudaSuccess) e = cudaMemcpyAsync(sums, S.sums.p, 32, cudaMemcpyDeviceToHost, ctx->stream);
@@ -632,7 +637,7 @@ myql_status myql_cv_price(myql_ctx *ctx_, const myql_mc_job *job, const myql_cv_
                         if (e2 == cudaSuccess) e2 = cudaEventRecord(ev[2], ctx->stream);
                         if (e2 == cudaSuccess)
                           e2 = launch_cv_reduce((const float *)S.Y.p, (const float *)S.cv.p, n, (double *)S.sums.p,
-                                                ctx->stream);
+                                                (double *)S.fpart.p, ctx->stream);
                         ctx->launches++;
                         if (e2 == cudaSuccess) e2 = cudaEventSynchronize(ev[2]);
                         float a = 0.0f, b = 0.0f;

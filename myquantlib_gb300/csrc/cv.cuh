@@ -36,6 +36,7 @@ constexpr int kCvFeatures = 6;
 constexpr uint32_t kCvTileBytes = 128u * kCvIn * 2u;  // 4096
 constexpr uint64_t kCvInSamplePaths = 1ull << 17;  // pilot paths of the in-sample diagnostic
 constexpr unsigned int kResidBlocks = 64;           // fixed grid of the residual reductions
+constexpr unsigned int kFoldBlocks = 608;           // fixed grid of the price / hedge-ratio sums
 
 // FP32 parameter blob: W1 [128][16], b1, W2 [128][128], b2, W3 [128][128], b3, w4 [128], b4
 constexpr int kPW1 = 0;
@@ -271,10 +272,10 @@ cudaError_t launch_cv_adam(float *params, float *m, float *v, const float *grad,
 cudaError_t launch_cv_resid(const float *Y, const float *cv, unsigned long long n, float *coef, double *loss_part,
                             double *part, cudaStream_t st);
 cudaError_t launch_cv_beta(const float *Y, const float *dM, unsigned long long n, unsigned int n_hedge,
-                           double *sums5, cudaStream_t st);
+                           double *sums5, double *part, cudaStream_t st);
 cudaError_t launch_cv_rowsum(const float *gdm, unsigned long long n_paths, unsigned int n_hedge, float *cv,
                              cudaStream_t st);
-cudaError_t launch_cv_reduce(const float *Y, const float *cv, unsigned long long n, double *sums4,
+cudaError_t launch_cv_reduce(const float *Y, const float *cv, unsigned long long n, double *sums4, double *part,
                              cudaStream_t st);
 
 }  // namespace myql

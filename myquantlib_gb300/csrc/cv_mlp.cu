@@ -658,37 +658,28 @@ __global__ void cv_rowsum_kernel(const float *gdm, unsigned long long n, unsigne
 }
 
 // sums4 += {sum Y, sum Y^2, sum (Y - C), sum (Y - C)^2} (FP64, per-block partials + atomics)
-__global__ void cv_reduce_kernel(const float *Y, const float *cv, unsigned long long n, double *sums4) {
+// Per-block partial sums (fixed grid, warps summed in order), folded into the
+// running sums by cv_fold_kernel in block order: deterministic.
+__global__ void __launch_bounds__(256) cv_reduce_kernel(const float *Y, const float *cv, unsigned long long n,
+                                                        double *part) {
   double a[4] = {0.0, 0.0, 0.0, 0.0};
-  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
-       i += (unsigned long long)gridDim.x * blockDim.x) {
+  for (unsigned long long i = blockIdx.x * 256ull + threadIdx.x; i < n; i += (unsigned long long)gridDim.x * 256ull) {
     const double y = Y[i], z = (double)Y[i] - (double)cv[i];
     a[0] += y;
     a[1] += y * y;
     a[2] += z;
     a[3] += z * z;
   }
-  __shared__ double red[4][8];
+#pragma unroll
   for (int q = 0; q < 4; ++q) {
-    double s = a[q];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = s;
-  }
-  __syncthreads();
-  if (threadIdx.x < 4) {
-    double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[threadIdx.x][w];
-    atomicAdd(sums4 + threadIdx.x, t);
+    const double t = block_sum256(a[q]);
+    if (threadIdx.x == 0) part[blockIdx.x * 4 + q] = t;
   }
 }
-
-// Moments for the constant hedge that starts the training: per path
-// S_p = sum_j dM_pj; sums5 += {S, S^2, Y S, Y, Y^2}.
-__global__ void cv_beta_kernel(const float *Y, const float *dM, unsigned long long n, unsigned int n_hedge,
-                               double *sums5) {
+__global__ void __launch_bounds__(256) cv_beta_kernel(const float *Y, const float *dM, unsigned long long n,
+                                                      unsigned int n_hedge, double *part) {
   double a[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-  for (unsigned long long p = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; p < n;
-       p += (unsigned long long)gridDim.x * blockDim.x) {
+  for (unsigned long long p = blockIdx.x * 256ull + threadIdx.x; p < n; p += (unsigned long long)gridDim.x * 256ull) {
     const unsigned long long pb = p >> 7, lane = p & 127u;
     double sp = 0.0;
     for (unsigned int j = 0; j < n_hedge; ++j) sp += (double)dM[(pb * n_hedge + j) * 128ull + lane];
@@ -699,18 +690,26 @@ __global__ void cv_beta_kernel(const float *Y, const float *dM, unsigned long lo
     a[3] += y;
     a[4] += y * y;
   }
+#pragma unroll
   for (int q = 0; q < 5; ++q) {
-    double s = a[q];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(sums5 + q, s);
+    const double t = block_sum256(a[q]);
+    if (threadIdx.x == 0) part[blockIdx.x * 5 + q] = t;
   }
+}
+// sums[q] += sum over blocks b (in order) of part[b][q]
+__global__ void cv_fold_kernel(const double *part, unsigned int nb, unsigned int nq, double *sums) {
+  if (threadIdx.x >= nq) return;
+  double t = 0.0;
+  for (unsigned int b = 0; b < nb; ++b) t += part[(size_t)b * nq + threadIdx.x];
+  sums[threadIdx.x] += t;
 }
 
 }  // namespace dev
 
 cudaError_t launch_cv_beta(const float *Y, const float *dM, unsigned long long n, unsigned int n_hedge,
-                           double *sums5, cudaStream_t st) {
-  dev::cv_beta_kernel<<<304, 256, 0, st>>>(Y, dM, n, n_hedge, sums5);
+                           double *sums5, double *part, cudaStream_t st) {
+  dev::cv_beta_kernel<<<kFoldBlocks, 256, 0, st>>>(Y, dM, n, n_hedge, part);
+  dev::cv_fold_kernel<<<1, 32, 0, st>>>(part, kFoldBlocks, 5, sums5);
   return cudaGetLastError();
 }
 
@@ -782,9 +781,10 @@ cudaError_t launch_cv_rowsum(const float *gdm, unsigned long long n_paths, unsig
   return cudaGetLastError();
 }
 
-cudaError_t launch_cv_reduce(const float *Y, const float *cv, unsigned long long n, double *sums4,
+cudaError_t launch_cv_reduce(const float *Y, const float *cv, unsigned long long n, double *sums4, double *part,
                              cudaStream_t st) {
-  dev::cv_reduce_kernel<<<1216, 256, 0, st>>>(Y, cv, n, sums4);
+  dev::cv_reduce_kernel<<<kFoldBlocks, 256, 0, st>>>(Y, cv, n, part);
+  dev::cv_fold_kernel<<<1, 32, 0, st>>>(part, kFoldBlocks, 4, sums4);
   return cudaGetLastError();
 }
 

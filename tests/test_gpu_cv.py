@@ -152,3 +152,20 @@ def test_cv_untrained_network_is_still_unbiased(engine):
     network(engine, seed=11)
     res = engine.cv_price(heston_call_job(1 << 18), cfg)
     assert abs(res.price - FOURIER_C1) < 4 * res.price_std_err + 1e-3, (res.price, res.price_std_err)
+
+
+def test_cv_training_and_pricing_are_reproducible(engine):
+    """Every reduction of the control variate (gradient slices, residuals, hedge ratio,
+    price sums) runs on a fixed grid in a fixed order: training twice from the same seed
+    gives the same network bit for bit, and pricing twice gives the same estimate."""
+    cfg = cv_cfg(8, iterations=30, pilot=1 << 14)
+    job = double_bates_asian_job(1 << 14)
+    r1 = engine.cv_train(job, cfg)
+    p1 = engine.cv_params()
+    r2 = engine.cv_train(job, cfg)
+    p2 = engine.cv_params()
+    assert np.array_equal(p1, p2)
+    assert r1.final_loss == r2.final_loss and r1.variance_ratio == r2.variance_ratio
+    pj = double_bates_asian_job(1 << 17, seed=9)
+    a, b = engine.cv_price(pj, cfg), engine.cv_price(pj, cfg)
+    assert a.price == b.price and a.price_std_err == b.price_std_err

@@ -292,6 +292,20 @@ myql_status myql_mlmc_price(myql_ctx *ctx, const myql_mc_job *job,
                             const myql_mlmc_config *mlmc,
                             myql_mlmc_result *result);
 
+/* Multilevel Richardson-Romberg extrapolation (ML2R; listed as future work in
+ * the reference's README.md:335) on the same coupled levels: the level-l
+ * difference is weighted by W_l = sum_{r >= l} w_r, w the Richardson weights for
+ * refinements 2^l and weak order mlmc->alpha (required > 0; re-estimated when
+ * adaptive_rates is set), so the bias is O(h^(alpha (L + 1))) instead of O(h^alpha).
+ * Levels are added while the extrapolations over L + 1 and L levels differ by
+ * more than epsilon / sqrt(2).  result->price = sum_l W_l mean_diffs[l];
+ * mean_diffs / var_diffs stay the unweighted level statistics.  The weights
+ * assume a regular expansion of the weak error in powers of h^alpha: smooth
+ * payoffs and Asians qualify; discretely monitored barriers do not (their error
+ * oscillates with the barrier's position on the monitoring grid). */
+myql_status myql_ml2r_price(myql_ctx *ctx, const myql_mc_job *job, const myql_mlmc_config *mlmc,
+                            myql_mlmc_result *result);
+
 /* One evaluate_level call of the MLMC pricer (MultiLevelMonteCarloPricer.hpp:244-341)
  * from a freshly seeded stream pool: dN paths of level l (0 = base stepper,
  * l > 0 = coupled fine/coarse pair).  sums[0] = sum of P_l - P_(l-1),

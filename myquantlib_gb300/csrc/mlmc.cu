@@ -93,7 +93,38 @@ using namespace myql;
 // network; plain_var (optional) receives the uncorrected level variances.
 static myql_status mlmc_run(myql_ctx *ctx_, const myql_mc_job *job_in, const myql_mlmc_config *cfg,
                             myql_mlmc_result *res, int probe_level, uint64_t probe_dN,
-                            double *probe_sums, bool cv = false, double *plain_var = nullptr);
+                            double *probe_sums, bool cv = false, double *plain_var = nullptr,
+                            bool ml2r = false);
+
+// Weights of the multilevel Richardson-Romberg estimator (Lemaire & Pages,
+// "Multilevel Richardson-Romberg extrapolation", Bernoulli 23(4A), 2017) over
+// the levels 0..L with refinements n_l = 2^l and weak order alpha.  The
+// Richardson weights w solve sum_l w_l x_l^k = [k == 0], k = 0..L, x_l = n_l^-alpha
+// (w_l = prod_{s != l} x_s / (x_s - x_l)); the level-l difference carries
+// W_l = sum_{r >= l} w_r, so W_0 = 1.
+static std::vector<double> ml2r_weights(size_t L, double alpha) {
+  std::vector<double> x(L + 1), w(L + 1), W(L + 1);
+  for (size_t l = 0; l <= L; ++l) x[l] = std::pow(2.0, -alpha * (double)l);
+  for (size_t l = 0; l <= L; ++l) {
+    double t = 1.0;
+    for (size_t s2 = 0; s2 <= L; ++s2)
+      if (s2 != l) t *= x[s2] / (x[s2] - x[l]);
+    w[l] = t;
+  }
+  double acc = 0.0;
+  for (size_t l = L + 1; l-- > 0;) {
+    acc += w[l];
+    W[l] = acc;
+  }
+  return W;
+}
+
+extern "C" myql_status myql_ml2r_price(myql_ctx *ctx_, const myql_mc_job *job_in,
+                                       const myql_mlmc_config *cfg, myql_mlmc_result *res) {
+  if (!res || !cfg) return set_error(MYQL_ERR_INVALID_ARG, "null argument");
+  if (!(cfg->alpha > 0.0)) return set_error(MYQL_ERR_INVALID_ARG, "ML2R needs the weak order alpha > 0");
+  return mlmc_run(ctx_, job_in, cfg, res, -1, 0, nullptr, false, nullptr, true);
+}
 
 extern "C" myql_status myql_mlmc_price(myql_ctx *ctx_, const myql_mc_job *job_in,
                                        const myql_mlmc_config *cfg, myql_mlmc_result *res) {
@@ -136,7 +167,7 @@ extern "C" myql_status myql_mlmc_cv_level(myql_ctx *ctx_, const myql_mc_job *job
 
 static myql_status mlmc_run(myql_ctx *ctx_, const myql_mc_job *job_in, const myql_mlmc_config *cfg,
                             myql_mlmc_result *res, int probe_level, uint64_t probe_dN,
-                            double *probe_sums, bool cv, double *plain_var) {
+                            double *probe_sums, bool cv, double *plain_var, bool ml2r) {
   CtxBase *ctx = reinterpret_cast<CtxBase *>(ctx_);
   if (!ctx || !job_in || !cfg || !res) return set_error(MYQL_ERR_INVALID_ARG, "null argument");
   cudaError_t e = cudaSetDevice(ctx->device);
@@ -283,7 +314,7 @@ static myql_status mlmc_run(myql_ctx *ctx_, const myql_mc_job *job_in, const myq
     return read_status(ctx, nullptr);
   }
   // ---- Giles' adaptive controller (MultiLevelMonteCarloPricer.hpp:64-211)
-  size_t L = cfg->L_min;
+  size_t L = ml2r ? std::max<uint64_t>(cfg->L_min, 1) : cfg->L_min;
   std::vector<uint64_t> N_l(L_max + 1, 0);
   std::vector<double> sum_dP(L_max + 1, 0.0), sum_sq_dP(L_max + 1, 0.0), V_l(L_max + 1, 0.0),
       cost_l(L_max + 1, 0.0);
@@ -292,14 +323,23 @@ static myql_status mlmc_run(myql_ctx *ctx_, const myql_mc_job *job_in, const myq
   const double eps_m2 = std::pow(cfg->epsilon, -2.0);
   bool converged = false;
   int guard = 0;
+  // level weights: 1 for MLMC; the ML2R weights of the current level count
+  std::vector<double> Wt(L_max + 1, 1.0);
+  auto set_weights = [&]() {
+    if (!ml2r) return;
+    const std::vector<double> W = ml2r_weights(L, alpha);
+    for (size_t l = 0; l <= L; ++l) Wt[l] = W[l];
+  };
   while (!converged) {
     if (++guard > 10000) return set_error(MYQL_ERR_LOOP_CAP, "MLMC controller did not converge");
+    set_weights();
     for (size_t l = 0; l <= L; ++l) {
       double sum_sqrt_VC_pilot = 0.0;
-      for (size_t k = 0; k <= L; ++k) sum_sqrt_VC_pilot += std::sqrt(V_l[k] * cost_l[k]);
+      for (size_t k = 0; k <= L; ++k) sum_sqrt_VC_pilot += std::abs(Wt[k]) * std::sqrt(V_l[k] * cost_l[k]);
       uint64_t optimal_N = 0;
       if (V_l[l] > 1e-18)
-        optimal_N = (uint64_t)std::ceil(2.0 * eps_m2 * std::sqrt(V_l[l] / cost_l[l]) * sum_sqrt_VC_pilot);
+        optimal_N = (uint64_t)std::ceil(2.0 * eps_m2 * std::abs(Wt[l]) * std::sqrt(V_l[l] / cost_l[l]) *
+                                        sum_sqrt_VC_pilot);
       const uint64_t pilot_N = std::max<uint64_t>(20, cfg->N0 / (1ull << l));
       const uint64_t target_N = std::max(pilot_N, optimal_N);
       if (N_l[l] < target_N) {
@@ -340,15 +380,32 @@ static myql_status mlmc_run(myql_ctx *ctx_, const myql_mc_job *job_in, const myq
       if (est_alpha > 0.3) alpha = std::min(2.0, est_alpha);
       if (est_beta > 0.3) beta = std::min(2.0, est_beta);
     }
+    set_weights();
     double sum_sqrt_VC = 0.0;
-    for (size_t l = 0; l <= L; ++l) sum_sqrt_VC += std::sqrt(V_l[l] * cost_l[l]);
+    for (size_t l = 0; l <= L; ++l) sum_sqrt_VC += std::abs(Wt[l]) * std::sqrt(V_l[l] * cost_l[l]);
     bool needs_more_paths = false;
     for (size_t l = 0; l <= L; ++l) {
       const uint64_t optimal_N =
-          (uint64_t)std::ceil(2.0 * eps_m2 * std::sqrt(V_l[l] / cost_l[l]) * sum_sqrt_VC);
+          (uint64_t)std::ceil(2.0 * eps_m2 * std::abs(Wt[l]) * std::sqrt(V_l[l] / cost_l[l]) * sum_sqrt_VC);
       if (optimal_N > N_l[l]) needs_more_paths = true;
     }
     if (needs_more_paths) continue;
+    if (ml2r) {
+      // bias test: the extrapolations over L + 1 and over L levels, from the same level
+      // means, differ by about the bias of the smaller one (conservative for the larger)
+      const std::vector<double> Wm = ml2r_weights(L - 1, alpha);
+      double est_L = 0.0, est_Lm1 = 0.0;
+      for (size_t l = 0; l <= L; ++l) {
+        const double m_l = sum_dP[l] / N_l[l];
+        est_L += Wt[l] * m_l;
+        if (l < L) est_Lm1 += Wm[l] * m_l;
+      }
+      if (std::abs(est_L - est_Lm1) > cfg->epsilon / 1.4142135623730951 && L < L_max)
+        L++;
+      else
+        converged = true;
+      continue;
+    }
     const double diff_mean_L = std::abs(sum_dP[L] / N_l[L]);
     double effective_diff = diff_mean_L;
     if (L > 0) effective_diff = std::max(diff_mean_L, 0.5 * std::abs(sum_dP[L - 1] / N_l[L - 1]));
@@ -375,8 +432,8 @@ static myql_status mlmc_run(myql_ctx *ctx_, const myql_mc_job *job_in, const myq
     const double mean_dP = sum_dP[l] / N_l[l];
     res->mean_diffs[l] = mean_dP * df;
     res->var_diffs[l] = V_l[l] * df * df;
-    res->price += mean_dP * df;
-    var_total += V_l[l] / N_l[l];
+    res->price += Wt[l] * mean_dP * df;
+    var_total += Wt[l] * Wt[l] * V_l[l] / N_l[l];
   }
   res->price_std_err = std::sqrt(var_total) * df;
   if (plain_var)

@@ -494,6 +494,18 @@ class Engine:
         _abi.check(self.lib.myql_cv_price(self.handle, C.byref(job.c), C.byref(cfg), C.byref(res)))
         return res
 
+    def mlmc_price(self, job: "_Job", mlmc_cfg: "_abi.MlmcConfigC") -> "_abi.MlmcResultC":
+        """MultiLevelMonteCarloPricer::calculate (MultiLevelMonteCarloPricer.hpp:46-238)."""
+        res = _abi.MlmcResultC()
+        _abi.check(self.lib.myql_mlmc_price(self.handle, C.byref(job.c), C.byref(mlmc_cfg), C.byref(res)))
+        return res
+
+    def ml2r_price(self, job: "_Job", mlmc_cfg: "_abi.MlmcConfigC") -> "_abi.MlmcResultC":
+        """Multilevel Richardson-Romberg extrapolation on the MLMC levels (myql_ml2r_price)."""
+        res = _abi.MlmcResultC()
+        _abi.check(self.lib.myql_ml2r_price(self.handle, C.byref(job.c), C.byref(mlmc_cfg), C.byref(res)))
+        return res
+
     def mlmc_cv_price(self, job: "_Job", mlmc_cfg: "_abi.MlmcConfigC", cv_cfg: "_abi.CvConfigC | None"):
         """MLMC with the control variate on every level -> (result, plain level variances)."""
         res = _abi.MlmcResultC()

@@ -103,6 +103,49 @@ def test_mlmc_european_against_fourier(engine):
     assert g.alpha_estimated > 0.3
 
 
+# ---------------------------------------------------------------- multilevel Richardson-Romberg
+def ml2r_weights(L, alpha):
+    """W_l = sum_{r >= l} w_r, w the Richardson weights (sum_l w_l x_l^k = [k == 0], x_l = 2^(-alpha l))."""
+    x = 2.0 ** (-alpha * np.arange(L + 1))
+    w = np.linalg.solve(np.vander(x, increasing=True).T, np.eye(L + 1)[0])
+    return np.cumsum(w[::-1])[::-1]
+
+
+def fixed_order_cfg(eps, alpha, L_min=1, L_max=8):
+    c = mlmc_cfg(eps, L_min=L_min, L_max=L_max)
+    c.alpha, c.adaptive_rates = alpha, 0
+    return c
+
+
+def test_ml2r_european_against_fourier(engine):
+    """Heston call (SchemeNV, weak order 1): the ML2R price is the W-weighted sum of the
+    level means, agrees with the reference's FP64 Fourier value, and needs no more levels
+    than MLMC at the same tolerance."""
+    j = CASES["heston_eur"]()
+    cfg = fixed_order_cfg(0.01, 1.0)
+    g = engine.ml2r_price(j, cfg)
+    four = FOURIER["c1_heston_call"]["fourier"][0]
+    assert abs(g.price - four) < 4 * g.price_std_err + cfg.epsilon / np.sqrt(2.0), (g.price, four)
+    W = ml2r_weights(g.n_levels - 1, 1.0)
+    assert abs(W[0] - 1.0) < 1e-12
+    assert abs(g.price - sum(W[l] * g.mean_diffs[l] for l in range(g.n_levels))) < 1e-9 * abs(g.price)
+    mc = engine.mlmc_price(j, fixed_order_cfg(0.01, 1.0))
+    assert g.n_levels <= mc.n_levels, (g.n_levels, mc.n_levels)
+
+
+def test_ml2r_asian_against_mlmc(engine):
+    """Black-Scholes arithmetic Asian (weak order 1): ML2R and MLMC agree within their
+    standard errors and tolerances, ML2R with no more levels.  (A discretely monitored
+    barrier has no regular expansion of its error in powers of h, so ML2R is not applied
+    to barriers.)"""
+    j = CASES["bs_asian"]()
+    g = engine.ml2r_price(j, fixed_order_cfg(0.005, 1.0))
+    mc = engine.mlmc_price(j, fixed_order_cfg(0.005, 1.0))
+    assert g.n_levels >= 2 and g.total_steps > 0 and g.n_levels <= mc.n_levels
+    tol = 4 * np.hypot(g.price_std_err, mc.price_std_err) + 0.005 * np.sqrt(2.0)
+    assert abs(g.price - mc.price) < tol, (g.price, mc.price, tol)
+
+
 # ---------------------------------------------------------------- MLMC with the neural control variate
 def cv_cfg_c(iterations=200, pilot=1 << 16):
     return m.pricers.ControlVariateConfig(hedge_every=1, iterations=iterations, pilot_paths=pilot,

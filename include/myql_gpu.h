@@ -306,6 +306,20 @@ myql_status myql_mlmc_price(myql_ctx *ctx, const myql_mc_job *job,
 myql_status myql_ml2r_price(myql_ctx *ctx, const myql_mc_job *job, const myql_mlmc_config *mlmc,
                             myql_mlmc_result *result);
 
+/* Randomized quasi-Monte Carlo (the reference's future work, README.md:331):
+ * Sobol points (Gray-code order; direction numbers from primitive polynomials by
+ * the Bratley-Fox recurrence with seeded odd initial values), a Brownian bridge
+ * per Brownian motion (spot and each CIR factor, bridge levels interleaved), and
+ * n_replicates random digital shifts.  out: price rows as myql_mc_price (standard
+ * error from the spread of the replicate estimates).  Models without jumps, every
+ * factor on SchemeNV, GreekMode None, at most 512 steps, num_paths a multiple of
+ * 2048 * n_replicates (n_replicates >= 2). */
+myql_status myql_qmc_price(myql_ctx *ctx, const myql_mc_job *job, uint32_t n_replicates, double *out,
+                           myql_mc_stats *stats);
+/* The Sobol direction numbers of myql_qmc_price: out[d * 32 + k - 1] = V_k of
+ * dimension d (host computation; needs no GPU). */
+myql_status myql_qmc_directions(uint32_t D, uint64_t seed, uint32_t *out);
+
 /* One evaluate_level call of the MLMC pricer (MultiLevelMonteCarloPricer.hpp:244-341)
  * from a freshly seeded stream pool: dN paths of level l (0 = base stepper,
  * l > 0 = coupled fine/coarse pair).  sums[0] = sum of P_l - P_(l-1),

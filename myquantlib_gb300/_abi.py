@@ -124,6 +124,9 @@ _SIGS = {
                                 C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "myql_mlmc_price": (C.c_int, [C.c_void_p, C.POINTER(McJobC), C.POINTER(MlmcConfigC),
                                   C.POINTER(MlmcResultC)]),
+    "myql_qmc_price": (C.c_int, [C.c_void_p, C.POINTER(McJobC), C.c_uint32, C.POINTER(C.c_double),
+                                 C.POINTER(McStatsC)]),
+    "myql_qmc_directions": (C.c_int, [C.c_uint32, C.c_uint64, C.POINTER(C.c_uint32)]),
     "myql_ml2r_price": (C.c_int, [C.c_void_p, C.POINTER(McJobC), C.POINTER(MlmcConfigC),
                                   C.POINTER(MlmcResultC)]),
     "myql_mlmc_level": (C.c_int, [C.c_void_p, C.POINTER(McJobC), C.POINTER(MlmcConfigC), C.c_uint32,

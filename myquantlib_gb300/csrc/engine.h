@@ -55,7 +55,7 @@ struct CtxBase {
   DevBuf records, partials, out, status, strikes;
   DevBuf probe_a, probe_b, probe_c;
   DevBuf aux_a, aux_b, aux_c, aux_d;  // batch / MLMC / control-variate work buffers
-  std::unique_ptr<ExtState> batch, cv;  // released with the context
+  std::unique_ptr<ExtState> batch, cv, qmc;  // released with the context
   // event pairs around the phase launches of the current call (tag 0 = simulate, 1 = payoff)
   std::vector<cudaEvent_t> ev_pool;
   std::vector<int> ev_tags;
@@ -72,6 +72,7 @@ struct CtxBase {
   void release_all() {
     batch.reset();
     cv.reset();
+    qmc.reset();
     for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
     ev_pool.clear();
     st_cached.release();
@@ -123,5 +124,8 @@ int nci_rows_wanted(const myql_heston_params &p, double dt_min);
 myql_status ensure_streams(CtxBase *ctx, uint64_t seed, uint64_t first, uint64_t n);
 myql_status ensure_nci(CtxBase *ctx, const myql_heston_params &p, double dt_min, NciTable &tab);
 myql_status read_status(CtxBase *ctx, myql_mc_stats *stats);
+// event-timed simulate / payoff phases of the last call
+void phase_times(CtxBase *ctx, double *sim_ms, double *pay_ms);
+cudaError_t launch_payoff(const PayoffParams &P, unsigned long long n_tiles, cudaStream_t stream);
 
 }  // namespace myql

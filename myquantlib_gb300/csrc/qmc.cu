@@ -1,0 +1,407 @@
+// qmc.cu -- randomized quasi-Monte Carlo pricing (myql_qmc_price).
+//
+// The reference lists quasi-Monte Carlo as future work (README.md:331).  Here a
+// path's normals come from a Sobol point instead of xoshiro draws:
+//   * Sobol points in Gray-code order (Antonov-Saleev), direction numbers from
+//     primitive polynomials over GF(2) by the Bratley-Fox recurrence (ACM TOMS
+//     659), dimension 0 the van der Corput sequence.  The initial direction
+//     numbers m_1..m_s of each dimension are odd integers m_k < 2^k drawn from
+//     splitmix64 (a randomly initialised Sobol sequence, not a published table);
+//   * each Brownian motion of the step (the spot's and one per CIR factor) is
+//     built by a Brownian bridge on the step grid, coarse points first, and the
+//     bridge levels of all motions are interleaved so that the first Sobol
+//     dimensions carry the paths' coarse shape;
+//   * R independent random digital shifts (one 32-bit XOR mask per replicate and
+//     dimension) give R unbiased replicate estimates; the price is their mean and
+//     the standard error comes from their spread.
+// Each factor is stepped with SchemeNV (one normal per step, VolSchemes.hpp:52-57),
+// the log-spot as in ASVJstepper.hpp:134-229, and the trackers of the path
+// kernels; the per-path records go through the engine's own payoff pass.
+// Fixed dimension per step is what QMC needs, so the schemes with a variable
+// number of draws per step (Exact, NCI's Poisson mixture) and the jump
+// policies are not offered.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "engine.h"
+#include "simulate.cuh"
+
+namespace myql {
+
+constexpr int kQmcMaxSteps = 512;
+constexpr int kQmcBits = 32;
+
+struct QmcParams {
+  SimParams P;                 // plan constants (records, trackers, scenario 0)
+  const uint32_t *dirs;        // [D][32] direction numbers V_1..V_32
+  const uint32_t *shift;       // [R][D] digital shifts
+  const int *br_mid, *br_left, *br_right;  // Brownian bridge, construction order
+  const float *br_wl, *br_wr, *br_sd;
+  unsigned long long n_pts;    // points per replicate
+  unsigned int D;              // dimensions per path = steps * (1 + factors)
+};
+
+namespace dev {
+
+__device__ __forceinline__ uint32_t sobol_coord(const uint32_t *V, uint32_t g) {
+  uint32_t x = 0;
+  for (int b = 0; g; ++b, g >>= 1)
+    if (g & 1u) x ^= __ldg(V + b);
+  return x;
+}
+
+template <int NF, bool PD>
+__global__ void __launch_bounds__(kSimBlock) qmc_kernel(const __grid_constant__ QmcParams Q) {
+  const SimParams &P = Q.P;
+  const unsigned long long i = blockIdx.x * (unsigned long long)kSimBlock + threadIdx.x;
+  if (i >= P.path_end) return;
+  const unsigned long long rep = i / Q.n_pts, pt = i % Q.n_pts;
+  const uint32_t g = (uint32_t)(pt ^ (pt >> 1));  // Gray code
+  const int n = P.n_steps;
+  constexpr int NC = 1 + NF;  // Brownian motions: the spot's, then one per factor
+  const uint32_t *shift = Q.shift + rep * Q.D;
+  float W[NC][kQmcMaxSteps + 1];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) W[c][0] = 0.0f;
+  for (int b = 0; b < n; ++b) {
+    const int m = Q.br_mid[b], l = Q.br_left[b], r = Q.br_right[b];
+    const float wl = Q.br_wl[b], wr = Q.br_wr[b], sd = Q.br_sd[b];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      const unsigned int d = (unsigned int)b * NC + c;
+      const uint32_t x = sobol_coord(Q.dirs + (size_t)d * kQmcBits, g) ^ __ldg(shift + d);
+      const float z = inv_normal_bits(((unsigned long long)x << 32) | 0x80000000ull);
+      W[c][m] = fmaf(wl, W[c][l], fmaf(wr, W[c][r], sd * z));
+    }
+  }
+  const ScenarioConst &C = P.sc[0];
+  float X = 0.0f, va = C.f[0].v0, vb = C.f[1].v0;
+  TrackerState ts;
+  ts.init(P, PD);
+  const float dt = C.dt;
+  for (int k = 0; k < n; ++k) {
+    const float G = W[0][k + 1] - W[0][k];
+    if (NF == 0) {
+      X += fmaf(C.gbm_vol, G, C.gbm_drift);
+    } else {
+      const FactorConst &f0 = C.f[0];
+      const float Za = W[1][k + 1] - W[1][k];
+      const float ra = sqrt_approx(fmaf(f0.w0, va, f0.w1)) + f0.w2 * Za;
+      const float van = fmaf(f0.w0 * ra, ra, f0.w1);
+      if (NF == 1) {
+        const float root = sqrt_approx(f0.C3 * (va + van));
+        const float drift = fmaf(f0.C2, van, fmaf(f0.C1, va, f0.C0));
+        X += fmaf(root, G, drift);
+        va = van;
+      } else {
+        const FactorConst &f1 = C.f[1];
+        const float Zb = W[NC - 1][k + 1] - W[NC - 1][k];
+        const float rb = sqrt_approx(fmaf(f1.w0, vb, f1.w1)) + f1.w2 * Zb;
+        const float vbn = fmaf(f1.w0 * rb, rb, f1.w1);
+        const float root = sqrt_approx(fmaf(f0.C3, va + van, f1.C3 * (vb + vbn)));
+        const float drift = fmaf(f1.C2, vbn, fmaf(f1.C1, vb, fmaf(f0.C2, van, fmaf(f0.C1, va, f0.C0 + f1.C0))));
+        X += fmaf(root, G, drift);
+        va = van;
+        vb = vbn;
+      }
+    }
+    if (PD) ts.step(P, k, dt, X);
+  }
+  float out[kMaxFields];
+  ts.finish(P, C, X, PD, out);
+  const int F = P.n_fields;
+  for (int f = 0; f < F; ++f) P.records[(size_t)f * P.rec_stride + i] = out[f];
+}
+
+}  // namespace dev
+
+static cudaError_t launch_qmc(const QmcParams &Q, int nf, bool pd, cudaStream_t st) {
+  const unsigned int grid = (unsigned int)((Q.P.path_end + kSimBlock - 1) / kSimBlock);
+  switch (nf * 2 + (pd ? 1 : 0)) {
+    case 0: dev::qmc_kernel<0, false><<<grid, kSimBlock, 0, st>>>(Q); break;
+    case 1: dev::qmc_kernel<0, true><<<grid, kSimBlock, 0, st>>>(Q); break;
+    case 2: dev::qmc_kernel<1, false><<<grid, kSimBlock, 0, st>>>(Q); break;
+    case 3: dev::qmc_kernel<1, true><<<grid, kSimBlock, 0, st>>>(Q); break;
+    case 4: dev::qmc_kernel<2, false><<<grid, kSimBlock, 0, st>>>(Q); break;
+    case 5: dev::qmc_kernel<2, true><<<grid, kSimBlock, 0, st>>>(Q); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------- host
+namespace {
+
+uint64_t splitmix(uint64_t &s) {
+  uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// x^e mod p over GF(2), p of degree s given with its x^s bit
+uint32_t gf2_powmod(uint64_t e, uint32_t p, int s) {
+  auto mulmod = [&](uint32_t a, uint32_t b) {
+    uint32_t r = 0;
+    while (b) {
+      if (b & 1u) r ^= a;
+      b >>= 1;
+      a <<= 1;
+      if (a >> s & 1u) a ^= p;
+    }
+    return r;
+  };
+  uint32_t r = 1, base = s == 1 ? 1u : 2u;  // x mod p (x mod (x + 1) = 1)
+  while (e) {
+    if (e & 1u) r = mulmod(r, base);
+    base = mulmod(base, base);
+    e >>= 1;
+  }
+  return r;
+}
+
+// primitive: x has multiplicative order 2^s - 1 modulo p
+bool primitive(uint32_t p, int s) {
+  const uint64_t order = (1ull << s) - 1;
+  if (gf2_powmod(order, p, s) != 1u) return false;
+  uint64_t m = order;
+  for (uint64_t q = 2; q * q <= m; ++q) {
+    if (m % q) continue;
+    while (m % q == 0) m /= q;
+    if (gf2_powmod(order / q, p, s) == 1u) return false;
+  }
+  if (m > 1 && m != order && gf2_powmod(order / m, p, s) == 1u) return false;
+  return true;
+}
+
+// direction numbers of D dimensions, [D][32]
+std::vector<uint32_t> sobol_directions(unsigned int D, uint64_t seed) {
+  std::vector<uint32_t> V((size_t)D * kQmcBits, 0u);
+  for (int k = 1; k <= kQmcBits; ++k) V[k - 1] = 1u << (kQmcBits - k);  // van der Corput
+  unsigned int d = 1;
+  uint64_t rs = seed ^ 0xD1B54A32D192ED03ull;
+  for (int s = 1; d < D && s <= 20; ++s) {
+    for (uint32_t low = 0; d < D && low < (1u << (s - 1)); ++low) {
+      const uint32_t p = (1u << s) | (low << 1) | 1u;  // x^s + a_1 x^(s-1) + ... + 1
+      if (!primitive(p, s)) continue;
+      std::vector<uint64_t> m(kQmcBits + 1, 0);
+      for (int k = 1; k <= s && k <= kQmcBits; ++k) m[k] = ((splitmix(rs) % (1ull << (k - 1))) << 1) | 1ull;
+      for (int k = s + 1; k <= kQmcBits; ++k) {
+        uint64_t v = m[k - s] ^ (m[k - s] << s);
+        for (int j = 1; j < s; ++j)
+          if (p >> (s - j) & 1u) v ^= m[k - j] << j;  // coefficient a_j of x^(s-j)
+        m[k] = v;
+      }
+      for (int k = 1; k <= kQmcBits; ++k) V[(size_t)d * kQmcBits + k - 1] = (uint32_t)(m[k] << (kQmcBits - k));
+      ++d;
+    }
+  }
+  return V;
+}
+
+struct Bridge {
+  std::vector<int> mid, left, right;
+  std::vector<float> wl, wr, sd;
+};
+
+// Brownian bridge on the unit step grid 0..n, coarse points first (breadth first)
+Bridge brownian_bridge(int n) {
+  Bridge B;
+  B.mid.push_back(n);
+  B.left.push_back(0);
+  B.right.push_back(0);
+  B.wl.push_back(0.0f);
+  B.wr.push_back(0.0f);
+  B.sd.push_back((float)std::sqrt((double)n));
+  std::vector<std::pair<int, int>> q{{0, n}};
+  for (size_t h = 0; h < q.size(); ++h) {
+    const int l = q[h].first, r = q[h].second;
+    if (r - l < 2) continue;
+    const int m = (l + r) / 2;
+    B.mid.push_back(m);
+    B.left.push_back(l);
+    B.right.push_back(r);
+    B.wl.push_back((float)((double)(r - m) / (double)(r - l)));
+    B.wr.push_back((float)((double)(m - l) / (double)(r - l)));
+    B.sd.push_back((float)std::sqrt((double)(m - l) * (double)(r - m) / (double)(r - l)));
+    q.push_back({l, m});
+    q.push_back({m, r});
+  }
+  return B;
+}
+
+struct QmcState : ExtState {
+  DevBuf dirs, shift, bridge;
+  unsigned int dirs_D = 0;
+  uint64_t dirs_seed = 0;
+  int bridge_n = -1;
+};
+
+}  // namespace
+
+extern "C" myql_status myql_qmc_directions(uint32_t D, uint64_t seed, uint32_t *out) {
+  if (!out || D == 0 || D > 1u << 16) return set_error(MYQL_ERR_INVALID_ARG, "need 1 <= D <= 65536 and an output");
+  const std::vector<uint32_t> V = sobol_directions(D, seed);
+  if (V[(size_t)(D - 1) * kQmcBits] == 0u) return set_error(MYQL_ERR_TOO_LARGE, "too many dimensions");
+  std::memcpy(out, V.data(), V.size() * 4);
+  return MYQL_OK;
+}
+
+extern "C" myql_status myql_qmc_price(myql_ctx *ctx_, const myql_mc_job *job, uint32_t n_replicates,
+                                      double *out, myql_mc_stats *stats) {
+  CtxBase *ctx = reinterpret_cast<CtxBase *>(ctx_);
+  if (!ctx || !job || !out) return set_error(MYQL_ERR_INVALID_ARG, "null argument");
+  myql_status s = validate_job(*job);
+  if (s != MYQL_OK) return s;
+  const int nf = job->model.num_factors;
+  for (int f = 0; f < nf; ++f)
+    if (job->config.scheme[f] != MYQL_SCHEME_NV)
+      return set_error(MYQL_ERR_UNSUPPORTED, "quasi-Monte Carlo steps the CIR factors with SchemeNV only");
+  if (job->model.jump != MYQL_JUMP_NONE)
+    return set_error(MYQL_ERR_UNSUPPORTED, "quasi-Monte Carlo supports models without jumps");
+  if (job->config.greek_mode != MYQL_GREEKS_NONE)
+    return set_error(MYQL_ERR_UNSUPPORTED, "quasi-Monte Carlo prices only (GreekMode None)");
+  const uint64_t M = job->config.num_paths, R = n_replicates;
+  if (R < 2 || M % (R * 2048ull) != 0)
+    return set_error(MYQL_ERR_INVALID_ARG, "quasi-Monte Carlo needs >= 2 replicates and num_paths a multiple "
+                                           "of 2048 x replicates");
+  if (M / R > (1ull << 32)) return set_error(MYQL_ERR_TOO_LARGE, "at most 2^32 points per replicate");
+  Plan pl;
+  s = make_plan(*job, pl, true);
+  if (s != MYQL_OK) return s;
+  if (pl.steps > kQmcMaxSteps) return set_error(MYQL_ERR_UNSUPPORTED, "quasi-Monte Carlo takes at most 512 steps");
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return cuda_status(e, "cudaSetDevice");
+  if (!ctx->qmc) ctx->qmc.reset(new QmcState);
+  QmcState &S = *static_cast<QmcState *>(ctx->qmc.get());
+  const unsigned int D = (unsigned int)pl.steps * (unsigned int)(1 + nf);
+  const uint64_t seed = job->config.seed;
+  cudaStream_t st = ctx->stream;
+  ctx->launches = 0;
+  ctx->phase_reset();
+  e = cudaEventRecord(ctx->ev0, st);
+  // tables: direction numbers, shifts, bridge
+  if (S.dirs_D != D || S.dirs_seed != seed) {
+    const std::vector<uint32_t> V = sobol_directions(D, seed);
+    if ((size_t)D * kQmcBits > V.size() || V[(size_t)(D - 1) * kQmcBits] == 0u)
+      return set_error(MYQL_ERR_TOO_LARGE, "too many quasi-Monte Carlo dimensions");
+    e = S.dirs.ensure(V.size() * 4);
+    if (e == cudaSuccess) e = cudaMemcpy(S.dirs.p, V.data(), V.size() * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_status(e, "Sobol directions");
+    S.dirs_D = D;
+    S.dirs_seed = seed;
+  }
+  std::vector<uint32_t> sh((size_t)R * D);
+  uint64_t ss = seed ^ 0x8BB84B93962EACC9ull;
+  for (auto &x : sh) x = (uint32_t)(splitmix(ss) >> 32);
+  e = S.shift.ensure(sh.size() * 4);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(S.shift.p, sh.data(), sh.size() * 4, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // sh is a host temporary
+  if (e != cudaSuccess) return cuda_status(e, "digital shifts");
+  const int n = pl.steps;
+  if (S.bridge_n != n) {
+    const Bridge B = brownian_bridge(n);
+    std::vector<uint8_t> blob((size_t)n * 24);
+    std::memcpy(blob.data(), B.mid.data(), n * 4);
+    std::memcpy(blob.data() + 4 * n, B.left.data(), n * 4);
+    std::memcpy(blob.data() + 8 * n, B.right.data(), n * 4);
+    std::memcpy(blob.data() + 12 * n, B.wl.data(), n * 4);
+    std::memcpy(blob.data() + 16 * n, B.wr.data(), n * 4);
+    std::memcpy(blob.data() + 20 * n, B.sd.data(), n * 4);
+    e = S.bridge.ensure(blob.size());
+    if (e == cudaSuccess) e = cudaMemcpy(S.bridge.p, blob.data(), blob.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_status(e, "Brownian bridge");
+    S.bridge_n = n;
+  }
+  // buffers: records (one scenario), strikes, tile partials
+  const int nk = (int)job->instrument.n_strikes;
+  const uint64_t tiles = M / 2048;
+  e = ctx->records.ensure(M * pl.n_fields * 4);
+  if (e == cudaSuccess) e = ctx->strikes.ensure(nk * sizeof(double));
+  if (e == cudaSuccess) e = ctx->partials.ensure(tiles * (uint64_t)nk * 2 * kQ * sizeof(double));
+  if (e == cudaSuccess) e = ctx->status.ensure(16);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ctx->status.p, 0, 16, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(ctx->strikes.p, job->instrument.strikes, nk * sizeof(double), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_status(e, "quasi-Monte Carlo buffers");
+  QmcParams Q;
+  std::memset(&Q, 0, sizeof Q);
+  Q.P = pl.sim;
+  Q.P.records = (float *)ctx->records.p;
+  Q.P.status = (unsigned int *)ctx->status.p;
+  Q.P.rec_stride = M;
+  Q.P.path_begin = 0;
+  Q.P.path_end = M;
+  Q.P.rec_offset = 0;
+  Q.dirs = (const uint32_t *)S.dirs.p;
+  Q.shift = (const uint32_t *)S.shift.p;
+  const uint8_t *bb = (const uint8_t *)S.bridge.p;
+  Q.br_mid = (const int *)bb;
+  Q.br_left = (const int *)(bb + 4 * n);
+  Q.br_right = (const int *)(bb + 8 * n);
+  Q.br_wl = (const float *)(bb + 12 * n);
+  Q.br_wr = (const float *)(bb + 16 * n);
+  Q.br_sd = (const float *)(bb + 20 * n);
+  Q.n_pts = M / R;
+  Q.D = D;
+  cudaEvent_t sa = ctx->phase_event(), sb = ctx->phase_event();
+  cudaEventRecord(sa, st);
+  e = launch_qmc(Q, nf, pl.path_dep, st);
+  cudaEventRecord(sb, st);
+  ctx->ev_tags.push_back(0);
+  if (e != cudaSuccess) return cuda_status(e, "quasi-Monte Carlo launch");
+  ctx->launches++;
+  PayoffParams PQ = pl.pay;
+  PQ.records = (const float *)ctx->records.p;
+  PQ.rec_stride = M;
+  PQ.partials = (double *)ctx->partials.p;
+  PQ.strikes = (const double *)ctx->strikes.p;
+  PQ.n_paths = M;
+  PQ.tile0 = 0;
+  cudaEvent_t pa = ctx->phase_event(), pb = ctx->phase_event();
+  cudaEventRecord(pa, st);
+  e = launch_payoff(PQ, tiles, st);
+  cudaEventRecord(pb, st);
+  ctx->ev_tags.push_back(1);
+  if (e != cudaSuccess) return cuda_status(e, "payoff launch");
+  ctx->launches++;
+  e = cudaEventRecord(ctx->ev1, st);
+  std::vector<double> part(tiles * (uint64_t)nk * 2 * kQ);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(part.data(), ctx->partials.p, part.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_status(e, "quasi-Monte Carlo run");
+  // replicate estimates (tiles never straddle replicates) -> mean and its standard error
+  const uint64_t tpr = tiles / R;
+  std::memset(out, 0, MYQL_OUT_DOUBLES(nk) * sizeof(double));
+  for (int k = 0; k < nk; ++k) {
+    double sum = 0.0, sum_sq = 0.0;
+    for (uint64_t r = 0; r < R; ++r) {
+      double t = 0.0;
+      for (uint64_t tl = r * tpr; tl < (r + 1) * tpr; ++tl) t += part[(tl * nk + k) * 2 * kQ];
+      const double est = t / (double)Q.n_pts * pl.df;
+      sum += est;
+      sum_sq += est * est;
+    }
+    const double mean = sum / (double)R;
+    const double var = std::max(sum_sq / (double)R - mean * mean, 0.0) * (double)R / (double)(R - 1);
+    out[k] = mean;
+    out[nk + k] = std::sqrt(var / (double)R);
+  }
+  myql_mc_stats local{};
+  myql_mc_stats *stt = stats ? stats : &local;
+  std::memset(stt, 0, sizeof *stt);
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  stt->device_ms = ms;
+  stt->paths = M;
+  stt->scenarios = 1;
+  stt->path_steps = M * (uint64_t)n;
+  stt->kernel_launches = ctx->launches;
+  phase_times(ctx, &stt->simulate_ms, &stt->payoff_ms);
+  return read_status(ctx, stt);
+}
+
+}  // namespace myql

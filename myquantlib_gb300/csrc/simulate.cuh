@@ -129,6 +129,74 @@ __device__ __forceinline__ float jump_draw(const SimParams &P, const ScenarioCon
   return C.jump_comp + total;
 }
 
+// Tracker state of one path (PathTrackers.hpp:8-301): the running sum of an
+// average, the running extremes of log S, and the hit times of the three
+// barriers (base, spot-up, spot-down; < 0 = not hit).
+struct TrackerState {
+  float acc, mn, mx, tb, tu, td;
+  __device__ __forceinline__ void init(const SimParams &P, bool pd) {
+    acc = 0.0f;
+    mn = P.lb_min0;
+    mx = P.lb_max0;
+    tb = tu = td = -1.0f;
+    if (pd && P.tracker >= TRK_BARRIER_UP) {  // Day-0 breach (PathTrackers.hpp:194-215)
+      if (P.tracker == TRK_BARRIER_UP) {
+        if (0.0f >= P.b_log[0]) tb = 0.0f;
+        if (0.0f >= P.b_log[1]) tu = 0.0f;
+        if (0.0f >= P.b_log[2]) td = 0.0f;
+      } else {
+        if (0.0f <= P.b_log[0]) tb = 0.0f;
+        if (0.0f <= P.b_log[1]) tu = 0.0f;
+        if (0.0f <= P.b_log[2]) td = 0.0f;
+      }
+    }
+  }
+  // after step k (0-based) with log-spot X
+  __device__ __forceinline__ void step(const SimParams &P, int k, float dt, float X) {
+    const float t = (float)(k + 1) * dt;
+    switch (P.tracker) {
+      case TRK_GEO_ASIAN: acc += X; break;
+      case TRK_ARITH_ASIAN: acc += __expf(X); break;
+      case TRK_LOOKBACK:
+        mn = fminf(mn, X);
+        mx = fmaxf(mx, X);
+        break;
+      case TRK_BARRIER_UP:
+        if (tu < 0.0f && X >= P.b_log[1]) tu = t;
+        if (tb < 0.0f && X >= P.b_log[0]) tb = t;
+        if (td < 0.0f && X >= P.b_log[2]) td = t;
+        break;
+      case TRK_BARRIER_DOWN:
+        if (td < 0.0f && X <= P.b_log[2]) td = t;
+        if (tb < 0.0f && X <= P.b_log[0]) tb = t;
+        if (tu < 0.0f && X <= P.b_log[1]) tu = t;
+        break;
+      default: break;
+    }
+  }
+  // the terminal record: X, then the tracker's fields
+  __device__ __forceinline__ void finish(const SimParams &P, const ScenarioConst &C, float X, bool pd,
+                                         float (&out)[kMaxFields]) const {
+    out[0] = X;
+    if (!pd) return;
+    switch (P.tracker) {
+      case TRK_GEO_ASIAN: out[1] = C.dt * (acc - 0.5f * X); break;
+      case TRK_ARITH_ASIAN: out[1] = C.dt * (0.5f + acc - 0.5f * __expf(X)); break;
+      case TRK_LOOKBACK:
+        out[1] = mn;
+        out[2] = mx;
+        break;
+      case TRK_BARRIER_UP:
+      case TRK_BARRIER_DOWN:
+        out[1] = tb;
+        out[2] = tu;
+        out[3] = td;
+        break;
+      default: break;
+    }
+  }
+};
+
 // Observer of a path's steps (the control-variate kernels record hedge-time
 // states and martingale increments through it).  NoHook compiles away.
 struct NoHook {
@@ -151,20 +219,8 @@ __device__ __forceinline__ void sim_path_h(const SimParams &P, const ScenarioCon
                                            unsigned int &fallbacks, Hook &hook) {
   float X = 0.0f;
   float va = C.f[0].v0, vb = C.f[1].v0;
-  const int trk = P.tracker;
-  float acc = 0.0f, mn = P.lb_min0, mx = P.lb_max0;
-  float tb = -1.0f, tu = -1.0f, td = -1.0f;
-  if (PD && trk >= TRK_BARRIER_UP) {  // Day-0 breach (PathTrackers.hpp:194-215)
-    if (trk == TRK_BARRIER_UP) {
-      if (0.0f >= P.b_log[0]) tb = 0.0f;
-      if (0.0f >= P.b_log[1]) tu = 0.0f;
-      if (0.0f >= P.b_log[2]) td = 0.0f;
-    } else {
-      if (0.0f <= P.b_log[0]) tb = 0.0f;
-      if (0.0f <= P.b_log[1]) tu = 0.0f;
-      if (0.0f <= P.b_log[2]) td = 0.0f;
-    }
-  }
+  TrackerState ts;
+  ts.init(P, PD);
   const int n = P.n_steps;
   if (Hook::active) hook.begin(va, vb);
   if (NF == 0 && !PD && !Hook::active) {
@@ -206,28 +262,9 @@ __device__ __forceinline__ void sim_path_h(const SimParams &P, const ScenarioCon
           X += J;
           if (Hook::active) hook.jump(J);
         }
-        const float t = (float)(k + 1) * dt;
-        switch (trk) {
-          case TRK_GEO_ASIAN: acc += X; break;
-          case TRK_ARITH_ASIAN: acc += __expf(X); break;
-          case TRK_LOOKBACK:
-            mn = fminf(mn, X);
-            mx = fmaxf(mx, X);
-            break;
-          case TRK_BARRIER_UP:
-            if (tu < 0.0f && X >= P.b_log[1]) tu = t;
-            if (tb < 0.0f && X >= P.b_log[0]) tb = t;
-            if (td < 0.0f && X >= P.b_log[2]) td = t;
-            break;
-          case TRK_BARRIER_DOWN:
-            if (td < 0.0f && X <= P.b_log[2]) td = t;
-            if (tb < 0.0f && X <= P.b_log[0]) tb = t;
-            if (tu < 0.0f && X <= P.b_log[1]) tu = t;
-            break;
-          default: break;
-        }
+        ts.step(P, k, dt, X);
       }
-      if (Hook::active) hook.step_end(k + 1, X, va, vb, acc, tb >= 0.0f);
+      if (Hook::active) hook.step_end(k + 1, X, va, vb, ts.acc, ts.tb >= 0.0f);
     }
     if (!PD && (NF > 0 || Hook::active) && P.jump_kind) {
       const float J = jump_draw(P, C, rng, caphits);
@@ -236,24 +273,7 @@ __device__ __forceinline__ void sim_path_h(const SimParams &P, const ScenarioCon
     }
   }
   if (Hook::active) hook.finish();
-  out[0] = X;
-  if (PD) {
-    switch (trk) {
-      case TRK_GEO_ASIAN: out[1] = C.dt * (acc - 0.5f * X); break;
-      case TRK_ARITH_ASIAN: out[1] = C.dt * (0.5f + acc - 0.5f * __expf(X)); break;
-      case TRK_LOOKBACK:
-        out[1] = mn;
-        out[2] = mx;
-        break;
-      case TRK_BARRIER_UP:
-      case TRK_BARRIER_DOWN:
-        out[1] = tb;
-        out[2] = tu;
-        out[3] = td;
-        break;
-      default: break;
-    }
-  }
+  ts.finish(P, C, X, PD, out);
 }
 
 template <int NF, int S1, int S2, bool PD>

@@ -500,6 +500,13 @@ class Engine:
         _abi.check(self.lib.myql_mlmc_price(self.handle, C.byref(job.c), C.byref(mlmc_cfg), C.byref(res)))
         return res
 
+    def qmc_price(self, job: "_Job", n_replicates: int = 16):
+        """Randomized quasi-Monte Carlo price rows (myql_qmc_price) and the run statistics."""
+        out = np.zeros(2 * _abi.Q_COUNT * job.n_strikes, dtype=np.float64)
+        st = _abi.McStatsC()
+        _abi.check(self.lib.myql_qmc_price(self.handle, C.byref(job.c), n_replicates, _ptr(out), C.byref(st)))
+        return out.reshape(2 * _abi.Q_COUNT, job.n_strikes), st
+
     def ml2r_price(self, job: "_Job", mlmc_cfg: "_abi.MlmcConfigC") -> "_abi.MlmcResultC":
         """Multilevel Richardson-Romberg extrapolation on the MLMC levels (myql_ml2r_price)."""
         res = _abi.MlmcResultC()

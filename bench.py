@@ -464,6 +464,34 @@ def time_to_se(eng, m, kind: str, probe_paths: int = 1 << 22) -> dict:
             "price_cv": res.price, "price_plain": float(raw[0, 0])}
 
 
+def qmc_time_to_se(eng, m, target: float = 1e-4, R: int = 16, probe_paths: int = 1 << 20) -> dict:
+    """The Heston European call of the control-variate comparison (SchemeNV, 100 steps) priced
+    by randomized quasi-Monte Carlo (Sobol + Brownian bridge, R digital shifts): wall time
+    to the relative standard error target against plain GPU Monte Carlo.  The probe fixes
+    the QMC error at one size; the timed run takes the path count (rounded up to whole
+    2048 x R blocks) that the plain 1/sqrt(n) rate gives for the target, an upper bound
+    since the QMC error falls faster."""
+    import torch
+    unit = 2048 * R
+    job, steps = cv_jobs(m, "european", probe_paths)
+    q, _ = eng.qmc_price(job, R)
+    n_q = max(unit, -(-int(probe_paths * (q[1, 0] / (target * q[0, 0])) ** 2) // unit) * unit)
+    pj, _ = cv_jobs(m, "european", 1 << 22)
+    raw, _ = eng.price(pj)
+    n_plain = int((1 << 22) * (raw[1, 0] / (target * raw[0, 0])) ** 2) + 1
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    q, _ = eng.qmc_price(cv_jobs(m, "european", n_q, seed=48)[0], R)
+    t_q = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    raw, _ = eng.price(cv_jobs(m, "european", n_plain, seed=49)[0])
+    t_plain = time.perf_counter() - t0
+    return {"instrument": "Heston European call (SchemeNV, 100 steps)", "target_rel_se": target, "replicates": R,
+            "qmc_paths": n_q, "qmc_s": t_q, "qmc_rel_se": q[1, 0] / q[0, 0], "plain_paths": n_plain,
+            "plain_s": t_plain, "plain_rel_se": raw[1, 0] / raw[0, 0], "speedup": t_plain / t_q,
+            "price_qmc": q[0, 0], "price_plain": raw[0, 0]}
+
+
 def run_cv(args) -> dict:
     """Headline metric part 1: time-to-relative-SE of the neural control variate against
     plain GPU Monte Carlo (seconds, lower is better), for the Asian (target 1e-3) and the
@@ -479,6 +507,8 @@ def run_cv(args) -> dict:
         res = {kind: time_to_se(eng, m, kind) for kind in ("asian", "european")}
         CV_TARGETS["asian_1e-4"] = 1e-4
         res["asian_1e-4"] = time_to_se(eng, m, "asian_1e-4")
+        eng.qmc_price(cv_jobs(m, "european", 1 << 19)[0], 16)  # warm-up
+        res["european_qmc"] = qmc_time_to_se(eng, m)
     a = res["asian"]
     return {"metric": "time-to-relative-SE (s) neural-CV vs plain MC", "value": a["cv_s"], "unit": "s",
             "n_gpus": 1, "steps": 1, "warmup": 1, "ms_per_step": a["cv_s"] * 1e3, "higher_is_better": False,

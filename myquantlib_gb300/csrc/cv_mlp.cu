@@ -696,12 +696,15 @@ __global__ void __launch_bounds__(256) cv_beta_kernel(const float *Y, const floa
     if (threadIdx.x == 0) part[blockIdx.x * 5 + q] = t;
   }
 }
-// sums[q] += sum over blocks b (in order) of part[b][q]
+// sums[q] += sum over blocks b of part[b][q]: warp q, lane l sums b = l, l + 32, ...
+// in order, then a fixed shuffle tree (deterministic)
 __global__ void cv_fold_kernel(const double *part, unsigned int nb, unsigned int nq, double *sums) {
-  if (threadIdx.x >= nq) return;
+  const unsigned int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (q >= nq) return;
   double t = 0.0;
-  for (unsigned int b = 0; b < nb; ++b) t += part[(size_t)b * nq + threadIdx.x];
-  sums[threadIdx.x] += t;
+  for (unsigned int b = lane; b < nb; b += 32) t += part[(size_t)b * nq + q];
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if (lane == 0) sums[q] += t;
 }
 
 }  // namespace dev
@@ -709,7 +712,7 @@ __global__ void cv_fold_kernel(const double *part, unsigned int nb, unsigned int
 cudaError_t launch_cv_beta(const float *Y, const float *dM, unsigned long long n, unsigned int n_hedge,
                            double *sums5, double *part, cudaStream_t st) {
   dev::cv_beta_kernel<<<kFoldBlocks, 256, 0, st>>>(Y, dM, n, n_hedge, part);
-  dev::cv_fold_kernel<<<1, 32, 0, st>>>(part, kFoldBlocks, 5, sums5);
+  dev::cv_fold_kernel<<<1, 32 * 5, 0, st>>>(part, kFoldBlocks, 5, sums5);
   return cudaGetLastError();
 }
 
@@ -784,7 +787,7 @@ cudaError_t launch_cv_rowsum(const float *gdm, unsigned long long n_paths, unsig
 cudaError_t launch_cv_reduce(const float *Y, const float *cv, unsigned long long n, double *sums4, double *part,
                              cudaStream_t st) {
   dev::cv_reduce_kernel<<<kFoldBlocks, 256, 0, st>>>(Y, cv, n, part);
-  dev::cv_fold_kernel<<<1, 32, 0, st>>>(part, kFoldBlocks, 4, sums4);
+  dev::cv_fold_kernel<<<1, 32 * 4, 0, st>>>(part, kFoldBlocks, 4, sums4);
   return cudaGetLastError();
 }
 

@@ -12,3 +12,4 @@ from .pricers import (  # noqa: F401
 from . import _abi  # noqa: F401
 from . import dispatch  # noqa: F401
 from . import registry  # noqa: F401
+from . import calibration  # noqa: F401

@@ -468,14 +468,17 @@ def qmc_time_to_se(eng, m, target: float = 1e-4, R: int = 16, probe_paths: int =
     """The Heston European call of the control-variate comparison (SchemeNV, 100 steps) priced
     by randomized quasi-Monte Carlo (Sobol + Brownian bridge, R digital shifts): wall time
     to the relative standard error target against plain GPU Monte Carlo.  The probe fixes
-    the QMC error at one size; the timed run takes the path count (rounded up to whole
-    2048 x R blocks) that the plain 1/sqrt(n) rate gives for the target, an upper bound
-    since the QMC error falls faster."""
+    the QMC error at one size; the timed run takes the path count that the plain 1/sqrt(n)
+    rate gives for the target (an upper bound, since the QMC error falls faster), rounded up
+    to a power of two per replicate."""
     import torch
-    unit = 2048 * R
     job, steps = cv_jobs(m, "european", probe_paths)
     q, _ = eng.qmc_price(job, R)
-    n_q = max(unit, -(-int(probe_paths * (q[1, 0] / (target * q[0, 0])) ** 2) // unit) * unit)
+    need = probe_paths * (q[1, 0] / (target * q[0, 0])) ** 2
+    pts = 2048
+    while pts * R < need:  # a power of two per replicate: the balanced Sobol point sets
+        pts *= 2
+    n_q = pts * R
     pj, _ = cv_jobs(m, "european", 1 << 22)
     raw, _ = eng.price(pj)
     n_plain = int((1 << 22) * (raw[1, 0] / (target * raw[0, 0])) ** 2) + 1

@@ -524,8 +524,9 @@ def run_cv(args) -> dict:
 def run_mlmc(args) -> dict:
     """MLMC down-and-out put (Heston kappa 2, theta .04, sigma .5, rho -.7, v0 .04, SchemeNV,
     K 100, B 80, T 1; levels 2..10, dt = T / 2^l; target RMSE 1e-3 x price): plain MLMC
-    against MLMC with the neural control variate on every level (training included), both
-    through the public API, wall-clock."""
+    against MLMC with the neural control variate (training included; each level keeps the
+    control only where its variance ratio pays for the MLP rows), both through the public
+    API, wall-clock, and at equal standard error (time x SE^2)."""
     import myquantlib_gb300 as m
     from myquantlib_gb300 import _abi
     if int(os.environ.get("RANK", "0")) != 0:
@@ -572,7 +573,11 @@ def run_mlmc(args) -> dict:
                    "variance_ratio_per_level": [float(plain_var[l] / max(res_cv.var_diffs[l], 1e-300))
                                                 for l in range(nl)],
                    "path_steps": int(res_cv.total_steps)},
-            "speedup": t_plain / t_cv, "clocks": clk.summary()}
+            "speedup": t_plain / t_cv,
+            # cost at equal standard error (the two controllers stop at different SEs):
+            "efficiency_ratio": (t_plain * res_plain.price_std_err ** 2) / (t_cv * res_cv.price_std_err ** 2),
+            "cv_levels": [l for l in range(nl) if abs(plain_var[l] / max(res_cv.var_diffs[l], 1e-300) - 1.0) > 1e-9],
+            "clocks": clk.summary()}
 
 
 def run_ncu_cv_case() -> None:

@@ -234,6 +234,21 @@ static myql_status mlmc_run(myql_ctx *ctx_, const myql_mc_job *job_in, const myq
   std::vector<uint64_t> plain_n(L_max + 1, 0);
   cudaEventRecord(ctx->ev0, ctx->stream);
   uint32_t launches = 0;
+  // With the control variate, a level keeps it only where it pays: after the level's first
+  // (pilot) batch, both unbiased estimators' variances are known, and the CV stays if
+  // Var(Y) > kappa_l Var(Y - C), kappa_l the cost of a CV path in plain coupled paths
+  // (an MLP row costs about 25 coupled path-steps on this engine).  Otherwise the level's
+  // statistics switch to the plain estimator of the same samples and its later batches run
+  // the plain level kernel.
+  std::vector<char> use_cv(L_max + 1, cv ? 1 : 0), decided(L_max + 1, 0);
+  std::vector<double> cost_l(L_max + 1, 0.0);  // path cost of each level, in steps
+  for (size_t l = 0; l <= L_max; ++l) cost_l[l] = (double)(cfg->base_steps * (1ull << l));
+  auto cv_kappa = [&](size_t l) {
+    const int n = l == 0 ? (int)cfg->base_steps : (int)((cfg->base_steps << l) / 2);
+    const int he = std::max(1, n / 32), nh = (n + he - 1) / he;
+    const double coupled_steps = l == 0 ? (double)cfg->base_steps : 1.5 * (double)(cfg->base_steps << l);
+    return 1.0 + 25.0 * (double)nh / coupled_steps;
+  };
   auto evaluate_level = [&](size_t l, uint64_t dN, double &sum, double &sum_sq) -> myql_status {
     const uint64_t fine = cfg->base_steps << l;
     if (l == 0) {
@@ -259,7 +274,7 @@ static myql_status mlmc_run(myql_ctx *ctx_, const myql_mc_job *job_in, const myq
     M.level = (int)l;
     M.dN = dN;
     M.n_used = (unsigned int)std::min<uint64_t>(S, dN);
-    if (cv) {
+    if (cv && (use_cv[l] || (probe_sums && probe_level >= 0))) {
       MlmcCvParams Q;
       std::memset(&Q, 0, sizeof Q);
       Q.M = M;
@@ -281,10 +296,21 @@ static myql_status mlmc_run(myql_ctx *ctx_, const myql_mc_job *job_in, const myq
       }
       sum += s4[2] / df;
       sum_sq += s4[3] / (df * df);
-      if (plain_var) {
-        plain_sums[l][0] += s4[0] / df;
-        plain_sums[l][1] += s4[1] / (df * df);
-        plain_n[l] += dN;
+      plain_sums[l][0] += s4[0] / df;
+      plain_sums[l][1] += s4[1] / (df * df);
+      plain_n[l] += dN;
+      if (!decided[l] && plain_n[l] > 1) {
+        decided[l] = 1;
+        const double n = (double)plain_n[l];
+        const double mp = plain_sums[l][0] / n, mc = sum / n;
+        const double vp = plain_sums[l][1] / n - mp * mp, vc = sum_sq / n - mc * mc;
+        if (!(vp > cv_kappa(l) * vc)) {
+          use_cv[l] = 0;  // the plain estimator of the same samples
+          sum = plain_sums[l][0];
+          sum_sq = plain_sums[l][1];
+        } else {
+          cost_l[l] *= cv_kappa(l);
+        }
       }
       return MYQL_OK;
     }
@@ -303,6 +329,11 @@ static myql_status mlmc_run(myql_ctx *ctx_, const myql_mc_job *job_in, const myq
     }
     sum += a;
     sum_sq += b;
+    if (cv) {  // a level that dropped the control variate: its plain statistics
+      plain_sums[l][0] += a;
+      plain_sums[l][1] += b;
+      plain_n[l] += dN;
+    }
     return MYQL_OK;
   };
 
@@ -316,9 +347,7 @@ static myql_status mlmc_run(myql_ctx *ctx_, const myql_mc_job *job_in, const myq
   // ---- Giles' adaptive controller (MultiLevelMonteCarloPricer.hpp:64-211)
   size_t L = ml2r ? std::max<uint64_t>(cfg->L_min, 1) : cfg->L_min;
   std::vector<uint64_t> N_l(L_max + 1, 0);
-  std::vector<double> sum_dP(L_max + 1, 0.0), sum_sq_dP(L_max + 1, 0.0), V_l(L_max + 1, 0.0),
-      cost_l(L_max + 1, 0.0);
-  for (size_t l = 0; l <= L_max; ++l) cost_l[l] = (double)(cfg->base_steps * (1ull << l));
+  std::vector<double> sum_dP(L_max + 1, 0.0), sum_sq_dP(L_max + 1, 0.0), V_l(L_max + 1, 0.0);
   double alpha = cfg->alpha, beta = cfg->beta;
   const double eps_m2 = std::pow(cfg->epsilon, -2.0);
   bool converged = false;

@@ -178,8 +178,13 @@ def test_mlmc_cv_levels_unbiased_and_reduced(engine, name):
         assert min(ratios) > 0.9, ratios
 
 
-@pytest.mark.parametrize("name,eps,gain", [("c5_do_put", 0.01, False), ("heston_eur", 0.01, True)])
-def test_mlmc_cv_price_against_plain_mlmc(engine, oracle_lib, name, eps, gain):
+@pytest.mark.parametrize("name,eps", [("c5_do_put", 0.01), ("heston_eur", 0.01)])
+def test_mlmc_cv_price_against_plain_mlmc(engine, oracle_lib, name, eps):
+    """MLMC with the control variate agrees with plain MLMC and the reference's estimator.
+    A level keeps the control only where its variance ratio beats the cost of the MLP rows
+    (about 25 coupled path-steps a row): on the one-step and few-step low levels a CV path
+    costs 9 to 26 plain ones, so there the level runs the plain estimator and its variance
+    is the plain one."""
     j = CASES[name]()
     cfg = mlmc_cfg(eps, L_max=8)
     plain = run_mlmc(engine, j, cfg)
@@ -189,7 +194,5 @@ def test_mlmc_cv_price_against_plain_mlmc(engine, oracle_lib, name, eps, gain):
     r = oracle_lib.mlmc_price(j, cfg, oracle_lib.LAYOUT_REFERENCE, 8)
     assert abs(res.price - r.price) < 4 * np.hypot(res.price_std_err, r.price_std_err) + cfg.epsilon
     v_cv = np.array([res.var_diffs[l] for l in range(res.n_levels)])
-    if gain:
-        assert v_cv[0] < plain_var[0] / 3.0, (v_cv[0], plain_var[0])
-        # fewer level-0 paths for the same target accuracy
-        assert res.paths_per_level[0] < plain.paths_per_level[0]
+    for level in range(3):
+        assert abs(v_cv[level] - plain_var[level]) <= 1e-9 * plain_var[level] + 1e-18, (level, v_cv, plain_var)

@@ -219,8 +219,8 @@ myql_status simulate_chunks(CtxBase *ctx, CvSimParams C, int klass, uint64_t see
 }
 
 // persistent grids: one block per SM
-unsigned int mlp_blocks(const CtxBase *ctx, uint64_t n_pb, int per_sm = 1) {
-  return (unsigned int)std::max<uint64_t>(1, std::min<uint64_t>(n_pb, (uint64_t)ctx->sm_count * per_sm));
+unsigned int mlp_blocks(const CtxBase *ctx, uint64_t n_units) {
+  return (unsigned int)std::max<uint64_t>(1, std::min<uint64_t>(n_units, (uint64_t)ctx->sm_count));
 }
 
 myql_status forward(CtxBase *ctx, CvState &S, const uint8_t *feat, const float *dM, uint64_t n_paths, uint32_t nh,

@@ -657,9 +657,9 @@ __global__ void cv_rowsum_kernel(const float *gdm, unsigned long long n, unsigne
   cv[p] = s;
 }
 
-// sums4 += {sum Y, sum Y^2, sum (Y - C), sum (Y - C)^2} (FP64, per-block partials + atomics)
-// Per-block partial sums (fixed grid, warps summed in order), folded into the
-// running sums by cv_fold_kernel in block order: deterministic.
+// sums4 += {sum Y, sum Y^2, sum (Y - C), sum (Y - C)^2} and the hedge-ratio sums: per-block
+// FP64 partials (fixed grid, warps summed in order), folded into the running sums by
+// cv_fold_kernel in a fixed order: deterministic.
 __global__ void __launch_bounds__(256) cv_reduce_kernel(const float *Y, const float *cv, unsigned long long n,
                                                         double *part) {
   double a[4] = {0.0, 0.0, 0.0, 0.0};

@@ -344,6 +344,14 @@ myql_status myql_rng_draws(myql_ctx *ctx, uint64_t seed, uint64_t first,
  * SchemeNCI tables (VolSchemes.hpp:240-313). */
 myql_status myql_chi2_quantile(myql_ctx *ctx, const double *dof, const double *p,
                                double *out, size_t n);
+/* The FP64 nodes of the SchemeNCI table of degrees-of-freedom offset d, rows
+ * 0..rows-1 (row k: chi-squared with d + 2k degrees of freedom), as the table
+ * build computes them before fitting the Hermite cells
+ * (VolSchemes.hpp:240-313).  main_out: rows * 10000 quantiles at p = i * 0.999
+ * / 9999; tail_out: rows * 512 upper-tail quantiles at q = exp(-w_j), w_j =
+ * w0 + j (44.5 - w0) / 511, w0 = -log(0.001).  1 <= rows <= 1024. */
+myql_status myql_probe_nci_nodes(myql_ctx *ctx, double d, int rows, double *main_out,
+                                 double *tail_out);
 /* FP32 device samplers on given 64-bit draws: kind 0 = inverse normal of the
  * uniform of x, kind 1 = inverse Poisson CDF with mean lambda[i] of the uniform
  * of x.  out: n floats. */

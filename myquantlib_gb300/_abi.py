@@ -137,6 +137,8 @@ _SIGS = {
                                  C.POINTER(C.c_uint64)]),
     "myql_chi2_quantile": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                      C.POINTER(C.c_double), C.c_size_t]),
+    "myql_probe_nci_nodes": (C.c_int, [C.c_void_p, C.c_double, C.c_int, C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double)]),
     "myql_probe_sampler": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_uint64),
                                      C.POINTER(C.c_double), C.POINTER(C.c_float), C.c_size_t]),
     "myql_probe_peak": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),

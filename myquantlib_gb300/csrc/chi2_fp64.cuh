@@ -7,7 +7,9 @@
 // (x >= a + 1); the quantile is a safeguarded Newton iteration on
 // log P(a, x) (lower tail) or log Q(a, x) (upper tail) in u = log x, started
 // from the Wilson-Hilferty cube or, for small P and shape below 1, from the
-// leading power term x^a / Gamma(a + 1).  chi2_nu^-1(p) = 2 * x with a = nu / 2.
+// leading power term x^a / Gamma(a + 1) -- or, along a table row, from the
+// Taylor step of the quantile function from the previous node.
+// chi2_nu^-1(p) = 2 * x with a = nu / 2.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -62,53 +64,57 @@ __device__ inline GammaEval gamma_eval(double a, double x, double lga) {
   return g;
 }
 
+// Starting point u = log x (x = y / 2, the gamma variable of shape a) of the
+// Newton iteration for the quantile at tail probability p (lp = log p).
+__device__ inline double chi2_start(double a, double p, double lp, bool upper) {
+  const double z = upper ? -normcdfinv(p) : normcdfinv(p);
+  const double h = 1.0 / (9.0 * a);
+  const double cwh = 1.0 - h + z * sqrt(h);
+  const double u_small = (lp + lgamma(a + 1.0)) / a;  // log of (p Gamma(a+1))^(1/a)
+  if (cwh > 0.0) {
+    const double u = log(a) + 3.0 * log(cwh);
+    return (!upper && a < 1.0 && u_small < u) ? u_small : u;
+  }
+  return upper ? log(a + 1.0) : u_small;
+}
+
+// Safeguarded Newton iteration on G(u) = log P(a, e^u) - lp (lower tail) or
+// lp - log Q(a, e^u) (upper tail), both increasing in u, from u.  A step
+// shorter than max(accept, 1e-14 max(1, |u|)) is taken and ends the iteration
+// before the bracket test (a step that rounds to zero must not be mistaken for
+// one that leaves the bracket).  The error left after a Newton step s is about
+// |G''/(2 G')| s^2, and |G''/G'| stays below about sqrt(a) + 1 over the tables'
+// range, so accept = 1e-8 leaves about 1e-15 relative in x.
+__device__ inline double chi2_newton(double a, double lga, double lp, bool upper, double u,
+                                     double accept) {
+  double lo = -INFINITY, hi = INFINITY;
+  for (int it = 0; it < 200; ++it) {
+    const double x = exp(u);
+    if (x <= 0.0) return -700.0;
+    const GammaEval g = gamma_eval(a, x, lga);
+    const double G = upper ? lp - g.logQ : g.logP - lp;
+    const double step = G / (upper ? g.xpdf_Q : g.xpdf_P);
+    if (fabs(step) < fmax(accept, 1e-14 * fmax(1.0, fabs(u)))) return u - step;
+    if (G < 0.0) lo = u; else hi = u;
+    double un = u - step;
+    if (!(un > lo && un < hi)) {
+      if (isinf(lo)) un = u - 2.0;
+      else if (isinf(hi)) un = u + 2.0;
+      else un = 0.5 * (lo + hi);
+    }
+    u = un;
+  }
+  return u;
+}
+
 // Quantile of chi-squared with nu degrees of freedom at lower-tail probability p
 // (upper = false) or upper-tail probability p (upper = true).
 __device__ inline double chi2_quantile(double nu, double p, bool upper) {
   if (p <= 0.0) return upper ? INFINITY : 0.0;
   if (p >= 1.0) return upper ? 0.0 : INFINITY;
   const double a = 0.5 * nu;
-  const double lga = lgamma(a);
   const double lp = log(p);
-  // initial guess
-  const double z = upper ? -normcdfinv(p) : normcdfinv(p);
-  const double h = 1.0 / (9.0 * a);
-  const double cwh = 1.0 - h + z * sqrt(h);
-  double u;
-  const double u_small = (lp + lgamma(a + 1.0)) / a;  // log of (p Gamma(a+1))^(1/a)
-  if (cwh > 0.0) {
-    u = log(a) + 3.0 * log(cwh);
-    if (!upper && a < 1.0 && u_small < u) u = u_small;
-  } else {
-    u = upper ? log(a + 1.0) : u_small;
-  }
-  double lo = -INFINITY, hi = INFINITY;
-  for (int it = 0; it < 200; ++it) {
-    const double x = exp(u);
-    if (x <= 0.0) { u = -700.0; break; }
-    const GammaEval g = gamma_eval(a, x, lga);
-    double G, dG;  // G increasing in u
-    if (!upper) {
-      G = g.logP - lp;
-      dG = g.xpdf_P;
-    } else {
-      G = lp - g.logQ;
-      dG = g.xpdf_Q;
-    }
-    if (G < 0.0) lo = u; else hi = u;
-    double un = u - G / dG;
-    if (!(un > lo && un < hi)) {
-      if (isinf(lo)) un = u - 2.0;
-      else if (isinf(hi)) un = u + 2.0;
-      else un = 0.5 * (lo + hi);
-    }
-    if (fabs(un - u) < 1e-14 * fmax(1.0, fabs(u))) {
-      u = un;
-      break;
-    }
-    u = un;
-  }
-  return 2.0 * exp(u);
+  return 2.0 * exp(chi2_newton(a, lgamma(a), lp, upper, chi2_start(a, p, lp, upper), 0.0));
 }
 
 // chi-squared density (for the exact tail slopes)

@@ -30,6 +30,8 @@ cudaError_t launch_rng_draws(const unsigned long long *states, unsigned long lon
 cudaError_t launch_nci_build(double d, int rows, double *tmp_main, double *tmp_ty, double *tmp_tm,
                              float4 *cells_main, float4 *cells_tail, double w0, double dw,
                              cudaStream_t stream);
+cudaError_t launch_nci_nodes(double d, int rows, double *tmp_main, double *tmp_ty, double *tmp_tm,
+                             double w0, double dw, cudaStream_t stream);
 cudaError_t launch_chi2_probe(const double *dof, const double *p, double *out, size_t n,
                               cudaStream_t stream);
 cudaError_t run_peak_probe(int kind, int sm_count, cudaStream_t stream, double *ops_per_s);
@@ -551,8 +553,7 @@ myql_status ensure_nci(CtxBase *ctx, const myql_heston_params &p, double dt_min,
     }
     double *tm = (double *)tmp.p;
     const double w0 = -std::log1p(-kNciUmax);
-    const double w1 = 44.5;
-    const double dw = (w1 - w0) / (kNciTail - 1);
+    const double dw = (kNciTailWmax - w0) / (kNciTail - 1);
     e = launch_nci_build(d, rows, tm, tm + nm, tm + nm + nt, (float4 *)ent.main.p,
                          (float4 *)ent.tail.p, w0, dw, ctx->stream);
     ctx->launches += 4;
@@ -571,7 +572,7 @@ myql_status ensure_nci(CtxBase *ctx, const myql_heston_params &p, double dt_min,
   tab.rows = ent.rows;
   tab.d = (float)d;
   const double w0 = -std::log1p(-kNciUmax);
-  const double dw = (44.5 - w0) / (kNciTail - 1);
+  const double dw = (kNciTailWmax - w0) / (kNciTail - 1);
   tab.tail_w0 = (float)w0;
   tab.tail_inv_dw = (float)(1.0 / dw);
   const double inv_dx = (kNciGrid - 1) / kNciUmax;
@@ -912,6 +913,26 @@ myql_status myql_chi2_quantile(myql_ctx *ctx, const double *dof, const double *p
   if (e == cudaSuccess) e = cudaMemcpyAsync(out, ctx->probe_c.p, n * 8, cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   return cuda_status(e, "chi2 probe");
+}
+
+myql_status myql_probe_nci_nodes(myql_ctx *ctx, double d, int rows, double *main_out,
+                                 double *tail_out) {
+  myql_status s = ctx_check(ctx);
+  if (s != MYQL_OK) return s;
+  if (!main_out || !tail_out || rows < 1 || rows > 1024 || !(d > 0.0) || !std::isfinite(d))
+    return set_error(MYQL_ERR_INVALID_ARG, "bad probe arguments");
+  const size_t nm = (size_t)rows * kNciGrid, nt = (size_t)rows * kNciTail;
+  cudaError_t e = ctx->probe_a.ensure((nm + 2 * nt) * sizeof(double));
+  double *tm = (double *)ctx->probe_a.p;
+  const double w0 = -std::log1p(-kNciUmax);
+  const double dw = (kNciTailWmax - w0) / (kNciTail - 1);
+  if (e == cudaSuccess) e = launch_nci_nodes(d, rows, tm, tm + nm, tm + nm + nt, w0, dw, ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(main_out, tm, nm * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(tail_out, tm + nm, nt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  return cuda_status(e, "NCI node probe");
 }
 
 myql_status myql_probe_sampler(myql_ctx *ctx, int kind, const uint64_t *x, const double *lambda,

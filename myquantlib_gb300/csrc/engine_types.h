@@ -60,6 +60,7 @@ struct NciTable {
 constexpr int kNciGrid = 10000;  // VolSchemes.hpp:257
 constexpr int kNciTail = 512;
 constexpr double kNciUmax = 0.999;  // VolSchemes.hpp:258,342
+constexpr double kNciTailWmax = 44.5;  // tail grid w = -log(1 - U) in [-log(1 - kNciUmax), 44.5]
 
 struct ScenarioConst {
   FactorConst f[2];

@@ -104,28 +104,87 @@ __global__ void rng_draws_kernel(const unsigned long long *states, unsigned long
 }
 
 // ---- SchemeNCI table build (FP64) -----------------------------------------
+// A thread fills a run of consecutive nodes of one row.  The first node of a
+// run starts Newton from chi2_start; each later node starts from the Taylor
+// step of the quantile function u(p) = log(y(p) / 2) from the previous node:
+// with g = du/dp = 1 / (x f(x)) (f the gamma(a) density, x = e^u) and
+// s = a - x, d2u/dp2 = -s g^2 and d3u/dp3 = (x + 2 s^2) g^3.  The step is used
+// while g dx (1 + |s|) < 0.2, where its error is far below the Newton
+// acceptance step, so most nodes take one evaluation of the incomplete gamma.
+constexpr int kNciRunMain = 16;
+constexpr int kNciRunTail = 4;
+constexpr int kNciRunsMain = (kNciGrid + kNciRunMain - 1) / kNciRunMain;
+constexpr int kNciRunsTail = (kNciTail + kNciRunTail - 1) / kNciRunTail;
+constexpr double kNciAccept = 1e-8;
+constexpr double kNciStepGate = 0.2;
+
 __global__ void nci_nodes_main_kernel(double d, int rows, double dx, double *y) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (long long)rows * kNciGrid) return;
-  const int k = (int)(idx / kNciGrid), i = (int)(idx % kNciGrid);
-  const double nu = d + 2.0 * k;
-  const double p = i * dx;
-  double v = 0.0;
-  if (i > 0) v = p <= 0.5 ? chi2_quantile(nu, p, false) : chi2_quantile(nu, 1.0 - p, true);
-  y[idx] = v;
+  if (idx >= (long long)rows * kNciRunsMain) return;
+  const int k = (int)(idx / kNciRunsMain), i0 = (int)(idx % kNciRunsMain) * kNciRunMain;
+  const int i1 = min(i0 + kNciRunMain, kNciGrid);
+  const double a = 0.5 * d + k, lga = lgamma(a);
+  double *yr = y + (size_t)k * kNciGrid;
+  double u = 0.0;
+  bool have = false;
+  for (int i = i0; i < i1; ++i) {
+    if (i == 0) {
+      yr[0] = 0.0;
+      continue;
+    }
+    const double p = i * dx;
+    const bool upper = p > 0.5;
+    const double pt = upper ? 1.0 - p : p;
+    const double lp = log(pt);
+    double u0 = 0.0;
+    bool warm = false;
+    if (have) {
+      const double x = exp(u), gh = exp(lga + x - a * u) * dx, s = a - x;
+      if (gh * (1.0 + fabs(s)) < kNciStepGate) {
+        u0 = u + gh * (1.0 + gh * (-0.5 * s + gh * (x + 2.0 * s * s) * (1.0 / 6.0)));
+        warm = true;
+      }
+    }
+    if (!warm) u0 = chi2_start(a, pt, lp, upper);
+    u = chi2_newton(a, lga, lp, upper, u0, kNciAccept);
+    have = true;
+    yr[i] = 2.0 * exp(u);
+  }
 }
 
+// Tail nodes at upper-tail probability q = e^-w, w = w0 + j dw.  Along w,
+// g = du/dw = q / (x f(x)) and d2u/dw2 = -g (1 + s g); the warm start is the
+// second-order step from the previous node.
 __global__ void nci_nodes_tail_kernel(double d, int rows, double w0, double dw, double *y,
                                       double *m) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (long long)rows * kNciTail) return;
-  const int k = (int)(idx / kNciTail), j = (int)(idx % kNciTail);
+  if (idx >= (long long)rows * kNciRunsTail) return;
+  const int k = (int)(idx / kNciRunsTail), j0 = (int)(idx % kNciRunsTail) * kNciRunTail;
+  const int j1 = min(j0 + kNciRunTail, kNciTail);
   const double nu = d + 2.0 * k;
-  const double w = w0 + j * dw;
-  const double q = exp(-w);
-  const double v = chi2_quantile(nu, q, true);
-  y[idx] = v;
-  m[idx] = exp(-w - chi2_logpdf(nu, v));  // dy/dw = q / f(y)
+  const double a = 0.5 * nu, lga = lgamma(a);
+  double u = 0.0, w_prev = 0.0;
+  bool have = false;
+  for (int j = j0; j < j1; ++j) {
+    const double w = w0 + j * dw;
+    double u0 = 0.0;
+    bool warm = false;
+    if (have) {
+      const double x = exp(u), gd = exp(-w_prev - (a * u - x - lga)) * dw, s = a - x;
+      if (gd * (1.0 + fabs(s)) < kNciStepGate) {
+        u0 = u + gd - 0.5 * gd * (dw + s * gd);
+        warm = true;
+      }
+    }
+    if (!warm) u0 = chi2_start(a, exp(-w), -w, true);
+    u = chi2_newton(a, lga, -w, true, u0, kNciAccept);
+    have = true;
+    w_prev = w;
+    const double v = 2.0 * exp(u);
+    const size_t o = (size_t)k * kNciTail + j;
+    y[o] = v;
+    m[o] = exp(-w - chi2_logpdf(nu, v));  // dy/dw = q / f(y)
+  }
 }
 
 // Monotone cubic Hermite cells with the reference's harmonic-mean slopes
@@ -202,13 +261,21 @@ cudaError_t launch_rng_draws(const unsigned long long *states, unsigned long lon
   return cudaGetLastError();
 }
 
+cudaError_t launch_nci_nodes(double d, int rows, double *tmp_main, double *tmp_ty, double *tmp_tm,
+                             double w0, double dw, cudaStream_t stream) {
+  const double dx = kNciUmax / (kNciGrid - 1);
+  const long long nm = (long long)rows * dev::kNciRunsMain, nt = (long long)rows * dev::kNciRunsTail;
+  dev::nci_nodes_main_kernel<<<(unsigned int)((nm + 127) / 128), 128, 0, stream>>>(d, rows, dx, tmp_main);
+  dev::nci_nodes_tail_kernel<<<(unsigned int)((nt + 63) / 64), 64, 0, stream>>>(d, rows, w0, dw, tmp_ty, tmp_tm);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_nci_build(double d, int rows, double *tmp_main, double *tmp_ty, double *tmp_tm,
                              float4 *cells_main, float4 *cells_tail, double w0, double dw,
                              cudaStream_t stream) {
   const double dx = kNciUmax / (kNciGrid - 1);
-  const long long nm = (long long)rows * kNciGrid, nt = (long long)rows * kNciTail;
-  dev::nci_nodes_main_kernel<<<(unsigned int)((nm + 127) / 128), 128, 0, stream>>>(d, rows, dx, tmp_main);
-  dev::nci_nodes_tail_kernel<<<(unsigned int)((nt + 127) / 128), 128, 0, stream>>>(d, rows, w0, dw, tmp_ty, tmp_tm);
+  cudaError_t e = launch_nci_nodes(d, rows, tmp_main, tmp_ty, tmp_tm, w0, dw, stream);
+  if (e != cudaSuccess) return e;
   const long long cm = (long long)rows * (kNciGrid - 1), ct = (long long)rows * (kNciTail - 1);
   dev::nci_cells_main_kernel<<<(unsigned int)((cm + 255) / 256), 256, 0, stream>>>(rows, tmp_main, dx, cells_main);
   dev::nci_cells_tail_kernel<<<(unsigned int)((ct + 255) / 256), 256, 0, stream>>>(rows, tmp_ty, tmp_tm, dw, cells_tail);

@@ -570,6 +570,13 @@ class Engine:
         _abi.check(self.lib.myql_chi2_quantile(self.handle, _ptr(dof), _ptr(p), _ptr(out), p.size))
         return out
 
+    def nci_nodes(self, d: float, rows: int):
+        """FP64 nodes of the SchemeNCI table of offset d: (main [rows, 10000], tail [rows, 512])."""
+        main = np.zeros((rows, 10000))
+        tail = np.zeros((rows, 512))
+        _abi.check(self.lib.myql_probe_nci_nodes(self.handle, float(d), int(rows), _ptr(main), _ptr(tail)))
+        return main, tail
+
     def sampler(self, kind: int, x, lam=None) -> np.ndarray:
         x = np.ascontiguousarray(x, dtype=np.uint64)
         out = np.zeros(x.size, dtype=np.float32)

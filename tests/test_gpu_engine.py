@@ -98,6 +98,27 @@ def test_device_chi2_quantile(engine):
     assert np.max(np.abs(got - want) / want) < 1e-9
 
 
+@pytest.mark.parametrize("d,rows", [(0.494, 110), (3.7, 40), (0.05, 1024)])
+def test_device_nci_nodes(engine, d, rows):
+    """Every FP64 node of the SchemeNCI table (main grid p = i 0.999/9999 and the upper tail
+    q = e^-w) against scipy's chi-squared quantiles, to 1e-11 relative.  The nodes of a row
+    are built from the previous node's quantile by a Taylor step plus Newton, so a row's
+    values depend on each other: the test covers whole rows, up to the 1024-row maximum."""
+    main, tail = engine.nci_nodes(d, rows)
+    nu = d + 2.0 * np.arange(rows)[:, None]
+    p = np.arange(10000) * (0.999 / 9999)
+    want = stats.chi2.ppf(p[None, :], nu)
+    assert np.all(main[:, 0] == 0.0)
+    rel = np.abs(main[:, 1:] - want[:, 1:]) / want[:, 1:]
+    assert rel.max() < 1e-11, (rel.max(), np.unravel_index(rel.argmax(), rel.shape))
+    assert np.all(np.diff(main, axis=1) > 0)
+    w0 = -np.log1p(-0.999)
+    w = w0 + np.arange(512) * ((44.5 - w0) / 511)
+    want_t = stats.chi2.isf(np.exp(-w)[None, :], nu)
+    rel_t = np.abs(tail - want_t) / want_t
+    assert rel_t.max() < 1e-11, (rel_t.max(), np.unravel_index(rel_t.argmax(), rel_t.shape))
+
+
 def base_spec():
     return jobspec.with_config(MC_SPECS["c1_heston_nv_call"], paths=50000, steps=50, streams=1024)
 

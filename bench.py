@@ -420,10 +420,16 @@ def cv_jobs(m, kind: str, paths: int, seed: int = 42):
     return m.make_job(model, stepper, instr, m.GreekMode.NONE, cfg, 100.0, 0.02, 0.0), steps
 
 
-def cv_config(m, kind: str, pilot: int = 1 << 19, iterations: int = 120):
+def cv_config(m, kind: str, pilot: int = 1 << 19, iterations: int = 120, plain_seconds: float | None = None):
+    """The control variate's settings: hedge every 8 (Asian) or 5 (European) steps; the
+    training budget given, or sized by ControlVariateConfig.for_plain_time."""
     kind = kind.split("_")[0]
-    return m.pricers.ControlVariateConfig(hedge_every=8 if kind == "asian" else 5, iterations=iterations,
-                                          pilot_paths=pilot, batch_paths=4096, learning_rate=5e-3, seed=7).c()
+    he = 8 if kind == "asian" else 5
+    if plain_seconds is not None:
+        return m.pricers.ControlVariateConfig.for_plain_time(plain_seconds, hedge_every=he, learning_rate=5e-3,
+                                                             seed=7).c()
+    return m.pricers.ControlVariateConfig(hedge_every=he, iterations=iterations, pilot_paths=pilot,
+                                          batch_paths=4096, learning_rate=5e-3, seed=7).c()
 
 
 def time_to_se(eng, m, kind: str, probe_paths: int = 1 << 22) -> dict:
@@ -434,10 +440,14 @@ def time_to_se(eng, m, kind: str, probe_paths: int = 1 << 22) -> dict:
     import torch
     target = CV_TARGETS[kind]
     job, steps = cv_jobs(m, kind, probe_paths)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
     raw, _ = eng.price(job)
+    t_probe = time.perf_counter() - t0
     price, se = raw[0, 0], raw[1, 0]
     n_plain = int(probe_paths * (se / (target * price)) ** 2) + 1
-    cfg = cv_config(m, kind)
+    # the training budget follows the plain estimator's expected time to the target
+    cfg = cv_config(m, kind, plain_seconds=t_probe * n_plain / probe_paths)
     t0 = time.perf_counter()
     tr = eng.cv_train(cv_jobs(m, kind, 1 << 16)[0], cfg)
     probe = eng.cv_price(cv_jobs(m, kind, probe_paths, seed=43)[0], cfg)
@@ -459,7 +469,7 @@ def time_to_se(eng, m, kind: str, probe_paths: int = 1 << 22) -> dict:
             "target_rel_se": target, "plain_paths": n_plain, "plain_s": t_plain, "plain_rel_se": rel_plain,
             "plain_path_steps_per_s": n_plain * steps / t_plain,
             "cv_paths": n_cv, "cv_s": t_cv, "cv_rel_se": res.price_std_err / res.price, "cv_train_s": tr.train_ms / 1e3,
-            "cv_pilot_paths": int(tr.paths), "cv_iterations": int(cfg.iterations),
+            "cv_pilot_paths": int(tr.paths), "cv_iterations": int(cfg.iterations), "cv_batch_paths": int(cfg.batch_paths),
             "variance_ratio": res.variance_ratio, "speedup": t_plain / t_cv,
             "price_cv": res.price, "price_plain": float(raw[0, 0])}
 
@@ -468,13 +478,14 @@ def qmc_time_to_se(eng, m, target: float = 1e-4, R: int = 16, probe_paths: int =
     """The Heston European call of the control-variate comparison (SchemeNV, 100 steps) priced
     by randomized quasi-Monte Carlo (Sobol + Brownian bridge, R digital shifts): wall time
     to the relative standard error target against plain GPU Monte Carlo.  The probe fixes
-    the QMC error at one size; the timed run takes the path count that the plain 1/sqrt(n)
-    rate gives for the target (an upper bound, since the QMC error falls faster), rounded up
-    to a power of two per replicate."""
+    the QMC error at one size; the timed run starts at the path count that the plain 1/sqrt(n)
+    rate gives for 0.8 x the target, rounded up to a power of two per replicate, and doubles the
+    points per replicate while the estimated error (R replicates, so itself noisy) is above
+    the target: every attempt is inside the timed region."""
     import torch
     job, steps = cv_jobs(m, "european", probe_paths)
     q, _ = eng.qmc_price(job, R)
-    need = probe_paths * (q[1, 0] / (target * q[0, 0])) ** 2
+    need = probe_paths * (q[1, 0] / (0.8 * target * q[0, 0])) ** 2  # 1.25x margin on the noisy estimate
     pts = 2048
     while pts * R < need:  # a power of two per replicate: the balanced Sobol point sets
         pts *= 2
@@ -484,13 +495,20 @@ def qmc_time_to_se(eng, m, target: float = 1e-4, R: int = 16, probe_paths: int =
     n_plain = int((1 << 22) * (raw[1, 0] / (target * raw[0, 0])) ** 2) + 1
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    q, _ = eng.qmc_price(cv_jobs(m, "european", n_q, seed=48)[0], R)
+    attempts = 0
+    while True:
+        attempts += 1
+        q, _ = eng.qmc_price(cv_jobs(m, "european", n_q, seed=48)[0], R)
+        if q[1, 0] <= target * q[0, 0] or attempts == 6:
+            break
+        n_q *= 2
     t_q = time.perf_counter() - t0
     t0 = time.perf_counter()
     raw, _ = eng.price(cv_jobs(m, "european", n_plain, seed=49)[0])
     t_plain = time.perf_counter() - t0
     return {"instrument": "Heston European call (SchemeNV, 100 steps)", "target_rel_se": target, "replicates": R,
-            "qmc_paths": n_q, "qmc_s": t_q, "qmc_rel_se": q[1, 0] / q[0, 0], "plain_paths": n_plain,
+            "qmc_paths": n_q, "qmc_attempts": attempts, "qmc_s": t_q, "qmc_rel_se": q[1, 0] / q[0, 0],
+            "plain_paths": n_plain,
             "plain_s": t_plain, "plain_rel_se": raw[1, 0] / raw[0, 0], "speedup": t_plain / t_q,
             "price_qmc": q[0, 0], "price_plain": raw[0, 0]}
 

@@ -755,6 +755,22 @@ class ControlVariateConfig:
     learning_rate: float = 5e-3
     seed: int = 1
 
+    @classmethod
+    def for_plain_time(cls, plain_seconds: float, **kw) -> "ControlVariateConfig":
+        """A training budget sized to the job: `plain_seconds` is the estimated time of plain
+        Monte Carlo to the wanted standard error.  Training is a fixed cost and its variance
+        ratio grows slowly with it (Double Bates Asian, 256 steps: ratio 11 after 30 Adam steps
+        on 2^16 pilot paths in 6 ms, 18 after 120 steps on 2^19 paths in 24 ms), so a short
+        job gets the short training and a long one the full training."""
+        if plain_seconds < 0.05:
+            budget = dict(pilot_paths=1 << 16, iterations=30, batch_paths=4096)
+        elif plain_seconds < 0.5:
+            budget = dict(pilot_paths=1 << 18, iterations=60, batch_paths=2048)
+        else:
+            budget = dict(pilot_paths=1 << 19, iterations=120, batch_paths=4096)
+        budget.update(kw)
+        return cls(**budget)
+
     def c(self) -> _abi.CvConfigC:
         c = _abi.CvConfigC()
         c.hedge_every, c.iterations, c.pilot_paths = self.hedge_every, self.iterations, self.pilot_paths

@@ -39,3 +39,17 @@ def test_backprop_matches_finite_differences():
 def test_bf16_rounding():
     x = np.array([1.0, 1.0 + 2 ** -8, 1.0 + 3 * 2 ** -8, -3.1415926, 0.0])
     assert list(mo.bf16(x)) == [1.0, 1.0, 1.0 + 2 ** -6, -3.140625, 0.0]
+
+
+def test_cv_training_budget_follows_the_plain_time():
+    """The control variate's training budget grows with the plain estimator's time to the
+    target, and explicit settings (hedging interval, seed) pass through."""
+    from myquantlib_gb300.pricers import ControlVariateConfig
+    light = ControlVariateConfig.for_plain_time(0.02, hedge_every=8, seed=7)
+    mid = ControlVariateConfig.for_plain_time(0.1)
+    full = ControlVariateConfig.for_plain_time(2.0, iterations=150)
+    assert light.pilot_paths < mid.pilot_paths < full.pilot_paths
+    assert light.iterations < mid.iterations < full.iterations
+    assert (light.hedge_every, light.seed, full.iterations) == (8, 7, 150)
+    c = light.c()
+    assert (c.pilot_paths, c.iterations, c.batch_paths) == (1 << 16, 30, 4096)

@@ -297,7 +297,11 @@ def run_engine(args) -> dict:
     xu_ach = XU_PER_STEP * sim / (sim_ms / 1e3)
     alu_frac, xu_frac = alu_ach / alu_peak, xu_ach / xu_peak
     bound = "alu" if alu_frac >= xu_frac else "xu"
-    roof = {"bound": bound, "kernel": "simulate_lockstep_kernel<1,NCI,-,5 scenarios>",
+    roof = {"bound": bound, "kernel": "simulate_lockstep_kernel<1,NCI,-,5 scenarios,merged variance paths>",
+            "note": ("achieved counts the algorithmic ops of every simulated scenario path-step (153 ALU, "
+                     "5 XU); the lockstep kernel shares the draws of a step across scenarios and, once a "
+                     "v0-bumped variance path has merged into the base's, its Poisson inversion and table "
+                     "cell, so it issues fewer (about 100 lane-ops per scenario path-step under ncu)"),
             "achieved": (alu_ach if bound == "alu" else xu_ach) / 1e9,
             "peak": (alu_peak if bound == "alu" else xu_peak) / 1e9, "unit": "Gop/s",
             "frac": max(alu_frac, xu_frac),

@@ -411,6 +411,24 @@ myql_status make_plan(const myql_mc_job &job, Plan &pl, bool stepped) {
       C.jump_comp = (float)(-m.jump_lambda * kjump * window);
     }
   }
+  // The lockstep kernel merges a v0-bumped scenario's variance path into the
+  // base's when its NCI constants (Poisson mean factor, degrees of freedom,
+  // table scale) are the base's for every factor.  (After a v0 bump of 1e-4 about
+  // one lane in ten draws a different Poisson count at the first step, and such
+  // paths merge over tens of steps; on the Bates strip merging still gains 2 %
+  // at 50 steps and 18 % at 800.)
+  P.lock_merge = 0;
+  if (pl.mode == MYQL_GREEKS_FULL && pl.nf >= 1) {
+    bool same = true;
+    for (int i = 1; i < pl.n_sc; ++i) {
+      if (i != SC_VUP0 && i != SC_VDN0 && i != SC_VUP1 && i != SC_VDN1) continue;
+      for (int f = 0; f < pl.nf; ++f) {
+        const FactorConst &a = P.sc[i].f[f], &b = P.sc[0].f[f];
+        same = same && a.w0 == b.w0 && a.w1 == b.w1 && a.w2 == b.w2;
+      }
+    }
+    P.lock_merge = same ? 1 : 0;
+  }
 
   // ---- payoff pass
   PayoffParams &Q = pl.pay;

@@ -93,6 +93,7 @@ struct SimParams {
   float kou_p_up, kou_inv_eta1, kou_inv_eta2;
   NciTable nci[2];
   unsigned long long nci_u999;  // smallest 64-bit draw whose uniform is >= 0.999
+  int lock_merge;               // lockstep kernel: v0-bumped variance paths merge into the base's
   // exact-scheme small-alpha constants (VolSchemes.hpp:95-103), per factor
   float sm_p[2], sm_inv_p[2], sm_1mp[2], sm_1ma[2], sm_inv_a[2];
   unsigned long long *states;  // [4][n_streams] xoshiro states, updated in place

@@ -346,6 +346,19 @@ __global__ void __launch_bounds__(kSimBlock) simulate_kernel(const __grid_consta
 // v0 (or factor-0 v0) up / down, T up / down, then factor-1 v0 up / down.
 __host__ __device__ constexpr int lockstep_sc(int j) { return j < 5 ? j : j + 2; }
 
+// Merged variance paths.  Under SchemeNCI the next variance depends on the
+// current one only through the Poisson count N (the table row): a v0-bumped
+// scenario shares the base's time step, so once its variance equals the
+// base's bit for bit (the first step at which both draw the same N, usually
+// the first), it stays equal for the rest of the path.  A step then evolves
+// inline only the scenarios with their own time step -- base, T up, T down --
+// and gives a merged scenario the base's new variance: the value its own
+// evaluation would give.  A scenario that has not merged yet runs on its own
+// (nci_step_one), on the lanes that need it.  Lockstep order of the shared
+// subset: 0, 3, 4.
+__host__ __device__ constexpr int lockstep_sub(int j) { return j == 0 ? 0 : j + 2; }
+__host__ __device__ constexpr bool lockstep_merges(int j) { return j != 0 && j != 3 && j != 4; }
+
 // The per-step draws of one factor, shared by every scenario.
 template <int SCH>
 struct FactorDraws {
@@ -371,15 +384,18 @@ __device__ __forceinline__ void factor_draws(FactorDraws<SCH> &d, Xo &rng, const
 // evolve<SCH> (above) of one factor for every scenario, with the step's draws
 // given: the Poisson inversions of all scenarios first, then all their table
 // gathers (independent loads in flight together), then the cubic cells.
-template <int SCH, int NS>
+// SUB: the NS = 3 scenarios of lockstep_sub; a table fallback of the base then
+// stands for the base and its `merged` copies.
+template <int SCH, int NS, bool SUB = false>
 __device__ __forceinline__ void evolve_lockstep(const float (&v)[NS], float (&vn)[NS],
                                                 const FactorDraws<SCH> &d, const SimParams &P,
                                                 int fi, unsigned int &caphits,
-                                                unsigned int &fallbacks) {
+                                                unsigned int &fallbacks, unsigned int merged = 0) {
+  auto sc = [](int j) { return SUB ? lockstep_sub(j) : lockstep_sc(j); };
   if (SCH == SCH_NV) {
 #pragma unroll
     for (int j = 0; j < NS; ++j) {
-      const FactorConst &f = P.sc[lockstep_sc(j)].f[fi];
+      const FactorConst &f = P.sc[sc(j)].f[fi];
       const float root = sqrt_approx(fmaf(f.w0, v[j], f.w1)) + f.w2 * d.Z;
       vn[j] = fmaf(f.w0 * root, root, f.w1);
     }
@@ -387,7 +403,7 @@ __device__ __forceinline__ void evolve_lockstep(const float (&v)[NS], float (&vn
     float lam[NS];
     int N[NS];
 #pragma unroll
-    for (int j = 0; j < NS; ++j) lam[j] = P.sc[lockstep_sc(j)].f[fi].w0 * v[j];
+    for (int j = 0; j < NS; ++j) lam[j] = P.sc[sc(j)].f[fi].w0 * v[j];
     poisson_eval_n<NS>(lam, d.U, d.xp, P.loop_cap, caphits, N);
     const NciTable &tab = P.nci[fi];
     float4 c[NS];
@@ -397,18 +413,77 @@ __device__ __forceinline__ void evolve_lockstep(const float (&v)[NS], float (&vn
     for (int j = 0; j < NS; ++j) {
       float q = nci_cubic(c[j], d.pos.t);
       if (N[j] >= tab.rows) {
-        ++fallbacks;
+        fallbacks += (SUB && j == 0) ? 1 + merged : 1;
         q = nci_beyond(tab, N[j], d.x2);
       }
-      vn[j] = q * P.sc[lockstep_sc(j)].f[fi].w2;
+      vn[j] = q * P.sc[sc(j)].f[fi].w2;
     }
   }
 }
 
-template <int NF, int S1, int S2, int NSIM>
+// One NCI scenario on the step's shared draws, for the lanes whose scenario
+// has not merged yet: the arithmetic of evolve_lockstep for one mean
+// (poisson_eval_n gives each mean poisson_eval's N).  Inline: an out-of-line
+// call cost 13 % at 200 steps in instruction-fetch stalls.
+struct NciOne {
+  float v;
+  unsigned int caphits, fallbacks;
+};
+__device__ __forceinline__ NciOne nci_step_one(float lam, float scale, const NciTable &tab,
+                                                   unsigned long long xp, float U,
+                                                   unsigned long long x2, NciPos pos,
+                                                   unsigned int cap) {
+  NciOne o{0.0f, 0u, 0u};
+  const float W = lam > kPoissonAsymMin ? inv_normal_bits(xp) : 0.0f;
+  const int N = poisson_eval(lam, U, W, xp, cap, o.caphits);
+  float q = nci_cubic(nci_cell(tab, N, pos), pos.t);
+  if (N >= tab.rows) {
+    o.fallbacks = 1;
+    q = nci_beyond(tab, N, x2);
+  }
+  o.v = q * scale;
+  return o;
+}
+
+// evolve_lockstep of one NCI factor with merged variance paths (see lockstep_sub).
+template <int NS>
+__device__ __forceinline__ void evolve_merged(const float (&v)[NS], float (&vn)[NS],
+                                              const FactorDraws<SCH_NCI> &d, const SimParams &P,
+                                              int fi, unsigned int &caphits,
+                                              unsigned int &fallbacks) {
+  bool same[NS];
+  unsigned int nm = 0;
+#pragma unroll
+  for (int j = 0; j < NS; ++j) {
+    same[j] = lockstep_merges(j) && v[j] == v[0];
+    nm += same[j] ? 1u : 0u;
+  }
+  const float v3[3] = {v[0], v[3], v[4]};
+  float o3[3];
+  evolve_lockstep<SCH_NCI, 3, true>(v3, o3, d, P, fi, caphits, fallbacks, nm);
+#pragma unroll
+  for (int j = 0; j < NS; ++j) {
+    if (j == 3 || j == 4) {
+      vn[j] = o3[j - 2];
+    } else if (j == 0 || same[j]) {
+      vn[j] = o3[0];
+    } else {
+      const FactorConst &f = P.sc[lockstep_sc(j)].f[fi];
+      const NciOne o = nci_step_one(f.w0 * v[j], f.w2, P.nci[fi], d.xp, d.U, d.x2, d.pos, P.loop_cap);
+      vn[j] = o.v;
+      caphits += o.caphits;
+      fallbacks += o.fallbacks;
+    }
+  }
+}
+
+// MERGE: the v0-bumped scenarios' variance paths merge into the base's (every
+// factor on NCI, and P.lock_merge: the host found their NCI constants equal).
+template <int NF, int S1, int S2, int NSIM, bool MERGE = false>
 __global__ void __launch_bounds__(kSimBlock) simulate_lockstep_kernel(
     const __grid_constant__ SimParams P) {
   static_assert(NF >= 1 && S1 != SCH_EXACT && S2 != SCH_EXACT, "lockstep needs NV/NCI factors");
+  static_assert(!MERGE || (S1 == SCH_NCI && (NF == 1 || S2 == SCH_NCI)), "merging needs NCI factors");
   const unsigned int s = blockIdx.x * kSimBlock + threadIdx.x;
   const unsigned int S = P.n_streams;
   if (s >= S) return;
@@ -435,8 +510,13 @@ __global__ void __launch_bounds__(kSimBlock) simulate_lockstep_kernel(
       factor_draws<S1>(da, rng, P, 0);
       if (NF == 2) factor_draws<S2>(db, rng, P, 1);
       float van[NSIM], vbn[NSIM];
-      evolve_lockstep<S1, NSIM>(va, van, da, P, 0, caphits, fallbacks);
-      if (NF == 2) evolve_lockstep<S2, NSIM>(vb, vbn, db, P, 1, caphits, fallbacks);
+      if constexpr (MERGE) {
+        evolve_merged<NSIM>(va, van, da, P, 0, caphits, fallbacks);
+        if constexpr (NF == 2) evolve_merged<NSIM>(vb, vbn, db, P, 1, caphits, fallbacks);
+      } else {
+        evolve_lockstep<S1, NSIM>(va, van, da, P, 0, caphits, fallbacks);
+        if (NF == 2) evolve_lockstep<S2, NSIM>(vb, vbn, db, P, 1, caphits, fallbacks);
+      }
 #pragma unroll
       for (int j = 0; j < NSIM; ++j) {
         const ScenarioConst &C = P.sc[lockstep_sc(j)];

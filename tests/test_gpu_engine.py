@@ -228,20 +228,27 @@ LOCKSTEP = {
     "bateskou_nci": (m.BatesKouModel(_H_NV, _KJ), m.BatesKouStepper(m.SchemeNCI)),
     "dbates_nci_nv": (m.DoubleBatesModel(_H_NCI, _H_NV2, _MJ), m.DoubleBatesStepper(m.SchemeNCI, m.SchemeNV)),
     "dheston_nv_nci": (m.DoubleHestonModel(_H_NV, _H_NCI), m.DoubleHestonStepper(m.SchemeNV, m.SchemeNCI)),
+    # both factors on NCI: the v0-bumped variance paths merge into the base's
+    "dbates_nci_nci": (m.DoubleBatesModel(_H_NCI, m.HestonParams(1.0, 0.03, 0.6, -0.4, 0.03), _MJ),
+                       m.DoubleBatesStepper(m.SchemeNCI, m.SchemeNCI)),
 }
 
 
-@pytest.mark.parametrize("name", list(LOCKSTEP))
-def test_full_greek_scenarios_equal_single_scenario_runs(engine, name):
+LOCKSTEP_CASES = [(n, 40) for n in LOCKSTEP] + [(n, 200) for n in ("bates_nci", "dbates_nci_nci")]
+
+
+@pytest.mark.parametrize("name,steps", LOCKSTEP_CASES, ids=[f"{n}-{k}" for n, k in LOCKSTEP_CASES])
+def test_full_greek_scenarios_equal_single_scenario_runs(engine, name, steps):
     """Full Greeks of a European advance every bumped scenario of a path in lockstep
     on shared draws.  Each scenario's records must be bit-identical to a request
     that prices that bumped scenario alone (MonteCarloPricer.hpp:302-410 replays
-    the path from rng_start for each bump)."""
+    the path from rng_start for each bump).  The v0-bumped variance paths of NCI factors
+    merge into the base's; the 200-step cases run most steps merged."""
     model, stepper = LOCKSTEP[name]
     # one path per stream: a stream continues from the base scenario's end state, and a
     # bumped scenario priced alone continues from its own, which differs once its jump
     # count (and so its draw count) differs from the base's
-    cfg = m.MonteCarloConfig(num_paths=6000, time_steps=40, seed=7, n_streams=6000)
+    cfg = m.MonteCarloConfig(num_paths=6000, time_steps=steps, seed=7, n_streams=6000)
     T, S0, r, q = 0.75, 100.0, 0.02, 0.01
     full = m.make_job(model, stepper, m.EuropeanOption([90.0, 100.0, 110.0], T), m.GreekMode.FULL,
                       cfg, S0, r, q)

@@ -349,8 +349,8 @@ __host__ __device__ constexpr int lockstep_sc(int j) { return j < 5 ? j : j + 2;
 // Merged variance paths.  Under SchemeNCI the next variance depends on the
 // current one only through the Poisson count N (the table row): a v0-bumped
 // scenario shares the base's time step, so once its variance equals the
-// base's bit for bit (the first step at which both draw the same N, usually
-// the first), it stays equal for the rest of the path.  A step then evolves
+// base's bit for bit (from the first step at which both draw the same N), it
+// stays equal for the rest of the path.  A step then evolves
 // inline only the scenarios with their own time step -- base, T up, T down --
 // and gives a merged scenario the base's new variance: the value its own
 // evaluation would give.  A scenario that has not merged yet runs on its own
@@ -430,9 +430,9 @@ struct NciOne {
   unsigned int caphits, fallbacks;
 };
 __device__ __forceinline__ NciOne nci_step_one(float lam, float scale, const NciTable &tab,
-                                                   unsigned long long xp, float U,
-                                                   unsigned long long x2, NciPos pos,
-                                                   unsigned int cap) {
+                                               unsigned long long xp, float U,
+                                               unsigned long long x2, NciPos pos,
+                                               unsigned int cap) {
   NciOne o{0.0f, 0u, 0u};
   const float W = lam > kPoissonAsymMin ? inv_normal_bits(xp) : 0.0f;
   const int N = poisson_eval(lam, U, W, xp, cap, o.caphits);

@@ -571,34 +571,54 @@ def run_mlmc(args) -> dict:
     eps = 1e-3 * price
     # warm-up (tables, streams, first launches)
     eng.mlmc_cv_price(job, cfg(20 * eps), cvc)
-    res_plain = _abi.MlmcResultC()
+    # Each arm on three controller seeds: one run's allocation rests on pilot variance estimates
+    # of rare barrier events, and a single noisy estimate on the finest level can triple its
+    # path count, so one seed per arm compares allocations rather than estimators.
+    seeds = (42, 43, 44)
+    runs_plain, runs_cv = [], []
     with ClockSampler(0) as clk:
-        t0 = time.perf_counter()
-        _abi.check(eng.lib.myql_mlmc_price(eng.handle, m.pricers.C.byref(job.c), m.pricers.C.byref(cfg(eps)),
-                                           m.pricers.C.byref(res_plain)))
-        t_plain = time.perf_counter() - t0
-        t0 = time.perf_counter()
-        res_cv, plain_var = eng.mlmc_cv_price(job, cfg(eps), cvc)
-        t_cv = time.perf_counter() - t0
-    nl = res_cv.n_levels
+        for sd in seeds:
+            c = cfg(eps)
+            c.seed = sd
+            res_plain = _abi.MlmcResultC()
+            t0 = time.perf_counter()
+            _abi.check(eng.lib.myql_mlmc_price(eng.handle, m.pricers.C.byref(job.c), m.pricers.C.byref(c),
+                                               m.pricers.C.byref(res_plain)))
+            runs_plain.append((time.perf_counter() - t0, res_plain, None))
+            c = cfg(eps)
+            c.seed = sd
+            t0 = time.perf_counter()
+            res_cv, plain_var = eng.mlmc_cv_price(job, c, cvc)
+            runs_cv.append((time.perf_counter() - t0, res_cv, plain_var))
+
+    def arm(runs, with_ratio):
+        out = []
+        for t, r, pv in runs:
+            nl = int(r.n_levels)
+            d = {"s": t, "price": r.price, "se": r.price_std_err, "levels": nl,
+                 "paths_per_level": [int(r.paths_per_level[l]) for l in range(nl)], "path_steps": int(r.total_steps)}
+            if with_ratio:
+                d["variance_ratio_per_level"] = [float(pv[l] / max(r.var_diffs[l], 1e-300)) for l in range(nl)]
+                d["cv_levels"] = [l for l in range(nl) if abs(pv[l] / max(r.var_diffs[l], 1e-300) - 1.0) > 1e-9]
+            out.append(d)
+        return out
+
+    t_plain = statistics.median(t for t, _, _ in runs_plain)
+    t_cv = statistics.median(t for t, _, _ in runs_cv)
+    cost_plain = sum(t * r.price_std_err ** 2 for t, r, _ in runs_plain)
+    cost_cv = sum(t * r.price_std_err ** 2 for t, r, _ in runs_cv)
     return {"metric": "time-to-RMSE (s) MLMC + neural CV vs plain MLMC", "value": t_cv, "unit": "s", "n_gpus": 1,
-            "steps": 1, "warmup": 1, "ms_per_step": t_cv * 1e3, "higher_is_better": False, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 paths, fp64 level sums, bf16 MLP", "data": "synthetic",
+            "steps": len(seeds), "warmup": 1, "ms_per_step": t_cv * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 paths, fp64 level sums, bf16 MLP",
+            "data": "synthetic",
             "config": {"workload": "MLMC Heston down-and-out put, SchemeNV, levels 2..10", "epsilon": eps,
-                       "price": price},
-            "plain": {"s": t_plain, "price": res_plain.price, "se": res_plain.price_std_err,
-                      "levels": int(res_plain.n_levels),
-                      "paths_per_level": [int(res_plain.paths_per_level[l]) for l in range(res_plain.n_levels)],
-                      "path_steps": int(res_plain.total_steps)},
-            "cv": {"s": t_cv, "price": res_cv.price, "se": res_cv.price_std_err, "levels": int(nl),
-                   "paths_per_level": [int(res_cv.paths_per_level[l]) for l in range(nl)],
-                   "variance_ratio_per_level": [float(plain_var[l] / max(res_cv.var_diffs[l], 1e-300))
-                                                for l in range(nl)],
-                   "path_steps": int(res_cv.total_steps)},
+                       "price": price, "controller_seeds": list(seeds),
+                       "value": "median over the seeds of the MLMC + CV wall time"},
+            "plain": {"median_s": t_plain, "runs": arm(runs_plain, False)},
+            "cv": {"median_s": t_cv, "runs": arm(runs_cv, True)},
             "speedup": t_plain / t_cv,
-            # cost at equal standard error (the two controllers stop at different SEs):
-            "efficiency_ratio": (t_plain * res_plain.price_std_err ** 2) / (t_cv * res_cv.price_std_err ** 2),
-            "cv_levels": [l for l in range(nl) if abs(plain_var[l] / max(res_cv.var_diffs[l], 1e-300) - 1.0) > 1e-9],
+            # cost at equal standard error (the controllers stop at different SEs): sum of time x SE^2
+            "efficiency_ratio": cost_plain / cost_cv,
             "clocks": clk.summary()}
 
 

@@ -342,6 +342,84 @@ def run_engine(args) -> dict:
     return line
 
 
+def run_c1(args) -> dict:
+    """Configuration 1: Heston SchemeNV European call (kappa 1.5, theta .04, sigma .3, rho -.7,
+    v0 .04; S0 = K = 100, T 1, r .02, q 0), 2^20 paths x 100 steps, seed 42, GreekMode::None.
+    value: path-steps / device time of R = 16 back-to-back requests per step (CUDA events on
+    the launching stream, L2 flushed between steps); e2e: the same through myql_mc_price with
+    a pinned host result buffer; cpu_baseline: the CPU port on the whole request."""
+    import torch
+    import myquantlib_gb300 as m
+
+    if int(os.environ.get("RANK", "0")) != 0:
+        return {}
+    R, paths, steps = 16, 1 << 20, 100
+    eng = m.Engine(0)
+    job = m.make_job(m.HestonModel(m.HestonParams(1.5, 0.04, 0.3, -0.7, 0.04)), m.HestonStepper(m.SchemeNV),
+                     m.EuropeanOption(100.0, 1.0), m.GreekMode.NONE,
+                     m.MonteCarloConfig(num_paths=paths, time_steps=steps, seed=SEED), 100.0, 0.02, 0.0)
+    stream = torch.cuda.Stream(device=0)
+    out = torch.empty(2 * 10, dtype=torch.float64, device="cuda:0")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda:0")
+    launches = 0
+    for _ in range(max(args.warmup, 1)):
+        _, st = eng.price(job)
+        launches = st.kernel_launches
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    sims = []
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clk:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                ev[k][0].record(stream)
+                for _ in range(R):
+                    m._abi.check(eng.lib.myql_mc_price_async(eng.handle, m.pricers.C.byref(job.c), out.data_ptr(),
+                                                             stream.cuda_stream))
+                ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        dev_ms = sum(a.elapsed_time(b) for a, b in ev)
+        pin = torch.empty(2 * 10, dtype=torch.float64).pin_memory()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps * R):
+            st = m._abi.McStatsC()
+            m._abi.check(eng.lib.myql_mc_price(eng.handle, m.pricers.C.byref(job.c),
+                                               m.pricers.C.cast(pin.data_ptr(), m.pricers.C.POINTER(m.pricers.C.c_double)),
+                                               m.pricers.C.byref(st)))
+            sims.append(st.simulate_ms)
+        e2e_s = time.perf_counter() - t0
+    work = paths * steps * R
+    value = work * args.steps / (dev_ms / 1e3)
+    sim_ms = statistics.median(sims)
+    alu_peak = eng.peak(0)
+    alu_ach = 97 * paths * steps / (sim_ms / 1e3)
+    line = {"metric": "paths*steps/s", "value": value, "unit": "paths*steps/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "Heston SchemeNV European call, 2^20 paths x 100 steps, GreekMode None "
+                                   "(configuration 1)", "requests_per_step": R, "path_steps_per_step": work,
+                       "l2": "flushed between steps (256 MiB write)", "price": float(pin[0])},
+            "e2e": {"value": work * args.steps / e2e_s, "unit": "paths*steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 8 * 20 * R},
+            "gpu_launches": launches * R * args.steps,
+            "roofline": {"bound": "alu", "kernel": "simulate_kernel<1,NV,-,false>", "achieved": alu_ach / 1e9,
+                         "peak": alu_peak / 1e9, "unit": "Gop/s", "frac": alu_ach / alu_peak,
+                         "ops_per_path_step": 97, "simulate_ms_per_request": sim_ms,
+                         "peak_source": "measured by myql_probe_peak (FP32-FMA microbenchmark on this GPU)"},
+            "clocks": clk.summary()}
+    if not args.no_cpu:
+        from oracle import oracle
+        oracle.build(ref=False)
+        cores = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        oracle.mc_price(job, oracle.LAYOUT_REFERENCE, cores, fast=True)
+        t = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": paths * steps / t, "unit": "paths*steps/s", "cores": cores, "kind": "port",
+                                "sample": f"the whole request, 2^20 paths x 100 steps ({t:.2f} s)"}
+    return line
+
+
 def run_batch(args) -> dict:
     """Batched uneven requests (4096 jobs, myquantlib_gb300.workloads.uneven_requests) in one
     persistent launch per step.  value: path-steps / device time of the batch graph (descriptor
@@ -661,9 +739,10 @@ def main():
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
     ap.add_argument("--cpu-paths", type=int, default=8192, help="paths of the smaller CPU-baseline sample")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
-    ap.add_argument("--workload", choices=["strip", "batch", "cv", "mlmc"], default="strip",
+    ap.add_argument("--workload", choices=["strip", "batch", "cv", "mlmc", "c1"], default="strip",
                     help="strip: the Bates Full-Greeks strip (headline); batch: uneven requests in one launch; "
-                         "cv: time-to-relative-SE of the neural control variate against plain MC")
+                         "cv: time-to-relative-SE of the neural control variate against plain MC; mlmc: MLMC "
+                         "with and without the control variate; c1: plain Heston NV European (configuration 1)")
     ap.add_argument("--batch-jobs", type=int, default=4096)
     ap.add_argument("--ncu-case", action="store_true",
                     help="profiling case: one maturity (T=1), 2^18 paths, two requests, no timing")
@@ -681,7 +760,7 @@ def main():
     if args.impl == "reference":
         line = run_reference(args)
     else:
-        line = {"batch": run_batch, "cv": run_cv, "mlmc": run_mlmc}.get(args.workload, run_engine)(args)
+        line = {"batch": run_batch, "cv": run_cv, "mlmc": run_mlmc, "c1": run_c1}.get(args.workload, run_engine)(args)
     if line:
         print(json.dumps(line), flush=True)
 

@@ -759,11 +759,11 @@ class ControlVariateConfig:
     def for_plain_time(cls, plain_seconds: float, **kw) -> "ControlVariateConfig":
         """A training budget sized to the job: `plain_seconds` is the estimated time of plain
         Monte Carlo to the wanted standard error.  Training is a fixed cost and its variance
-        ratio grows slowly with it (Double Bates Asian, 256 steps: ratio 11 after 30 Adam steps
-        on 2^16 pilot paths in 6 ms, 18 after 120 steps on 2^19 paths in 24 ms), so a short
-        job gets the short training and a long one the full training."""
+        ratio grows slowly with it (Double Bates Asian, 256 steps, GB300: ratio 7.8 after 15
+        Adam steps of 2048 paths on 2^15 pilot paths in 3 ms, 17.6 after 120 steps of 4096 on
+        2^19 in 18 ms), so a short job gets the short training and a long one the full one."""
         if plain_seconds < 0.05:
-            budget = dict(pilot_paths=1 << 16, iterations=30, batch_paths=4096)
+            budget = dict(pilot_paths=1 << 15, iterations=15, batch_paths=2048)
         elif plain_seconds < 0.5:
             budget = dict(pilot_paths=1 << 18, iterations=60, batch_paths=2048)
         else:

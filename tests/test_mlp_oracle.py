@@ -52,4 +52,4 @@ def test_cv_training_budget_follows_the_plain_time():
     assert light.iterations < mid.iterations < full.iterations
     assert (light.hedge_every, light.seed, full.iterations) == (8, 7, 150)
     c = light.c()
-    assert (c.pilot_paths, c.iterations, c.batch_paths) == (1 << 16, 30, 4096)
+    assert (c.pilot_paths, c.iterations, c.batch_paths) == (1 << 15, 15, 2048)

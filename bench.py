@@ -183,8 +183,10 @@ def run_reference(args) -> dict:
     v = statistics.median(vals)
     cpu = dict(times[-1])
     cpu["value"] = v
+    _, base = path_steps()
     return {"metric": "paths*steps/s", "value": v, "unit": "paths*steps/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": base / v * 1e3,  # one whole-strip step at the extrapolated rate
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference", "cpu_baseline": cpu,
             "e2e": {"value": v, "unit": "paths*steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

@@ -422,6 +422,18 @@ def run_c1(args) -> dict:
     return line
 
 
+def run_ncu_c1_case() -> None:
+    """Profiling case of configuration 1: two pricing requests of the full 2^20 paths x 100
+    steps, no timing."""
+    import myquantlib_gb300 as m
+    eng = m.Engine(0)
+    job = m.make_job(m.HestonModel(m.HestonParams(1.5, 0.04, 0.3, -0.7, 0.04)), m.HestonStepper(m.SchemeNV),
+                     m.EuropeanOption(100.0, 1.0), m.GreekMode.NONE,
+                     m.MonteCarloConfig(num_paths=1 << 20, time_steps=100, seed=SEED), 100.0, 0.02, 0.0)
+    for _ in range(2):
+        eng.price(job)
+
+
 def run_batch(args) -> dict:
     """Batched uneven requests (4096 jobs, myquantlib_gb300.workloads.uneven_requests) in one
     persistent launch per step.  value: path-steps / device time of the batch graph (descriptor
@@ -756,6 +768,8 @@ def main():
             run_ncu_cv_case()
         elif args.workload == "batch":
             run_ncu_batch_case()
+        elif args.workload == "c1":
+            run_ncu_c1_case()
         else:
             run_ncu_case(full=args.ncu_full)
         return

@@ -517,12 +517,14 @@ def cv_jobs(m, kind: str, paths: int, seed: int = 42):
 
 
 def cv_config(m, kind: str, pilot: int = 1 << 19, iterations: int = 120, plain_seconds: float | None = None):
-    """The control variate's settings: hedge every 8 (Asian) or 5 (European) steps; the
-    training budget given, or sized by ControlVariateConfig.for_plain_time."""
+    """The control variate's settings: the training budget and hedging interval sized by
+    ControlVariateConfig.for_plain_time from the plain estimator's time, or (for warm-up and
+    profiling) the given budget, hedging every 8 (Asian) or 5 (European) steps."""
     kind = kind.split("_")[0]
     he = 8 if kind == "asian" else 5
     if plain_seconds is not None:
-        return m.pricers.ControlVariateConfig.for_plain_time(plain_seconds, hedge_every=he, learning_rate=5e-3,
+        steps = 256 if kind == "asian" else 100
+        return m.pricers.ControlVariateConfig.for_plain_time(plain_seconds, time_steps=steps, learning_rate=5e-3,
                                                              seed=7).c()
     return m.pricers.ControlVariateConfig(hedge_every=he, iterations=iterations, pilot_paths=pilot,
                                           batch_paths=4096, learning_rate=5e-3, seed=7).c()
@@ -566,6 +568,7 @@ def time_to_se(eng, m, kind: str, probe_paths: int = 1 << 22) -> dict:
             "plain_path_steps_per_s": n_plain * steps / t_plain,
             "cv_paths": n_cv, "cv_s": t_cv, "cv_rel_se": res.price_std_err / res.price, "cv_train_s": tr.train_ms / 1e3,
             "cv_pilot_paths": int(tr.paths), "cv_iterations": int(cfg.iterations), "cv_batch_paths": int(cfg.batch_paths),
+            "cv_hedge_every": int(cfg.hedge_every),
             "variance_ratio": res.variance_ratio, "speedup": t_plain / t_cv,
             "price_cv": res.price, "price_plain": float(raw[0, 0])}
 

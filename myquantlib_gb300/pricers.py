@@ -756,18 +756,26 @@ class ControlVariateConfig:
     seed: int = 1
 
     @classmethod
-    def for_plain_time(cls, plain_seconds: float, **kw) -> "ControlVariateConfig":
-        """A training budget sized to the job: `plain_seconds` is the estimated time of plain
-        Monte Carlo to the wanted standard error.  Training is a fixed cost and its variance
-        ratio grows slowly with it (Double Bates Asian, 256 steps, GB300: ratio 7.8 after 15
-        Adam steps of 2048 paths on 2^15 pilot paths in 3 ms, 17.6 after 120 steps of 4096 on
-        2^19 in 18 ms), so a short job gets the short training and a long one the full one."""
+    def for_plain_time(cls, plain_seconds: float, time_steps: int | None = None, **kw) -> "ControlVariateConfig":
+        """A training budget and hedging interval sized to the job: `plain_seconds` is the
+        estimated time of plain Monte Carlo to the wanted standard error, `time_steps` the
+        job's steps.  Training is a fixed cost and its variance ratio grows slowly with it
+        (Double Bates Asian, 256 steps, GB300: ratio 7.8 after 15 Adam steps of 2048 paths on
+        2^15 pilot paths in 3 ms, 17.6 after 120 steps of 4096 on 2^19 in 18 ms); hedge rows
+        cost MLP evaluations on every priced path.  So a short job gets the short training and
+        8 hedge times per path, a mid-size one 10, a long one the full training and 32.  Keyword
+        arguments override any field (an explicit hedge_every wins over time_steps)."""
         if plain_seconds < 0.05:
             budget = dict(pilot_paths=1 << 15, iterations=15, batch_paths=2048)
+            rows = 8
         elif plain_seconds < 0.5:
             budget = dict(pilot_paths=1 << 18, iterations=60, batch_paths=2048)
+            rows = 10
         else:
             budget = dict(pilot_paths=1 << 19, iterations=120, batch_paths=4096)
+            rows = 32
+        if time_steps is not None:
+            budget["hedge_every"] = max(1, int(time_steps) // rows)
         budget.update(kw)
         return cls(**budget)
 

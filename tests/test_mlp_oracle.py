@@ -53,3 +53,9 @@ def test_cv_training_budget_follows_the_plain_time():
     assert (light.hedge_every, light.seed, full.iterations) == (8, 7, 150)
     c = light.c()
     assert (c.pilot_paths, c.iterations, c.batch_paths) == (1 << 15, 15, 2048)
+    # hedge times per path: 8 for short jobs, 10 mid-size, 32 long
+    assert ControlVariateConfig.for_plain_time(0.02, time_steps=256).hedge_every == 32
+    assert ControlVariateConfig.for_plain_time(0.1, time_steps=100).hedge_every == 10
+    assert ControlVariateConfig.for_plain_time(2.0, time_steps=256).hedge_every == 8
+    assert ControlVariateConfig.for_plain_time(2.0, time_steps=16).hedge_every == 1
+    assert ControlVariateConfig.for_plain_time(0.02, time_steps=256, hedge_every=4).hedge_every == 4

@@ -661,11 +661,10 @@ def run_mlmc(args) -> dict:
         c.alpha, c.beta, c.adaptive_rates, c.seed, c.fd_bump, c.n_streams = 2.0, 1.0, 1, 42, 1e-4, 0
         return c
 
-    cvc = m.pricers.ControlVariateConfig(hedge_every=1, iterations=200, pilot_paths=1 << 16, batch_paths=4096,
-                                         learning_rate=3e-3, seed=7).c()
     eps = 1e-3 * price
     # warm-up (tables, streams, first launches)
-    eng.mlmc_cv_price(job, cfg(20 * eps), cvc)
+    eng.mlmc_cv_price(job, cfg(20 * eps), m.pricers.ControlVariateConfig(
+        hedge_every=1, iterations=10, pilot_paths=1 << 15, batch_paths=2048, learning_rate=3e-3, seed=7).c())
     # Each arm on three controller seeds: one run's allocation rests on pilot variance estimates
     # of rare barrier events, and a single noisy estimate on the finest level can triple its
     # path count, so one seed per arm compares allocations rather than estimators.
@@ -680,6 +679,10 @@ def run_mlmc(args) -> dict:
             _abi.check(eng.lib.myql_mlmc_price(eng.handle, m.pricers.C.byref(job.c), m.pricers.C.byref(c),
                                                m.pricers.C.byref(res_plain)))
             runs_plain.append((time.perf_counter() - t0, res_plain, None))
+        # the training budget follows plain MLMC's median time (the networks train on 32 steps)
+        cvc = m.pricers.ControlVariateConfig.for_plain_time(statistics.median(t for t, _, _ in runs_plain),
+                                                            time_steps=32, learning_rate=3e-3, seed=7).c()
+        for sd in seeds:
             c = cfg(eps)
             c.seed = sd
             t0 = time.perf_counter()
@@ -708,6 +711,8 @@ def run_mlmc(args) -> dict:
             "data": "synthetic",
             "config": {"workload": "MLMC Heston down-and-out put, SchemeNV, levels 2..10", "epsilon": eps,
                        "price": price, "controller_seeds": list(seeds),
+                       "cv_training": {"pilot_paths": int(cvc.pilot_paths), "iterations": int(cvc.iterations),
+                                       "batch_paths": int(cvc.batch_paths), "hedge_every": int(cvc.hedge_every)},
                        "value": "median over the seeds of the MLMC + CV wall time"},
             "plain": {"median_s": t_plain, "runs": arm(runs_plain, False)},
             "cv": {"median_s": t_cv, "runs": arm(runs_cv, True)},

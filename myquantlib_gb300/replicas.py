@@ -68,4 +68,35 @@ def allreduce_price(raw: np.ndarray, n_local: int, group=None) -> np.ndarray:
     return combine(mom.cpu().numpy(), n_local * world)
 
 
+def pool_estimates(prices, std_errs) -> tuple[float, float]:
+    """Inverse-variance pooling of independent unbiased estimates (for example one MLMC run per
+    replica on disjoint stream ranges): sum(p_i / se_i^2) / sum(1 / se_i^2), with standard error
+    1 / sqrt(sum(1 / se_i^2)).  An estimate with zero standard error is exact and returned as is."""
+    p = np.asarray(prices, dtype=np.float64)
+    se = np.asarray(std_errs, dtype=np.float64)
+    if p.shape != se.shape or p.size == 0:
+        raise ValueError("one standard error per estimate, at least one estimate")
+    if np.any(se < 0.0) or not np.all(np.isfinite(se)) or not np.all(np.isfinite(p)):
+        raise ValueError("finite estimates and non-negative standard errors")
+    exact = se == 0.0
+    if exact.any():
+        return float(p[exact][0]), 0.0
+    w = 1.0 / (se * se)
+    return float(np.sum(w * p) / np.sum(w)), float(1.0 / np.sqrt(np.sum(w)))
+
+
+def allreduce_estimate(price: float, std_err: float, group=None) -> tuple[float, float]:
+    """pool_estimates over every rank's (price, standard error) through torch.distributed."""
+    import torch
+    import torch.distributed as dist
+    world = dist.get_world_size(group)
+    mine = torch.tensor([price, std_err], dtype=torch.float64)
+    if dist.get_backend(group) == "nccl":
+        mine = mine.cuda()
+    allv = [torch.zeros_like(mine) for _ in range(world)]
+    dist.all_gather(allv, mine, group=group)
+    allv = torch.stack(allv).cpu().numpy()
+    return pool_estimates(allv[:, 0], allv[:, 1])
+
+
 assert _abi.Q_COUNT == 10

@@ -88,3 +88,62 @@ def test_combine_is_compute_stats():
     pooled = replicas.combine(mom, 1000)
     np.testing.assert_allclose(pooled[0::2, 0], x.mean(1), rtol=1e-12)
     np.testing.assert_allclose(pooled[1::2, 0], np.sqrt(x.var(1) / 1000), rtol=1e-10)
+
+
+def test_pool_estimates():
+    """Inverse-variance pooling of independent estimates: weights 1/se^2, pooled SE
+    1/sqrt(sum 1/se^2); equal SEs give the plain mean and SE / sqrt(n)."""
+    p, se = replicas.pool_estimates([1.0, 2.0], [0.1, 0.2])
+    w = np.array([100.0, 25.0])
+    assert abs(p - (w @ [1.0, 2.0]) / w.sum()) < 1e-15 and abs(se - 1 / np.sqrt(w.sum())) < 1e-15
+    p, se = replicas.pool_estimates([3.0, 5.0, 7.0, 9.0], [0.4] * 4)
+    assert abs(p - 6.0) < 1e-14 and abs(se - 0.2) < 1e-15
+    assert replicas.pool_estimates([4.0, 2.5], [0.3, 0.0]) == (2.5, 0.0)
+    for bad in (([], []), ([1.0], [0.1, 0.2]), ([1.0], [-0.1]), ([np.nan], [0.1])):
+        with pytest.raises(ValueError):
+            replicas.pool_estimates(*bad)
+
+
+def _mlmc_cfg(seed):
+    from myquantlib_gb300 import _abi
+    c = _abi.MlmcConfigC()
+    c.epsilon, c.L_min, c.L_max, c.N0, c.base_steps = 0.05, 2, 5, 2000, 1
+    c.alpha, c.beta, c.adaptive_rates, c.seed, c.fd_bump, c.n_streams = 2.0, 1.0, 1, seed, 1e-4, 0
+    return c
+
+
+def _mlmc_job():
+    return m.make_job(m.HestonModel(m.HestonParams(1.5, 0.04, 0.3, -0.7, 0.04)), m.HestonStepper(m.SchemeNV),
+                      m.EuropeanOption(100.0, 1.0), m.GreekMode.NONE, m.MonteCarloConfig(), 100.0, 0.02, 0.0)
+
+
+def _mlmc_rank(rank, world, port, out_q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        from oracle import oracle
+        r = oracle.mlmc_price(_mlmc_job(), _mlmc_cfg(42 + rank), oracle.LAYOUT_REFERENCE, 1)
+        out_q.put((rank, replicas.allreduce_estimate(r.price, r.price_std_err)))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_rank_mlmc_estimates_pool(oracle_lib):
+    """Two CPU ranks each run an independent MLMC estimate (own controller seed) and pool them
+    by inverse variance through one all-gather; every rank gets the pooled estimate of both."""
+    world = 2
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_mlmc_rank, args=(r, world, port, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    got = [q.get(timeout=120) for _ in range(world)]
+    for p in procs:
+        p.join(60)
+        assert p.exitcode == 0
+    runs = [oracle_lib.mlmc_price(_mlmc_job(), _mlmc_cfg(42 + r), oracle_lib.LAYOUT_REFERENCE, 1) for r in range(world)]
+    want = replicas.pool_estimates([r.price for r in runs], [r.price_std_err for r in runs])
+    for _, (p, se) in got:
+        assert abs(p - want[0]) < 1e-12 * abs(want[0]) and abs(se - want[1]) < 1e-12 * want[1]
+    assert want[1] < min(r.price_std_err for r in runs)

@@ -206,6 +206,17 @@ myql_status myql_ctx_set_loop_cap(myql_ctx *ctx, uint32_t max_loop_iters);
  * rounds; results do not depend on the chunking. */
 myql_status myql_ctx_set_records_limit(myql_ctx *ctx, uint64_t bytes);
 
+/* SchemeNCI table cells (VolSchemes.hpp:240-313).  mode 0 (default): the
+ * reference's cells.  The cubic of the first cell runs from the node y(0) = 0,
+ * while for many degrees of freedom the quantile is near y(dx) on almost all of
+ * [0, dx].  So the cells' mean of the chi-squared draw falls short by 1.5e-5 to
+ * 4e-5 relative (rows 25 to 1000).  Over hundreds of steps this becomes a price
+ * bias of 0.2 to 1.6 % at 800 steps a year; through rho / sigma (v' - v) in the
+ * log-spot step its sign is that of -rho.  mode 1: exact slopes 1 / f(y) and a
+ * first cell that keeps the exact mean of its sliver, so the cells integrate to
+ * the mean within about 1e-8.  Tables are cached per mode. */
+myql_status myql_ctx_set_nci_slopes(myql_ctx *ctx, int mode);
+
 /* Host-side validation of a job, without a device: the checks myql_mc_price
  * runs before any launch (MYQL_ERR_NV_CONDITION for SchemeNV with
  * sigma^2 > 4 kappa theta, as VolSchemes.hpp:40-41 throws). */

@@ -113,6 +113,7 @@ _SIGS = {
     "myql_ctx_destroy": (C.c_int, [C.c_void_p]),
     "myql_ctx_set_loop_cap": (C.c_int, [C.c_void_p, C.c_uint32]),
     "myql_ctx_set_records_limit": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "myql_ctx_set_nci_slopes": (C.c_int, [C.c_void_p, C.c_int]),
     "myql_validate_job": (C.c_int, [C.POINTER(McJobC)]),
     "myql_mc_price": (C.c_int, [C.c_void_p, C.POINTER(McJobC), C.POINTER(C.c_double),
                                 C.POINTER(McStatsC)]),

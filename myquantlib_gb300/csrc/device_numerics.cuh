@@ -480,7 +480,13 @@ __device__ __forceinline__ int poisson_inv(float lam, unsigned long long x, unsi
 }
 
 // Poisson draw by sequential inversion, as boost::random::poisson_distribution
-// does for means below 10: one uniform_01 draw, subtract pmf terms.
+// does for means below 10: one uniform_01 draw, subtract pmf terms.  In FP32 the
+// subtractions leave u a few 1e-8 above the true remainder, so for u within
+// about 1e-7 of 1 the remainder can stay above every later term and the loop
+// would only end at the cap.  Past the mode, once a term is below 1e-9 the
+// remaining mass is too (below the FP32 resolution of u), so the draw is in
+// the last 1e-8 of the distribution and k is returned; a draw that stops by
+// the ordinary test never gets there (its last term is at least about 1e-8).
 __device__ __forceinline__ int poisson_small(float mean, float exp_neg_mean, Xo &rng,
                                              unsigned int cap, unsigned int &caphits) {
   float u = u01_bits(draw(rng));
@@ -491,6 +497,7 @@ __device__ __forceinline__ int poisson_small(float mean, float exp_neg_mean, Xo 
       ++caphits;
       break;
     }
+    if (p < 1.0e-9f && (float)k > mean) break;
     u -= p;
     ++k;
     p = __fdividef(mean * p, (float)k);

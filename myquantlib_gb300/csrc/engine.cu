@@ -29,7 +29,7 @@ cudaError_t launch_rng_draws(const unsigned long long *states, unsigned long lon
                              unsigned long long count, unsigned long long *out, cudaStream_t stream);
 cudaError_t launch_nci_build(double d, int rows, double *tmp_main, double *tmp_ty, double *tmp_tm,
                              float4 *cells_main, float4 *cells_tail, double w0, double dw,
-                             cudaStream_t stream);
+                             int exact_slopes, cudaStream_t stream);
 cudaError_t launch_nci_nodes(double d, int rows, double *tmp_main, double *tmp_ty, double *tmp_tm,
                              double w0, double dw, cudaStream_t stream);
 cudaError_t launch_chi2_probe(const double *dof, const double *p, double *out, size_t n,
@@ -548,7 +548,8 @@ myql_status ensure_nci(CtxBase *ctx, const myql_heston_params &p, double dt_min,
   const double d = 4.0 * p.kappa * p.theta / (p.sigma * p.sigma);
   const int rows = nci_rows_wanted(p, dt_min);
   uint64_t key;
-  std::memcpy(&key, &d, sizeof key);
+  std::memcpy(&key, &d, sizeof key);  // d > 0: the sign bit is free for the slope rule
+  if (ctx->nci_slopes) key |= 1ull << 63;
   auto it = ctx->nci.find(key);
   if (it == ctx->nci.end() || it->second.rows < rows) {
     if (it != ctx->nci.end()) {
@@ -573,7 +574,7 @@ myql_status ensure_nci(CtxBase *ctx, const myql_heston_params &p, double dt_min,
     const double w0 = -std::log1p(-kNciUmax);
     const double dw = (kNciTailWmax - w0) / (kNciTail - 1);
     e = launch_nci_build(d, rows, tm, tm + nm, tm + nm + nt, (float4 *)ent.main.p,
-                         (float4 *)ent.tail.p, w0, dw, ctx->stream);
+                         (float4 *)ent.tail.p, w0, dw, ctx->nci_slopes, ctx->stream);
     ctx->launches += 4;
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     tmp.release();
@@ -783,6 +784,13 @@ myql_status myql_ctx_set_loop_cap(myql_ctx *ctx, uint32_t cap) {
 myql_status myql_ctx_set_records_limit(myql_ctx *ctx, uint64_t bytes) {
   if (!ctx) return set_error(MYQL_ERR_INVALID_ARG, "null context");
   ctx->records_cap_bytes = bytes ? bytes : (2ull << 30);
+  return MYQL_OK;
+}
+
+myql_status myql_ctx_set_nci_slopes(myql_ctx *ctx, int mode) {
+  if (!ctx) return set_error(MYQL_ERR_INVALID_ARG, "null context");
+  if (mode != 0 && mode != 1) return set_error(MYQL_ERR_INVALID_ARG, "NCI slope mode is 0 or 1");
+  ctx->nci_slopes = mode;
   return MYQL_OK;
 }
 

@@ -202,13 +202,46 @@ __device__ __forceinline__ float4 hermite_cell(double y0, double y1, double hm0,
                      (float)(2.0 * (y0 - y1) + (hm0 + hm1)));
 }
 
-__global__ void nci_cells_main_kernel(int rows, const double *y, double dx, float4 *cells) {
+// Exact slope dy/dU = 1 / f(y) of the quantile function at an interior node
+// (f the chi-squared density with nu degrees of freedom); the first node keeps
+// the secant, since the derivative is 0 or unbounded at U = 0.
+__device__ __forceinline__ double nci_exact_slope(const double *yr, int i, double nu, double inv_dx) {
+  if (i == 0) return (yr[1] - yr[0]) * inv_dx;
+  return exp(-chi2_logpdf(nu, yr[i]));
+}
+
+// exact 0: the reference's cells (harmonic-mean slopes, the first cell a
+// Hermite cubic from the node y(0) = 0).  Their integral falls short of the
+// conditional mean d + 2k by 1.5e-5 to 4e-5 relative for rows k >= 25, almost
+// all of it in the first cell: for many degrees of freedom the quantile rises
+// from 0 to near y(dx) within a sliver of U, which a cubic from y(0) = 0 misses.
+// exact 1: exact slopes 1 / f(y) at the nodes, and, for rows k >= 4, a first
+// cell c(t) = y1 + h m1 (t - 1) + q (t - 1)^2 whose integral is the exact mean
+// of the quantile over [0, dx], nu P(nu/2 + 1, y1/2) / dx: the cells then
+// integrate to the mean within about 1e-8 relative.
+__global__ void nci_cells_main_kernel(int rows, const double *y, double dx, float4 *cells, double d,
+                                      int exact) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (long long)rows * (kNciGrid - 1)) return;
   const int k = (int)(idx / (kNciGrid - 1)), i = (int)(idx % (kNciGrid - 1));
   const double *yr = y + (size_t)k * kNciGrid;
   const double inv_dx = 1.0 / dx;
-  const double m0 = nci_slope(yr, i, inv_dx), m1 = nci_slope(yr, i + 1, inv_dx);
+  double m0, m1;
+  if (exact) {
+    const double nu = d + 2.0 * k;
+    m0 = nci_exact_slope(yr, i, nu, inv_dx);
+    m1 = nci_exact_slope(yr, i + 1, nu, inv_dx);
+    if (i == 0 && k >= 4) {
+      const double a = 0.5 * nu + 1.0, y1 = yr[1], hm1 = dx * m1;
+      const double mean = nu * exp(gamma_eval(a, 0.5 * y1, lgamma(a)).logP) * inv_dx;
+      const double q = 3.0 * (mean - y1 + 0.5 * hm1);
+      cells[idx] = make_float4((float)(y1 - hm1 + q), (float)(hm1 - 2.0 * q), (float)q, 0.0f);
+      return;
+    }
+  } else {
+    m0 = nci_slope(yr, i, inv_dx);
+    m1 = nci_slope(yr, i + 1, inv_dx);
+  }
   cells[idx] = hermite_cell(yr[i], yr[i + 1], dx * m0, dx * m1);
 }
 
@@ -272,12 +305,13 @@ cudaError_t launch_nci_nodes(double d, int rows, double *tmp_main, double *tmp_t
 
 cudaError_t launch_nci_build(double d, int rows, double *tmp_main, double *tmp_ty, double *tmp_tm,
                              float4 *cells_main, float4 *cells_tail, double w0, double dw,
-                             cudaStream_t stream) {
+                             int exact, cudaStream_t stream) {
   const double dx = kNciUmax / (kNciGrid - 1);
   cudaError_t e = launch_nci_nodes(d, rows, tmp_main, tmp_ty, tmp_tm, w0, dw, stream);
   if (e != cudaSuccess) return e;
   const long long cm = (long long)rows * (kNciGrid - 1), ct = (long long)rows * (kNciTail - 1);
-  dev::nci_cells_main_kernel<<<(unsigned int)((cm + 255) / 256), 256, 0, stream>>>(rows, tmp_main, dx, cells_main);
+  dev::nci_cells_main_kernel<<<(unsigned int)((cm + 255) / 256), 256, 0, stream>>>(rows, tmp_main, dx, cells_main,
+                                                                                   d, exact);
   dev::nci_cells_tail_kernel<<<(unsigned int)((ct + 255) / 256), 256, 0, stream>>>(rows, tmp_ty, tmp_tm, dw, cells_tail);
   return cudaGetLastError();
 }

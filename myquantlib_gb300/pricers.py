@@ -435,6 +435,11 @@ class Engine:
     def set_records_limit(self, nbytes: int):
         _abi.check(self.lib.myql_ctx_set_records_limit(self.handle, nbytes))
 
+    def set_nci_slopes(self, mode: int):
+        """SchemeNCI table cells: 0 the reference's (default), 1 exact slopes and a first cell
+        that keeps its exact mean, so the draw's conditional mean is unbiased."""
+        _abi.check(self.lib.myql_ctx_set_nci_slopes(self.handle, int(mode)))
+
     def price(self, job: "_Job") -> tuple[np.ndarray, _abi.McStatsC]:
         out = np.zeros(2 * _abi.Q_COUNT * job.n_strikes, dtype=np.float64)
         st = _abi.McStatsC()

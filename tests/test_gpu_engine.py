@@ -119,6 +119,44 @@ def test_device_nci_nodes(engine, d, rows):
     assert rel_t.max() < 1e-11, (rel_t.max(), np.unravel_index(rel_t.argmax(), rel_t.shape))
 
 
+def test_jump_count_tail_draws_end_without_the_cap(engine):
+    """A Merton jump count drawn by sequential inversion from a uniform within about 1e-7 of 1
+    runs to the loop cap in FP32 (the remainder stays above every later term) unless the
+    inversion stops in the deep tail.  The Bates strip's T = 1.5 request on seed 43 (2^22 paths,
+    5 simulated scenarios) holds such draws: it must price without a cap hit."""
+    model = m.BatesModel(m.HestonParams(2.0, 0.05, 0.9, -0.6, 0.05), m.MertonParams(0.5, -0.1, 0.15))
+    cfg = m.MonteCarloConfig(num_paths=1 << 22, time_steps=300, seed=43)
+    job = m.make_job(model, m.BatesStepper(m.SchemeNCI), m.EuropeanOption([80.0, 100.0, 120.0], 1.5),
+                     m.GreekMode.FULL, cfg, 100.0, 0.02, 0.0)
+    raw, st = engine.price(job)
+    assert st.loop_cap_hits == 0
+    assert np.all(np.isfinite(raw))
+
+
+def test_nci_exact_slopes_remove_the_table_mean_bias(engine):
+    """The reference's NCI cells bias the chi-squared draw's mean low (mostly in the first cell,
+    a cubic from the node y(0) = 0), and the log-spot step turns that into a price bias of sign
+    -rho that grows with the step count.  Heston (rho = 0.6, sigma^2 > 4 kappa theta), T = 2 at
+    800 steps a year, 2^22 paths: with the reference's cells the strikes' mean z against the
+    FP64 Fourier price is far below zero (about -7.5 on seeds 42-44); with mode 1 (exact slopes,
+    mean-preserving first cell) it is within the noise of a few correlated SEs."""
+    model = m.HestonModel(m.HestonParams(2.0, 0.05, 0.9, 0.6, 0.05))
+    cfg = m.MonteCarloConfig(num_paths=1 << 22, time_steps=1600, seed=42)
+    job = m.make_job(model, m.HestonStepper(m.SchemeNCI), m.EuropeanOption([80.0, 90.0, 100.0, 110.0, 120.0], 2.0),
+                     m.GreekMode.NONE, cfg, 100.0, 0.02, 0.0)
+    four = engine.fourier(job, m.GreekMode.NONE)[0]
+    zs = []
+    for mode in (0, 1):
+        engine.set_nci_slopes(mode)
+        try:
+            raw, _ = engine.price(job)
+        finally:
+            engine.set_nci_slopes(0)
+        zs.append(float(np.mean((raw[0] - four) / raw[1])))
+    assert zs[0] < -4.0, zs
+    assert abs(zs[1]) < 3.0, zs
+
+
 def base_spec():
     return jobspec.with_config(MC_SPECS["c1_heston_nv_call"], paths=50000, steps=50, streams=1024)
 

@@ -323,7 +323,7 @@ def run_engine(args) -> dict:
                     "d2h_bytes_per_step": 8 * 2 * 10 * nk * len(jobs)},
             "gpu_launches": launches_per_step * args.steps, "roofline": roof, "clocks": clk.summary()}
     # every price and Greek of the strip against the FP64 Gil-Pelaez oracle (z = error / SE)
-    try:
+    def fourier_check():
         zmax, zall = {}, []
         for j in jobs:
             raw, _ = eng.price(j)
@@ -337,12 +337,20 @@ def run_engine(args) -> dict:
                 zmax[name] = max(zmax.get(name, 0.0), float(z.max()))
                 zall.append(z)
         zall = np.concatenate(zall)
-        # a correct estimator leaves about 0.27 % of |z| above 3 (the strikes share paths, so the
-        # z of one maturity are correlated and the fraction is noisier than for independent tests)
-        line["fourier_check"] = {"max_abs_z": zmax, "options": len(jobs) * nk, "comparisons": int(zall.size),
-                                 "frac_abs_z_above_3": float(np.mean(zall > 3.0)),
-                                 "frac_abs_z_above_2": float(np.mean(zall > 2.0)),
-                                 "oracle": "FP64 Gil-Pelaez on the GPU (myql_fourier_price)"}
+        # a correct estimator leaves about 0.27 % of |z| above 3; the strikes and maturities share
+        # paths, so the z are correlated and the fractions are noisier than for independent tests
+        return {"max_abs_z": zmax, "options": len(jobs) * nk, "comparisons": int(zall.size),
+                "frac_abs_z_above_3": float(np.mean(zall > 3.0)), "frac_abs_z_above_2": float(np.mean(zall > 2.0)),
+                "oracle": "FP64 Gil-Pelaez on the GPU (myql_fourier_price)"}
+
+    try:
+        line["fourier_check"] = dict(fourier_check(), nci_cells="the reference's")
+        # the same with the opt-in NCI tables whose cells keep the exact chi-squared mean
+        eng.set_nci_slopes(1)
+        try:
+            line["fourier_check_exact_nci"] = dict(fourier_check(), nci_cells="exact slopes, mean-preserving first cell")
+        finally:
+            eng.set_nci_slopes(0)
     except Exception as exc:  # the oracle is a report, not the measurement
         line["fourier_check"] = {"error": str(exc)}
     if world == 1 and not args.no_cpu:

@@ -448,6 +448,25 @@ def run_ncu_c1_case() -> None:
         eng.price(job)
 
 
+def run_ncu_mlmc_case() -> None:
+    """Profiling case of the MLMC workload: two evaluations of level 6 (64 fine steps) of the
+    Heston down-and-out put with 2^20 coupled paths, no timing."""
+    import ctypes as C
+    import myquantlib_gb300 as m
+    from myquantlib_gb300 import _abi
+    eng = m.Engine(0)
+    model = m.HestonModel(m.HestonParams(2.0, 0.04, 0.5, -0.7, 0.04))
+    job = m.make_job(model, m.HestonStepper(m.SchemeNV, m.TrackerBarrier), m.DownAndOutPut(100.0, 80.0, 1.0),
+                     m.GreekMode.NONE, m.MonteCarloConfig(), 100.0, 0.02, 0.0)
+    c = _abi.MlmcConfigC()
+    c.epsilon, c.L_min, c.L_max, c.N0, c.base_steps = 1e-3, 2, 10, 10000, 1
+    c.alpha, c.beta, c.adaptive_rates, c.seed, c.fd_bump, c.n_streams = 2.0, 1.0, 1, SEED, 1e-4, 0
+    out = np.zeros(4)
+    for _ in range(2):
+        _abi.check(eng.lib.myql_mlmc_level(eng.handle, C.byref(job.c), C.byref(c), 6, 1 << 20,
+                                           out.ctypes.data_as(C.POINTER(C.c_double))))
+
+
 def run_batch(args) -> dict:
     """Batched uneven requests (4096 jobs, myquantlib_gb300.workloads.uneven_requests) in one
     persistent launch per step.  value: path-steps / device time of the batch graph (descriptor
@@ -792,6 +811,8 @@ def main():
             run_ncu_batch_case()
         elif args.workload == "c1":
             run_ncu_c1_case()
+        elif args.workload == "mlmc":
+            run_ncu_mlmc_case()
         else:
             run_ncu_case(full=args.ncu_full)
         return

@@ -534,6 +534,15 @@ template <typename T> T pick(const std::vector<double> &out, int q, int se, size
 // Selects the GPU the calling thread's pricers run on.
 inline void set_device(int device) { detail::thread_device() = device; }
 
+// SchemeNCI table cells of this thread's context: false (default) the reference's
+// (VolSchemes.hpp:240-313), true cells that keep the exact chi-squared mean (the
+// reference's first cell shortens it, which long, finely stepped paths turn into a
+// price bias; see myql_ctx_set_nci_slopes).
+inline void set_exact_nci_tables(bool on) {
+  const myql_status s = myql_ctx_set_nci_slopes(detail::context(), on ? 1 : 0);
+  if (s != MYQL_OK) detail::raise(s);
+}
+
 // ---------------------------------------------------------------- pricers
 template <typename Model, typename Stepper, typename Instrument, GreekMode Mode = GreekMode::None>
 class MonteCarloPricer {

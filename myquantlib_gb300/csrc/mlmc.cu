@@ -194,9 +194,10 @@ static myql_status mlmc_run(myql_ctx *ctx_, const myql_mc_job *job_in, const myq
   const double df = std::exp(-job.r * T);
   const size_t L_max = cfg->L_max;
 
-  // persistent stream pool (seed, streams 0..S-1)
+  // persistent stream pool: seed, streams [offset, offset + S) with the job's stream offset
+  // (0 for a single controller; replicas and the multi-rank controller give disjoint blocks)
   const uint64_t S = cfg->n_streams ? cfg->n_streams : kDefaultStreams;
-  s = ensure_streams(ctx, cfg->seed, 0, S);
+  s = ensure_streams(ctx, cfg->seed, job_in->config.stream_offset, S);
   if (s != MYQL_OK) return s;
   e = ctx->aux_a.ensure(S * 32);
   if (e == cudaSuccess)

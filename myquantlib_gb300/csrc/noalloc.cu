@@ -97,7 +97,9 @@ extern "C" myql_status myql_mc_price_noalloc(int device, const myql_mc_job *job,
   const myql_model &m = job->model;
   const myql_instrument &in = job->instrument;
   const uint64_t M = c.num_paths;
-  const uint64_t S = std::min<uint64_t>(c.n_streams ? c.n_streams : kDefaultStreams, M);
+  // the stream rule of myql_mc_price: the same streams, so the same paths and result
+  const uint64_t S = std::min<uint64_t>(c.n_streams ? c.n_streams : default_streams(M), M);
+  if (S > (1u << 26)) return set_error(MYQL_ERR_TOO_LARGE, "at most 2^26 streams");
   const int steps = (int)c.time_steps;
   const int tracker = tracker_of(in);
   const bool path_dep = tracker != TRK_EUROPEAN;

@@ -68,35 +68,45 @@ def allreduce_price(raw: np.ndarray, n_local: int, group=None) -> np.ndarray:
     return combine(mom.cpu().numpy(), n_local * world)
 
 
-def pool_estimates(prices, std_errs) -> tuple[float, float]:
-    """Inverse-variance pooling of independent unbiased estimates (for example one MLMC run per
-    replica on disjoint stream ranges): sum(p_i / se_i^2) / sum(1 / se_i^2), with standard error
-    1 / sqrt(sum(1 / se_i^2)).  An estimate with zero standard error is exact and returned as is."""
+def pool_estimates(prices, std_errs, weights=None) -> tuple[float, float]:
+    """Pools independent unbiased estimates (for example one MLMC run per replica on disjoint
+    stream ranges) with FIXED weights: the replicas' planned budgets (path counts or cost) when
+    given, equal weights otherwise.  Fixed weights keep the pooled estimate unbiased.  Weights
+    taken from each replica's own sample standard error would not: for option payoffs the
+    sample standard error grows with the sample mean, so 1/se^2 weights favour the low
+    estimates.  Pooled standard error: sqrt(sum w_i^2 se_i^2) / sum w_i.  A zero standard
+    error is accepted only when every replica reports it with the same price (a
+    deterministic payoff); otherwise it is an error, not an exact estimate."""
     p = np.asarray(prices, dtype=np.float64)
     se = np.asarray(std_errs, dtype=np.float64)
     if p.shape != se.shape or p.size == 0:
         raise ValueError("one standard error per estimate, at least one estimate")
     if np.any(se < 0.0) or not np.all(np.isfinite(se)) or not np.all(np.isfinite(p)):
         raise ValueError("finite estimates and non-negative standard errors")
-    exact = se == 0.0
-    if exact.any():
-        return float(p[exact][0]), 0.0
-    w = 1.0 / (se * se)
-    return float(np.sum(w * p) / np.sum(w)), float(1.0 / np.sqrt(np.sum(w)))
+    w = np.ones_like(p) if weights is None else np.asarray(weights, dtype=np.float64)
+    if w.shape != p.shape or np.any(w <= 0.0) or not np.all(np.isfinite(w)):
+        raise ValueError("one positive weight per estimate")
+    if np.any(se == 0.0):
+        if np.all(se == 0.0) and np.all(p == p[0]):
+            return float(p[0]), 0.0
+        raise ValueError("a replica reported a zero standard error that the others do not share")
+    return float(np.sum(w * p) / np.sum(w)), float(np.sqrt(np.sum(w * w * se * se)) / np.sum(w))
 
 
-def allreduce_estimate(price: float, std_err: float, group=None) -> tuple[float, float]:
-    """pool_estimates over every rank's (price, standard error) through torch.distributed."""
+def allreduce_estimate(price: float, std_err: float, weight: float = 1.0, group=None) -> tuple[float, float]:
+    """pool_estimates over every rank's (price, standard error, planned budget) through
+    torch.distributed (one all-gather).  For MLMC, mlmc_ranks runs one controller over all ranks
+    instead; this pools runs that were planned independently."""
     import torch
     import torch.distributed as dist
     world = dist.get_world_size(group)
-    mine = torch.tensor([price, std_err], dtype=torch.float64)
+    mine = torch.tensor([price, std_err, weight], dtype=torch.float64)
     if dist.get_backend(group) == "nccl":
         mine = mine.cuda()
     allv = [torch.zeros_like(mine) for _ in range(world)]
     dist.all_gather(allv, mine, group=group)
     allv = torch.stack(allv).cpu().numpy()
-    return pool_estimates(allv[:, 0], allv[:, 1])
+    return pool_estimates(allv[:, 0], allv[:, 1], allv[:, 2])
 
 
 assert _abi.Q_COUNT == 10

@@ -1471,6 +1471,7 @@ int myql_oracle_mlmc_price(const myql_mc_job *job_in, const myql_mlmc_config *cf
   } else {
     R.pool = (xo_t *)malloc(sizeof(xo_t) * R.S);
     xo_seed(&R.pool[0], cfg->seed);
+    for (uint64_t k = 0; k < job_in->config.stream_offset; ++k) xo_jump(&R.pool[0]); /* first stream */
     for (uint64_t k = 1; k < R.S; ++k) {
       R.pool[k] = R.pool[k - 1];
       xo_jump(&R.pool[k]);
@@ -1593,6 +1594,8 @@ int myql_oracle_mlmc_level(const myql_mc_job *job_in, const myql_mlmc_config *cf
     const uint64_t U = R.S < dN ? R.S : dN;
     R.pool = (xo_t *)malloc(sizeof(xo_t) * R.S);
     xo_seed(&R.pool[0], cfg->seed);
+    /* streams [offset, offset + S): the job's stream offset, as the GPU level evaluator */
+    for (uint64_t k = 0; k < job_in->config.stream_offset; ++k) xo_jump(&R.pool[0]);
     for (uint64_t k = 1; k < U; ++k) {
       R.pool[k] = R.pool[k - 1];
       xo_jump(&R.pool[k]);

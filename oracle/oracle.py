@@ -33,7 +33,7 @@ def build(ref: bool | None = None) -> None:
     if ref is None:
         ref = (REF_ROOT / "include" / "myql").exists()
     if ref:
-        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF_ROOT={REF_ROOT}"], check=True)
+        subprocess.run(["make", "-s", "-j2", "-C", str(HERE), "ref", f"REF_ROOT={REF_ROOT}"], check=True)
 
 
 def _load(name: str) -> C.CDLL:

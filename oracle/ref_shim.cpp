@@ -5,7 +5,10 @@
 //
 // The reference is a set of templates; this file instantiates the
 // configurations the tests and the CPU baseline use and picks one at run time
-// from a myql_mc_job.  Unlisted combinations return -2.
+// from a myql_mc_job.  Heston SchemeNV and Black-Scholes get every instrument
+// branch (Asian and lookback fixed/floating x call/put, barrier up/down x
+// in/out x call/put x rebate timing); the other stepper families get the
+// combinations the workloads use.  Unlisted combinations return -2.
 #include <omp.h>
 
 #include <cmath>
@@ -134,7 +137,10 @@ int european_any(const Model &model, const myql_mc_job &j, double *out) {
               : european<Model, St, PayoffAssetOrNothing<OptionType::Put>>(model, j, out);
 }
 
-// Path-dependent scalar vanilla instruments over a stepper family.
+// Path-dependent scalar vanilla instruments over a stepper family: the
+// combinations the batched and strip workloads use (fixed-strike Asian calls,
+// floating lookback calls, up-and-out calls and down-and-out puts without
+// rebate).  exotic_all below instantiates every branch for two families.
 template <class Model, class V1, class V2, class Jump>
 int exotic_any(const Model &model, const myql_mc_job &j, double *out) {
   const auto &in = j.instrument;
@@ -174,6 +180,100 @@ int exotic_any(const Model &model, const myql_mc_job &j, double *out) {
       }
       return -2;
     }
+    default: return -2;
+  }
+}
+
+// ---- every instrument branch of Asian.hpp, Lookback.hpp and Barrier.hpp
+
+// AsianOption<Tracker, Payoff, FixedStrike> (Asian.hpp:7-131) with its in-flight
+// constructor: arithmetic (:63-69) or geometric (:53-57).
+template <class Model, class V1, class V2, class Jump, class Trk, class Pay, bool Fixed>
+int asian_one(const Model &model, const myql_mc_job &j, double *out) {
+  using St = ASVJStepper<V1, V2, Jump, Trk>;
+  const auto &in = j.instrument;
+  if constexpr (std::is_same_v<Trk, TrackerArithAsian>) {
+    AsianOption<Trk, Pay, Fixed> opt(in.strikes[0], in.maturity, in.past_avg_S, in.past_avg_log, in.t_elapsed);
+    return run_mode<Model, St, decltype(opt)>(model, opt, j, out);
+  } else {
+    AsianOption<Trk, Pay, Fixed> opt(in.strikes[0], in.maturity, in.past_avg_log, in.t_elapsed);
+    return run_mode<Model, St, decltype(opt)>(model, opt, j, out);
+  }
+}
+
+template <class Model, class V1, class V2, class Jump, class Trk>
+int asian_all(const Model &model, const myql_mc_job &j, double *out) {
+  const bool call = j.instrument.option_type == MYQL_CALL, fixed = j.instrument.fixed_strike != 0;
+  if (fixed)
+    return call ? asian_one<Model, V1, V2, Jump, Trk, CallV, true>(model, j, out)
+                : asian_one<Model, V1, V2, Jump, Trk, PutV, true>(model, j, out);
+  return call ? asian_one<Model, V1, V2, Jump, Trk, CallV, false>(model, j, out)
+              : asian_one<Model, V1, V2, Jump, Trk, PutV, false>(model, j, out);
+}
+
+// LookbackOption<Payoff, FixedStrike> (Lookback.hpp:8-110) with historical extremes.
+template <class Model, class V1, class V2, class Jump, class Pay, bool Fixed>
+int lookback_one(const Model &model, const myql_mc_job &j, double *out) {
+  using St = ASVJStepper<V1, V2, Jump, TrackerLookback>;
+  const auto &in = j.instrument;
+  LookbackOption<Pay, Fixed> opt(in.strikes[0], in.maturity, in.hist_min_S, in.hist_max_S);
+  return run_mode<Model, St, decltype(opt)>(model, opt, j, out);
+}
+
+template <class Model, class V1, class V2, class Jump>
+int lookback_all(const Model &model, const myql_mc_job &j, double *out) {
+  const bool call = j.instrument.option_type == MYQL_CALL, fixed = j.instrument.fixed_strike != 0;
+  if (fixed)
+    return call ? lookback_one<Model, V1, V2, Jump, CallV, true>(model, j, out)
+                : lookback_one<Model, V1, V2, Jump, PutV, true>(model, j, out);
+  return call ? lookback_one<Model, V1, V2, Jump, CallV, false>(model, j, out)
+              : lookback_one<Model, V1, V2, Jump, PutV, false>(model, j, out);
+}
+
+// BarrierOption<Payoff, Dir, Action, Timing> (Barrier.hpp:17-124): up/down x
+// in/out x call/put x rebate {None, AtHit, AtMaturity}.
+template <class Model, class V1, class V2, class Jump, class Pay, BarrierDirection D, BarrierAction A,
+          RebateTiming R>
+int barrier_one(const Model &model, const myql_mc_job &j, double *out) {
+  using Opt = BarrierOption<Pay, D, A, R>;
+  using St = ASVJStepper<V1, V2, Jump, typename Opt::Tracker>;
+  const auto &in = j.instrument;
+  Opt opt(in.strikes[0], in.barrier, in.maturity, in.barrier_rate, in.rebate);
+  return run_mode<Model, St, Opt>(model, opt, j, out);
+}
+
+template <class Model, class V1, class V2, class Jump, class Pay, BarrierDirection D, BarrierAction A>
+int barrier_rebate(const Model &model, const myql_mc_job &j, double *out) {
+  switch (j.instrument.rebate_timing) {
+    case MYQL_REBATE_NONE: return barrier_one<Model, V1, V2, Jump, Pay, D, A, RebateTiming::None>(model, j, out);
+    case MYQL_REBATE_AT_HIT: return barrier_one<Model, V1, V2, Jump, Pay, D, A, RebateTiming::AtHit>(model, j, out);
+    default: return barrier_one<Model, V1, V2, Jump, Pay, D, A, RebateTiming::AtMaturity>(model, j, out);
+  }
+}
+
+template <class Model, class V1, class V2, class Jump, class Pay>
+int barrier_all_pay(const Model &model, const myql_mc_job &j, double *out) {
+  const auto &in = j.instrument;
+  constexpr auto Up = BarrierDirection::Up, Dn = BarrierDirection::Down;
+  constexpr auto In = BarrierAction::In, Out = BarrierAction::Out;
+  if (in.barrier_up)
+    return in.barrier_action == MYQL_BARRIER_OUT ? barrier_rebate<Model, V1, V2, Jump, Pay, Up, Out>(model, j, out)
+                                                 : barrier_rebate<Model, V1, V2, Jump, Pay, Up, In>(model, j, out);
+  return in.barrier_action == MYQL_BARRIER_OUT ? barrier_rebate<Model, V1, V2, Jump, Pay, Dn, Out>(model, j, out)
+                                               : barrier_rebate<Model, V1, V2, Jump, Pay, Dn, In>(model, j, out);
+}
+
+template <class Model, class V1, class V2, class Jump>
+int exotic_all(const Model &model, const myql_mc_job &j, double *out) {
+  const auto &in = j.instrument;
+  if (in.is_strip || in.payoff != MYQL_PAYOFF_VANILLA) return -2;
+  switch (in.kind) {
+    case MYQL_INSTR_ASIAN_ARITH: return asian_all<Model, V1, V2, Jump, TrackerArithAsian>(model, j, out);
+    case MYQL_INSTR_ASIAN_GEO: return asian_all<Model, V1, V2, Jump, TrackerGeoAsian>(model, j, out);
+    case MYQL_INSTR_LOOKBACK: return lookback_all<Model, V1, V2, Jump>(model, j, out);
+    case MYQL_INSTR_BARRIER:
+      return in.option_type == MYQL_CALL ? barrier_all_pay<Model, V1, V2, Jump, CallV>(model, j, out)
+                                         : barrier_all_pay<Model, V1, V2, Jump, PutV>(model, j, out);
     default: return -2;
   }
 }
@@ -274,7 +374,7 @@ int myql_ref_mc_price(const myql_mc_job *jp, int n_threads, double *out) {
   if (is(j, 1, MYQL_SCHEME_NV, 0, MYQL_JUMP_NONE)) {
     HestonModel model(hp(m.heston[0]));
     return eur ? european_any<HestonModel, SchemeNV, NullVolScheme, NoJumps>(model, j, out)
-               : exotic_any<HestonModel, SchemeNV, NullVolScheme, NoJumps>(model, j, out);
+               : exotic_all<HestonModel, SchemeNV, NullVolScheme, NoJumps>(model, j, out);
   }
   if (is(j, 1, MYQL_SCHEME_EXACT, 0, MYQL_JUMP_NONE) && eur) {
     HestonModel model(hp(m.heston[0]));
@@ -308,7 +408,7 @@ int myql_ref_mc_price(const myql_mc_job *jp, int n_threads, double *out) {
   if (is(j, 0, 0, 0, MYQL_JUMP_NONE)) {
     BlackScholesModel model(m.vol);
     return eur ? european_any<BlackScholesModel, NullVolScheme, NullVolScheme, NoJumps>(model, j, out)
-               : exotic_any<BlackScholesModel, NullVolScheme, NullVolScheme, NoJumps>(model, j, out);
+               : exotic_all<BlackScholesModel, NullVolScheme, NullVolScheme, NoJumps>(model, j, out);
   }
   return -2;
 }

@@ -95,6 +95,59 @@ MC_SPECS = [
     {"name": "bs_downout_put_day0_breach", "model": {"vol": 0.25}, "schemes": [],
      "instrument": {"kind": "barrier", "dir": "down", "action": "out", "K": 100.0, "B": 100.5, "T": 1.0,
                     "type": "put"}, "mode": "essential", "config": {"paths": 2000, "steps": 20}},
+] + [
+    # every remaining instrument branch: floating-strike Asians and Asian puts
+    # (Asian.hpp:31-37), fixed-strike lookbacks and lookback puts (Lookback.hpp:22-33,
+    # 70-74), knock-in barriers and the AtHit / AtMaturity rebates (Barrier.hpp:29-45)
+    {"name": name, "model": model, "schemes": ["NV"] if "heston" in model else [], "instrument": ins,
+     "mode": mode, "config": {"paths": paths, "steps": steps}}
+    for name, model, ins, mode, paths, steps in [
+        ("heston_asian_arith_float_call", {"heston": [H1]},
+         {"kind": "asian_arith", "K": 100.0, "T": 1.0, "fixed": False}, "essential", 4000, 64),
+        ("heston_asian_arith_fixed_put", {"heston": [H1]},
+         {"kind": "asian_arith", "K": 100.0, "T": 1.0, "type": "put"}, "essential", 4000, 64),
+        ("heston_asian_geo_float_put_full", {"heston": [H1]},
+         {"kind": "asian_geo", "K": 100.0, "T": 1.0, "fixed": False, "type": "put"}, "full", 2000, 50),
+        ("heston_asian_geo_fixed_put_inflight", {"heston": [H1]},
+         {"kind": "asian_geo", "K": 100.0, "T": 0.6, "type": "put", "past_avg_log": 4.63, "t_elapsed": 0.4},
+         "essential", 4000, 40),
+        ("bs_asian_arith_float_put_inflight", {"vol": 0.25},
+         {"kind": "asian_arith", "K": 100.0, "T": 0.7, "fixed": False, "type": "put", "past_avg_S": 98.0,
+          "past_avg_log": 4.58, "t_elapsed": 0.3}, "essential", 4000, 35),
+        ("heston_lookback_fixed_call", {"heston": [H1]},
+         {"kind": "lookback", "K": 105.0, "T": 1.0, "fixed": True}, "essential", 4000, 64),
+        ("heston_lookback_fixed_put_inflight", {"heston": [H1]},
+         {"kind": "lookback", "K": 98.0, "T": 0.5, "fixed": True, "type": "put", "hist_min_S": 95.0,
+          "hist_max_S": 104.0}, "none", 4000, 32),
+        ("heston_lookback_float_put_full", {"heston": [H1]},
+         {"kind": "lookback", "K": 100.0, "T": 1.0, "fixed": False, "type": "put"}, "full", 2000, 50),
+        ("bs_lookback_fixed_put", {"vol": 0.3},
+         {"kind": "lookback", "K": 95.0, "T": 1.0, "fixed": True, "type": "put"}, "essential", 4000, 50),
+        ("heston_upin_call", {"heston": [H1]},
+         {"kind": "barrier", "dir": "up", "action": "in", "K": 100.0, "B": 120.0, "T": 1.0},
+         "essential", 4000, 64),
+        ("heston_downin_put_full", {"heston": [H1]},
+         {"kind": "barrier", "dir": "down", "action": "in", "K": 100.0, "B": 85.0, "T": 1.0, "type": "put"},
+         "full", 2000, 50),
+        ("heston_upout_call_rebate_at_hit", {"heston": [H1]},
+         {"kind": "barrier", "dir": "up", "action": "out", "K": 100.0, "B": 125.0, "T": 1.0, "rebate": 3.0,
+          "r": 0.02, "rebate_timing": "at_hit"}, "essential", 4000, 64),
+        ("heston_downout_call_rebate_at_maturity", {"heston": [H1]},
+         {"kind": "barrier", "dir": "down", "action": "out", "K": 95.0, "B": 85.0, "T": 1.0, "rebate": 2.0,
+          "r": 0.02, "rebate_timing": "at_maturity"}, "essential", 4000, 64),
+        ("heston_upin_put_rebate_at_maturity", {"heston": [H1]},
+         {"kind": "barrier", "dir": "up", "action": "in", "K": 105.0, "B": 115.0, "T": 1.0, "type": "put",
+          "rebate": 1.5, "r": 0.02, "rebate_timing": "at_maturity"}, "none", 4000, 64),
+        ("heston_downin_call_rebate_at_hit", {"heston": [H1]},
+         {"kind": "barrier", "dir": "down", "action": "in", "K": 100.0, "B": 90.0, "T": 1.0, "rebate": 2.5,
+          "r": 0.03, "rebate_timing": "at_hit"}, "essential", 4000, 64),
+        ("heston_upout_put_rebate_at_hit_full", {"heston": [H1]},
+         {"kind": "barrier", "dir": "up", "action": "out", "K": 100.0, "B": 120.0, "T": 1.0, "type": "put",
+          "rebate": 4.0, "r": 0.02, "rebate_timing": "at_hit"}, "full", 2000, 50),
+        ("bs_downout_call_rebate_at_hit", {"vol": 0.3},
+         {"kind": "barrier", "dir": "down", "action": "out", "K": 100.0, "B": 90.0, "T": 1.0, "rebate": 5.0,
+          "r": 0.05, "rebate_timing": "at_hit"}, "essential", 4000, 50),
+    ]
 ]
 
 FOURIER_SPECS = [

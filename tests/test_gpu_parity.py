@@ -47,6 +47,17 @@ REPLAY = [
     ("heston_asset_digital_put_full", 4096, 512),
     ("dbateskou_nv_full", 2048, 512),
     ("bs_call_oneshot", 8192, 1024),
+] + [
+    # the remaining instrument branches: floating-strike and put Asians, fixed-strike
+    # and put lookbacks, knock-ins, AtHit and AtMaturity rebates
+    (name, 4096, 512) for name in (
+        "heston_asian_arith_float_call", "heston_asian_arith_fixed_put", "heston_asian_geo_float_put_full",
+        "heston_asian_geo_fixed_put_inflight", "bs_asian_arith_float_put_inflight",
+        "heston_lookback_fixed_call", "heston_lookback_fixed_put_inflight", "heston_lookback_float_put_full",
+        "bs_lookback_fixed_put", "heston_upin_call", "heston_downin_put_full",
+        "heston_upout_call_rebate_at_hit", "heston_downout_call_rebate_at_maturity",
+        "heston_upin_put_rebate_at_maturity", "heston_downin_call_rebate_at_hit",
+        "heston_upout_put_rebate_at_hit_full", "bs_downout_call_rebate_at_hit")
 ]
 
 
@@ -75,7 +86,8 @@ def views_from_gpu(spec, job, g):
     elif kind == "lookback":
         second = S0 * np.exp(g[:, 1, :])
     hits = g[:, 1:4, :] if kind == "barrier" else None
-    return ST, second, hits
+    third = S0 * np.exp(g[:, 2, :]) if kind == "lookback" else None
+    return ST, second, hits, third
 
 
 @pytest.mark.parametrize("name,paths,streams", REPLAY, ids=[r[0] for r in REPLAY])
@@ -86,7 +98,7 @@ def test_path_replay_against_oracle(engine, oracle_lib, name, paths, streams):
     raw, st = engine.price(job)
     want, rec = oracle_lib.mc_price(job, oracle_lib.LAYOUT_STREAMS, 8, records=True)
     nsc = g.shape[0]
-    ST, second, hits = views_from_gpu(spec, job, g)
+    ST, second, hits, third = views_from_gpu(spec, job, g)
     rel = np.abs(ST - rec[:nsc, :, 0]) / rec[:nsc, :, 0]
     # FP32 paths vs FP64 paths on identical random numbers
     assert np.median(rel) < 1e-5, np.median(rel)
@@ -95,6 +107,9 @@ def test_path_replay_against_oracle(engine, oracle_lib, name, paths, streams):
     if second is not None:
         rel2 = np.abs(second - rec[:nsc, :, 1]) / np.abs(rec[:nsc, :, 1])
         assert np.median(rel2) < 1e-5 and np.mean(rel2 > 1e-3) < 5e-3
+    if third is not None:  # the running maximum of a lookback
+        rel3 = np.abs(third - rec[:nsc, :, 2]) / np.abs(rec[:nsc, :, 2])
+        assert np.median(rel3) < 1e-5 and np.mean(rel3 > 1e-3) < 5e-3
     if hits is not None:
         ho = np.stack([rec[:nsc, :, 3], rec[:nsc, :, 4], rec[:nsc, :, 5]], axis=1)
         assert np.mean(np.abs(hits - ho) > 1e-4) < 2e-3
@@ -124,6 +139,18 @@ STAT = [
     ("c4_dbates_nv_nci_asian", 1 << 16, 1 << 13),
     ("heston_lookback_float_call", 1 << 17, 1 << 14),
     ("heston_cash_digital_essential", 1 << 18, 1 << 15),
+    ("heston_asian_arith_float_call", 1 << 17, 1 << 14),
+    ("heston_asian_geo_float_put_full", 1 << 16, 1 << 13),
+    ("bs_asian_arith_float_put_inflight", 1 << 17, 1 << 14),
+    ("heston_lookback_fixed_call", 1 << 17, 1 << 14),
+    ("heston_lookback_fixed_put_inflight", 1 << 17, 1 << 14),
+    ("heston_upin_call", 1 << 17, 1 << 14),
+    ("heston_downin_put_full", 1 << 16, 1 << 13),
+    ("heston_upout_call_rebate_at_hit", 1 << 17, 1 << 14),
+    ("heston_downout_call_rebate_at_maturity", 1 << 17, 1 << 14),
+    ("heston_upin_put_rebate_at_maturity", 1 << 17, 1 << 14),
+    ("heston_downin_call_rebate_at_hit", 1 << 17, 1 << 14),
+    ("bs_downout_call_rebate_at_hit", 1 << 17, 1 << 14),
 ]
 
 

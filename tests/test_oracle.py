@@ -33,10 +33,10 @@ def test_restatement_matches_reference_outputs(oracle_lib, spec):
             assert np.all(np.abs(got - want) <= tol * scale + 1e-15), spec["name"]
 
 
-@pytest.mark.skipif(not (Path("/root/reference") / "include").exists(),
-                    reason="reference sources not present on this machine")
 def test_restatement_matches_live_reference(oracle_lib):
     """Where the reference compiles (oracle/_ref), compare live on a fresh seed."""
+    if not (oracle_lib.REF_ROOT / "include").exists():
+        pytest.skip("reference sources not present on this machine")
     oracle_lib.build(ref=True)
     spec = jobspec.with_config(MC_SPECS[2], seed=2024, paths=1500)
     job = jobspec.make_job(spec)

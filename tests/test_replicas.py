@@ -91,15 +91,19 @@ def test_combine_is_compute_stats():
 
 
 def test_pool_estimates():
-    """Inverse-variance pooling of independent estimates: weights 1/se^2, pooled SE
-    1/sqrt(sum 1/se^2); equal SEs give the plain mean and SE / sqrt(n)."""
-    p, se = replicas.pool_estimates([1.0, 2.0], [0.1, 0.2])
-    w = np.array([100.0, 25.0])
-    assert abs(p - (w @ [1.0, 2.0]) / w.sum()) < 1e-15 and abs(se - 1 / np.sqrt(w.sum())) < 1e-15
+    """Fixed-weight pooling of independent estimates: equal weights by default, the planned
+    budgets when given; SE = sqrt(sum w^2 se^2) / sum w.  A zero standard error is accepted
+    only when every replica agrees on it."""
     p, se = replicas.pool_estimates([3.0, 5.0, 7.0, 9.0], [0.4] * 4)
     assert abs(p - 6.0) < 1e-14 and abs(se - 0.2) < 1e-15
-    assert replicas.pool_estimates([4.0, 2.5], [0.3, 0.0]) == (2.5, 0.0)
-    for bad in (([], []), ([1.0], [0.1, 0.2]), ([1.0], [-0.1]), ([np.nan], [0.1])):
+    p, se = replicas.pool_estimates([1.0, 2.0], [0.1, 0.2], weights=[3.0, 1.0])
+    assert abs(p - 1.25) < 1e-15 and abs(se - np.sqrt(9 * 0.01 + 0.04) / 4) < 1e-15
+    # unequal sample SEs do not move the weights (1/se^2 weights would bias the pool low)
+    p, _ = replicas.pool_estimates([1.0, 2.0], [0.1, 0.2])
+    assert abs(p - 1.5) < 1e-15
+    assert replicas.pool_estimates([2.5, 2.5], [0.0, 0.0]) == (2.5, 0.0)
+    for bad in (([], []), ([1.0], [0.1, 0.2]), ([1.0], [-0.1]), ([np.nan], [0.1]), ([4.0, 2.5], [0.3, 0.0]),
+                ([1.0, 1.0], [0.0, 0.0], [1.0, -1.0])):
         with pytest.raises(ValueError):
             replicas.pool_estimates(*bad)
 
@@ -123,14 +127,15 @@ def _mlmc_rank(rank, world, port, out_q):
     try:
         from oracle import oracle
         r = oracle.mlmc_price(_mlmc_job(), _mlmc_cfg(42 + rank), oracle.LAYOUT_REFERENCE, 1)
-        out_q.put((rank, replicas.allreduce_estimate(r.price, r.price_std_err)))
+        out_q.put((rank, replicas.allreduce_estimate(r.price, r.price_std_err, float(r.total_steps))))
     finally:
         dist.destroy_process_group()
 
 
 def test_two_rank_mlmc_estimates_pool(oracle_lib):
-    """Two CPU ranks each run an independent MLMC estimate (own controller seed) and pool them
-    by inverse variance through one all-gather; every rank gets the pooled estimate of both."""
+    """Two CPU ranks each run an independent MLMC estimate (own controller seed) and pool them,
+    weighted by their path-step budgets, through one all-gather; every rank gets the pooled
+    estimate of both."""
     world = 2
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
@@ -143,7 +148,8 @@ def test_two_rank_mlmc_estimates_pool(oracle_lib):
         p.join(60)
         assert p.exitcode == 0
     runs = [oracle_lib.mlmc_price(_mlmc_job(), _mlmc_cfg(42 + r), oracle_lib.LAYOUT_REFERENCE, 1) for r in range(world)]
-    want = replicas.pool_estimates([r.price for r in runs], [r.price_std_err for r in runs])
+    want = replicas.pool_estimates([r.price for r in runs], [r.price_std_err for r in runs],
+                                   [float(r.total_steps) for r in runs])
     for _, (p, se) in got:
         assert abs(p - want[0]) < 1e-12 * abs(want[0]) and abs(se - want[1]) < 1e-12 * want[1]
     assert want[1] < min(r.price_std_err for r in runs)

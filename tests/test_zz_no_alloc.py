@@ -24,7 +24,12 @@ def _jobs():
                    m.GreekMode.ESSENTIAL, cfg, 100.0, 0.02, 0.0)
     b = m.make_job(heston, m.HestonStepper(m.SchemeExact), m.DownAndOutPut(100.0, 85.0, 1.0),
                    m.GreekMode.NONE, m.MonteCarloConfig(num_paths=50000, time_steps=50, seed=3), 100.0, 0.02, 0.0)
-    return [a, b]
+    # 2^21 paths with the default stream count: above 2^20 paths the default is M / 8
+    # streams (2^18 here), not 2^17, and both entry points must pick the same layout
+    c = m.make_job(heston, m.HestonStepper(m.SchemeNV), m.EuropeanOption(100.0, 1.0),
+                   m.GreekMode.NONE, m.MonteCarloConfig(num_paths=1 << 21, time_steps=16, seed=11),
+                   100.0, 0.02, 0.0)
+    return [a, b, c]
 
 
 def test_noalloc_matches_the_allocating_entry_point():

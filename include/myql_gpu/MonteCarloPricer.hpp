@@ -13,7 +13,7 @@
 //   Payoff{Vanilla,CashOrNothing,AssetOrNothing}             instruments/Payoffs.hpp:14-69
 //   EuropeanOption / AsianOption / LookbackOption / BarrierOption   instruments/options/*.hpp
 //   GreekMode, MonteCarloResult, MlmcResult                  core/PricingTypes.hpp
-//   MonteCarloConfig, MonteCarloPricer                       pricers/montecarlo/MonteCarloPricer.hpp:16-96
+//   MonteCarloConfig, MonteCarloPricer (RNG parameter too)   pricers/montecarlo/MonteCarloPricer.hpp:16-96
 //   MLMCConfig, MultiLevelMonteCarloPricer                   pricers/mlmc/MultiLevelMonteCarloPricer.hpp:16-47
 // so that user code switches by namespace (myql_gpu::) and include.  Every
 // calculate() lowers its template arguments to a myql_mc_job (include/myql_gpu.h)
@@ -34,7 +34,28 @@
 
 #include "../myql_gpu.h"
 
+// The reference's pricers take the random engine as a template parameter
+// (MonteCarloPricer.hpp:86, MultiLevelMonteCarloPricer.hpp:37), spelled
+// boost::random::xoshiro256pp.  Where Boost's header is present the drop-in
+// accepts that type too.
+#if __has_include(<boost/random/xoshiro.hpp>)
+#include <boost/random/xoshiro.hpp>
+#define MYQL_GPU_HAVE_BOOST_XOSHIRO 1
+#endif
+
 namespace myql_gpu {
+
+// ---------------------------------------------------------------- random engine
+// The GPU engine always draws xoshiro256++ streams: stream k of seed s is the
+// generator seeded with s (splitmix64 expansion) advanced by k jumps of 2^128.
+// The RNG template parameter of the pricers is kept for source compatibility and
+// must name a xoshiro256++ engine: this tag or Boost's.
+struct xoshiro256pp {};
+template <typename RNG> struct is_xoshiro256pp : std::false_type {};
+template <> struct is_xoshiro256pp<xoshiro256pp> : std::true_type {};
+#ifdef MYQL_GPU_HAVE_BOOST_XOSHIRO
+template <> struct is_xoshiro256pp<boost::random::xoshiro256pp> : std::true_type {};
+#endif
 
 // ---------------------------------------------------------------- core types
 enum class GreekMode { None, Essential, Full };
@@ -416,6 +437,12 @@ inline int &thread_device() {
   thread_local int dev = 0;
   return dev;
 }
+// The SchemeNCI table mode of this thread's pricers: applied to every context the
+// thread creates, so a later set_device() keeps it.
+inline bool &thread_exact_nci() {
+  thread_local bool on = false;
+  return on;
+}
 struct ThreadCtx {
   myql_ctx *ctx = nullptr;
   int device = -1;
@@ -436,9 +463,13 @@ inline myql_ctx *context() {
   if (!tc.ctx || tc.device != dev) {
     if (tc.ctx) myql_ctx_destroy(tc.ctx);
     tc.ctx = nullptr;
-    const myql_status s = myql_ctx_create(&tc.ctx, dev);
+    myql_status s = myql_ctx_create(&tc.ctx, dev);
     if (s != MYQL_OK) raise(s);
     tc.device = dev;
+    if (thread_exact_nci()) {
+      s = myql_ctx_set_nci_slopes(tc.ctx, 1);
+      if (s != MYQL_OK) raise(s);
+    }
   }
   return tc.ctx;
 }
@@ -534,18 +565,24 @@ template <typename T> T pick(const std::vector<double> &out, int q, int se, size
 // Selects the GPU the calling thread's pricers run on.
 inline void set_device(int device) { detail::thread_device() = device; }
 
-// SchemeNCI table cells of this thread's context: false (default) the reference's
+// SchemeNCI table cells of this thread's pricers: false (default) the reference's
 // (VolSchemes.hpp:240-313), true cells that keep the exact chi-squared mean (the
 // reference's first cell shortens it, which long, finely stepped paths turn into a
-// price bias; see myql_ctx_set_nci_slopes).
+// price bias; see myql_ctx_set_nci_slopes).  The choice holds for the calling
+// thread, across set_device(): every context the thread creates applies it.
 inline void set_exact_nci_tables(bool on) {
+  detail::thread_exact_nci() = on;
   const myql_status s = myql_ctx_set_nci_slopes(detail::context(), on ? 1 : 0);
   if (s != MYQL_OK) detail::raise(s);
 }
 
 // ---------------------------------------------------------------- pricers
-template <typename Model, typename Stepper, typename Instrument, GreekMode Mode = GreekMode::None>
+template <typename Model, typename Stepper, typename Instrument, GreekMode Mode = GreekMode::None,
+          typename RNG = xoshiro256pp>
 class MonteCarloPricer {
+  static_assert(is_xoshiro256pp<RNG>::value,
+                "the GPU engine draws xoshiro256++ streams: RNG must be xoshiro256pp");
+
  public:
   using ResultType = typename Instrument::ResultType;
   using ReturnStruct = MonteCarloResult<Mode, ResultType>;
@@ -599,8 +636,12 @@ class MonteCarloPricer {
   MonteCarloConfig cfg_;
 };
 
-template <typename Model, typename CoupledStepperType, typename Instrument, GreekMode Mode = GreekMode::None>
+template <typename Model, typename CoupledStepperType, typename Instrument, GreekMode Mode = GreekMode::None,
+          typename RNG = xoshiro256pp>
 class MultiLevelMonteCarloPricer {
+  static_assert(is_xoshiro256pp<RNG>::value,
+                "the GPU engine draws xoshiro256++ streams: RNG must be xoshiro256pp");
+
  public:
   using ResultType = typename Instrument::ResultType;
   using ReturnStruct = MlmcResult<Mode, ResultType>;

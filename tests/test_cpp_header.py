@@ -92,6 +92,17 @@ def test_mismatched_stepper_does_not_compile():
     assert r.returncode != 0 and "jump policy must match" in r.stderr
 
 
+def test_rng_template_parameter():
+    """The fifth template parameter (the reference's RNG) accepts xoshiro256pp, Boost's spelling
+    included where a Boost-API header is on the include path, and rejects other engines."""
+    ok = subprocess.run(["g++", "-std=c++20", "-fsyntax-only", "-Wall", "-Werror", f"-I{ROOT / 'include'}",
+                         f"-I{ROOT / 'oracle' / 'compat'}", str(CPP / "rng_param.cpp")], capture_output=True, text=True)
+    assert ok.returncode == 0, ok.stderr
+    bad = subprocess.run(["g++", "-std=c++20", "-fsyntax-only", f"-I{ROOT / 'include'}", str(CPP / "rng_mismatch.cpp")],
+                         capture_output=True, text=True)
+    assert bad.returncode != 0 and "RNG must be xoshiro256pp" in bad.stderr
+
+
 @pytest.mark.gpu
 def test_header_prices_on_the_gpu(tmp_path):
     exe = compile_check(tmp_path)

@@ -217,6 +217,17 @@ myql_status myql_ctx_set_records_limit(myql_ctx *ctx, uint64_t bytes);
  * the mean within about 1e-8.  Tables are cached per mode. */
 myql_status myql_ctx_set_nci_slopes(myql_ctx *ctx, int mode);
 
+/* Upper bound on the rows of this context's SchemeNCI tables (memory and L2
+ * budget; 0, the default, leaves the sizing rule alone, which builds rows up to
+ * lambda + 6 sqrt(lambda) + 16 at a high variance level, at least the
+ * reference's n_max + 1 and at most 1024).  A Poisson count N at or beyond the
+ * rows has no table row: its chi-squared quantile (d + 2N degrees of freedom)
+ * is the Wilson-Hilferty cube, where the reference evaluates the exact quantile
+ * past its own n_max (VolSchemes.hpp:368-369); such draws are counted in
+ * myql_mc_stats.table_fallbacks.  Rows beyond 1024 have d + 2N > 2048, where
+ * the cube is within 6e-6 relative of the exact quantile. */
+myql_status myql_ctx_set_nci_rows(myql_ctx *ctx, int max_rows);
+
 /* Host-side validation of a job, without a device: the checks myql_mc_price
  * runs before any launch (MYQL_ERR_NV_CONDITION for SchemeNV with
  * sigma^2 > 4 kappa theta, as VolSchemes.hpp:40-41 throws). */
@@ -264,6 +275,30 @@ myql_status myql_mc_price_noalloc(int device, const myql_mc_job *job, double *ou
 myql_status myql_mc_price_batch(myql_ctx *ctx, const myql_mc_job *jobs,
                                 size_t n_jobs, double *const *outs,
                                 myql_mc_stats *stats);
+
+/* The kernel classes of the last myql_mc_price_batch call on this context and
+ * the launch shape the batch autotuner picked for each: threads per block,
+ * streams (each with all of its paths) per thread, unroll depth of the
+ * time-step loop (0 = the compiler's choice) and persistent grid size.  A class
+ * is the factor count, the scheme of each factor (MYQL_SCHEME_*) and path
+ * dependence.  tuned = 1 when the shape was timed among the candidates on the
+ * class's leading items (tuned_ms; default_ms is the default shape 128 x 1 x 0
+ * on the same items), 0 when the class had too few items to tune (default
+ * shape), -1 when the shape was forced by myql_ctx_set_batch_shape. */
+typedef struct {
+  int32_t factors, scheme1, scheme2, path_dependent;
+  int32_t block, streams_per_thread, unroll, tuned;
+  uint32_t grid;
+  uint64_t items;
+  double tuned_ms, default_ms;
+} myql_batch_class_plan;
+myql_status myql_batch_last_plan(myql_ctx *ctx, myql_batch_class_plan *out, size_t cap, size_t *n_classes);
+
+/* Forces one launch shape on every class of this context's batches: block 64,
+ * 128 or 256 threads, 1, 2 or 4 streams per thread (block x streams a multiple
+ * of 128), unroll 0 or 2.  block = 0 returns to the autotuner.  Results do not
+ * depend on the shape beyond FP64 summation order. */
+myql_status myql_ctx_set_batch_shape(myql_ctx *ctx, int block, int streams_per_thread, int unroll);
 
 /* Per-path terminal records of one request (debug / parity): writes
  * n_scenarios * n_fields * num_paths floats in [scenario][field][path] order.

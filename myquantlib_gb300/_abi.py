@@ -100,6 +100,13 @@ class CvResultC(C.Structure):
                 ("kernel_launches", C.c_uint32)]
 
 
+class BatchClassPlanC(C.Structure):
+    _fields_ = [("factors", C.c_int32), ("scheme1", C.c_int32), ("scheme2", C.c_int32),
+                ("path_dependent", C.c_int32), ("block", C.c_int32), ("streams_per_thread", C.c_int32),
+                ("unroll", C.c_int32), ("tuned", C.c_int32), ("grid", C.c_uint32), ("items", C.c_uint64),
+                ("tuned_ms", C.c_double), ("default_ms", C.c_double)]
+
+
 class MyqlError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"[myql status {status}] {message}")
@@ -114,6 +121,10 @@ _SIGS = {
     "myql_ctx_set_loop_cap": (C.c_int, [C.c_void_p, C.c_uint32]),
     "myql_ctx_set_records_limit": (C.c_int, [C.c_void_p, C.c_uint64]),
     "myql_ctx_set_nci_slopes": (C.c_int, [C.c_void_p, C.c_int]),
+    "myql_ctx_set_nci_rows": (C.c_int, [C.c_void_p, C.c_int]),
+    "myql_ctx_set_batch_shape": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "myql_batch_last_plan": (C.c_int, [C.c_void_p, C.POINTER(BatchClassPlanC), C.c_size_t,
+                                       C.POINTER(C.c_size_t)]),
     "myql_validate_job": (C.c_int, [C.POINTER(McJobC)]),
     "myql_mc_price": (C.c_int, [C.c_void_p, C.POINTER(McJobC), C.POINTER(C.c_double),
                                 C.POINTER(McStatsC)]),

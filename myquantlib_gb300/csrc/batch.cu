@@ -7,8 +7,12 @@
 // order the items by cost (longest first), then
 //   H2D(job descriptors, items)  ->  persistent batch_kernel  ->  per-job finalize  ->  D2H
 // captured once as a CUDA graph per batch shape and replayed afterwards (only
-// the pinned staging buffers change between calls).  The persistent grid size
-// is chosen by a small autotuner on the first batch of a shape and cached.
+// the pinned staging buffers change between calls).  Per kernel class, a small
+// autotuner picks the launch shape -- threads per block, streams (all of their
+// paths) per thread, unroll depth of the time-step loop -- and the persistent
+// grid size on the first batch of a shape, timing each candidate on the class's
+// leading (most expensive) items; the choice is cached and reported by
+// myql_batch_last_plan.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -45,7 +49,15 @@ struct BatchState : ExtState {
   std::map<uint64_t, DevBuf> seed_tables;  // seed -> [4][kDefaultStreams] states
   cudaGraphExec_t graph = nullptr;
   uint64_t graph_key = 0;
-  std::map<uint64_t, unsigned int> tuned_blocks;  // (segment class, shape) -> persistent grid
+  struct Tuned {
+    BatchShape shape;
+    unsigned int blocks;
+    int tuned;
+    double tuned_ms, default_ms;
+  };
+  std::map<uint64_t, Tuned> tuned;  // (segment class, batch shape) -> launch shape and grid
+  std::vector<myql_batch_class_plan> last_plan;  // the segments of the last call
+  BatchShape forced{0, 0, 0};                    // block 0: the autotuner decides
   static constexpr int kSide = 4;                  // side streams of the concurrent class kernels
   cudaStream_t side[kSide] = {};
   cudaEvent_t fork = nullptr, join[kSide] = {};
@@ -74,7 +86,21 @@ struct Segment {
   bool pd;
   uint64_t begin, end;
   unsigned int blocks;
+  BatchShape shape;
 };
+
+// The autotuner's launch shapes; the first is the default.
+constexpr BatchShape kShapes[] = {{128, 1, 0}, {64, 2, 0}, {256, 1, 0}, {128, 2, 0}, {256, 2, 0}, {128, 1, 2}};
+
+unsigned int items_per_pull(const BatchShape &sh) {
+  return (unsigned int)(sh.block * sh.streams_per_thread / kBatchItemStreams);
+}
+
+bool shape_ok(const BatchShape &sh) {
+  return (sh.block == 64 || sh.block == 128 || sh.block == 256) &&
+         (sh.streams_per_thread == 1 || sh.streams_per_thread == 2 || sh.streams_per_thread == 4) &&
+         (sh.unroll == 0 || sh.unroll == 2) && (sh.block * sh.streams_per_thread) % kBatchItemStreams == 0;
+}
 
 uint64_t mix(uint64_t h, uint64_t v) { return (h ^ v) * 0x100000001b3ull + (h >> 29); }
 
@@ -221,7 +247,7 @@ extern "C" myql_status myql_mc_price_batch(myql_ctx *ctx_, const myql_mc_job *jo
   for (uint64_t k = 0; k < total_items; ++k) {
     const int key = seg_key[order[k]];
     if (segs.empty() || 2 * segs.back().klass + (segs.back().pd ? 1 : 0) != key)
-      segs.push_back({key / 2, (key & 1) != 0, k, k, 0u});
+      segs.push_back({key / 2, (key & 1) != 0, k, k, 0u, kShapes[0]});
     segs.back().end = k + 1;
   }
   if (segs.size() > 64) return set_error(MYQL_ERR_TOO_LARGE, "too many kernel classes");
@@ -246,61 +272,122 @@ extern "C" myql_status myql_mc_price_batch(myql_ctx *ctx_, const myql_mc_job *jo
     P.item_end = g.end;
     P.counter = (unsigned int *)B.d_counter.p + gi;
     P.partials = (double *)B.d_partials.p;
+    P.streams_per_thread = (unsigned int)g.shape.streams_per_thread;
+    P.items_per_pull = items_per_pull(g.shape);
     return P;
   };
 
-  // ---- autotune the persistent grid of each class segment once per batch shape:
-  // candidates on the segment's leading (most expensive) items
+  // ---- autotune each class segment's launch shape and persistent grid once per batch
+  // shape: every candidate runs the segment's leading (most expensive) items
   signature = mix(signature, n_jobs);
   bool uploaded = false;
+  const bool forced = B.forced.block != 0;
+  B.last_plan.clear();
   for (size_t gi = 0; gi < segs.size(); ++gi) {
     Segment &g = segs[gi];
-    const int occ = batch_blocks_per_sm(g.klass, g.pd);
     const uint64_t n = g.end - g.begin;
-    g.blocks = (unsigned int)std::min<uint64_t>(n, (uint64_t)occ * ctx->sm_count);
+    auto grid_of = [&](const BatchShape &sh, int per_sm) {
+      const uint64_t pulls = (n + items_per_pull(sh) - 1) / items_per_pull(sh);
+      return (unsigned int)std::max<uint64_t>(1, std::min<uint64_t>(pulls, (uint64_t)per_sm * ctx->sm_count));
+    };
     const uint64_t tkey = mix(signature, 2 * g.klass + (g.pd ? 1 : 0));
-    auto tuned = B.tuned_blocks.find(tkey);
-    if (tuned != B.tuned_blocks.end()) {
-      g.blocks = tuned->second;
-      continue;
-    }
-    if (n > (uint64_t)8 * occ * ctx->sm_count) {
-      if (!uploaded) {
-        e = cudaMemcpyAsync(B.d_jobs.p, hj, n_jobs * sizeof(BatchJob), cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(B.d_items.p, hi, total_items * sizeof(BatchItem), cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(B.d_slots.p, hs, total_items * sizeof(unsigned int), cudaMemcpyHostToDevice, st);
-        if (e != cudaSuccess) return cuda_status(e, "batch autotune upload");
-        uploaded = true;
-      }
-      const unsigned int cands[3] = {(unsigned int)(occ * ctx->sm_count),
-                                     (unsigned int)std::max(1, occ / 2) * (unsigned int)ctx->sm_count,
-                                     (unsigned int)ctx->sm_count};
-      BatchParams T = params_of(g, gi);
-      T.item_end = g.begin + std::min<uint64_t>(n, (uint64_t)4 * occ * ctx->sm_count);
-      float best = 1e30f;
-      for (int c = 0; c < 3 && e == cudaSuccess; ++c) {
-        e = cudaMemsetAsync(T.counter, 0, 4, st);
-        if (e == cudaSuccess) e = cudaEventRecord(ctx->ev0, st);
-        if (e == cudaSuccess) e = launch_batch(T, g.klass, g.pd, cands[c], st);
-        if (e == cudaSuccess) e = cudaEventRecord(ctx->ev1, st);
-        if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev1);
-        float ms = 0.0f;
-        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-        ctx->launches++;
-        if (ms < best) {
-          best = ms;
-          g.blocks = cands[c];
+    BatchState::Tuned tu{forced ? B.forced : kShapes[0], 0u, 0, 0.0, 0.0};
+    auto cached = B.tuned.find(tkey);
+    if (forced) {
+      tu.blocks = grid_of(tu.shape, batch_blocks_per_sm(g.klass, g.pd, tu.shape));
+    } else if (cached != B.tuned.end()) {
+      tu = cached->second;
+    } else {
+      const int occ0 = batch_blocks_per_sm(g.klass, g.pd, kShapes[0]);
+      tu.blocks = grid_of(kShapes[0], occ0);
+      if (n > (uint64_t)8 * occ0 * ctx->sm_count) {
+        if (!uploaded) {
+          e = cudaMemcpyAsync(B.d_jobs.p, hj, n_jobs * sizeof(BatchJob), cudaMemcpyHostToDevice, st);
+          if (e == cudaSuccess) e = cudaMemcpyAsync(B.d_items.p, hi, total_items * sizeof(BatchItem), cudaMemcpyHostToDevice, st);
+          if (e == cudaSuccess) e = cudaMemcpyAsync(B.d_slots.p, hs, total_items * sizeof(unsigned int), cudaMemcpyHostToDevice, st);
+          if (e != cudaSuccess) return cuda_status(e, "batch autotune upload");
+          uploaded = true;
         }
+        // the same leading items for every candidate
+        const uint64_t n_tune = std::min<uint64_t>(n, (uint64_t)4 * occ0 * ctx->sm_count);
+        auto time_one = [&](const BatchShape &sh, unsigned int blocks, uint64_t items, float &ms) {
+          Segment t = g;
+          t.shape = sh;
+          BatchParams T = params_of(t, gi);
+          T.item_end = g.begin + items;
+          cudaError_t er = cudaMemsetAsync(T.counter, 0, 4, st);
+          if (er == cudaSuccess) er = cudaEventRecord(ctx->ev0, st);
+          if (er == cudaSuccess) er = launch_batch(T, g.klass, g.pd, sh, blocks, st);
+          if (er == cudaSuccess) er = cudaEventRecord(ctx->ev1, st);
+          if (er == cudaSuccess) er = cudaEventSynchronize(ctx->ev1);
+          ms = 0.0f;
+          if (er == cudaSuccess) cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+          ctx->launches++;
+          return er;
+        };
+        float best = 1e30f;
+        int best_occ = occ0;
+        for (const BatchShape &sh : kShapes) {
+          const int occ = batch_blocks_per_sm(g.klass, g.pd, sh);
+          const unsigned int pulls = (unsigned int)((n_tune + items_per_pull(sh) - 1) / items_per_pull(sh));
+          const unsigned int blocks = std::min<unsigned int>(pulls, (unsigned int)occ * (unsigned int)ctx->sm_count);
+          float ms = 0.0f;
+          e = time_one(sh, 1, items_per_pull(sh), ms);  // first launch of the variant: loads the kernel
+          if (e == cudaSuccess) e = time_one(sh, blocks, n_tune, ms);
+          if (e != cudaSuccess) return cuda_status(e, "batch autotune");
+          if (&sh == &kShapes[0]) tu.default_ms = ms;
+          if (ms < best) {
+            best = ms;
+            tu.shape = sh;
+            best_occ = occ;
+          }
+        }
+        // the persistent grid of the chosen shape: full occupancy (timed above), half, one
+        // block per SM
+        const unsigned int pulls = (unsigned int)((n_tune + items_per_pull(tu.shape) - 1) / items_per_pull(tu.shape));
+        const unsigned int full = std::min<unsigned int>(pulls, (unsigned int)best_occ * (unsigned int)ctx->sm_count);
+        int per_sm = best_occ;
+        for (int cand : {std::max(1, best_occ / 2), 1}) {
+          const unsigned int c = (unsigned int)cand * (unsigned int)ctx->sm_count;
+          if (cand >= per_sm || c >= full) continue;
+          float ms = 0.0f;
+          e = time_one(tu.shape, c, n_tune, ms);
+          if (e != cudaSuccess) return cuda_status(e, "batch autotune");
+          if (ms < best) {
+            best = ms;
+            per_sm = cand;
+          }
+        }
+        tu.tuned = 1;
+        tu.tuned_ms = best;
+        tu.blocks = grid_of(tu.shape, per_sm);
       }
-      if (e != cudaSuccess) return cuda_status(e, "batch autotune");
+      B.tuned[tkey] = tu;
     }
-    B.tuned_blocks[tkey] = g.blocks;
+    g.shape = tu.shape;
+    g.blocks = tu.blocks;
+    myql_batch_class_plan cp;
+    std::memset(&cp, 0, sizeof cp);
+    cp.factors = g.klass == BK_F0 ? 0 : (g.klass < BK_F2_NV_NV ? 1 : 2);
+    cp.scheme1 = g.klass == BK_F0 ? 0 : (g.klass < BK_F2_NV_NV ? g.klass : 1 + (g.klass - BK_F2_NV_NV) / 3);
+    cp.scheme2 = g.klass < BK_F2_NV_NV ? 0 : 1 + (g.klass - BK_F2_NV_NV) % 3;
+    cp.path_dependent = g.pd ? 1 : 0;
+    cp.block = g.shape.block;
+    cp.streams_per_thread = g.shape.streams_per_thread;
+    cp.unroll = g.shape.unroll;
+    cp.tuned = forced ? -1 : tu.tuned;
+    cp.grid = g.blocks;
+    cp.items = n;
+    cp.tuned_ms = tu.tuned_ms;
+    cp.default_ms = tu.default_ms;
+    B.last_plan.push_back(cp);
   }
 
   // ---- the batch itself, through a CUDA graph per shape: the class kernels run
   // concurrently on side streams between the uploads and the finalize
   uint64_t key = mix(signature, total_items);
-  for (const Segment &g : segs) key = mix(mix(key, g.end), g.blocks);
+  for (const Segment &g : segs)
+    key = mix(mix(mix(key, g.end), g.blocks), (uint64_t)(g.shape.block * 64 + g.shape.streams_per_thread * 4 + g.shape.unroll));
   for (const void *ptr : {B.h_jobs.p, B.h_items.p, B.h_slots.p, B.h_out.p, B.d_jobs.p, B.d_items.p, B.d_slots.p,
                           B.d_partials.p, B.d_out.p, B.d_counter.p})
     key = mix(key, (uint64_t)(uintptr_t)ptr);
@@ -317,7 +404,7 @@ extern "C" myql_status myql_mc_price_batch(myql_ctx *ctx_, const myql_mc_job *jo
     const int ns = (int)std::min<size_t>(segs.size(), (size_t)BatchState::kSide);
     for (int i = 0; i < ns && e == cudaSuccess; ++i) e = cudaStreamWaitEvent(B.side[i], B.fork, 0);
     for (size_t gi = 0; gi < segs.size() && e == cudaSuccess; ++gi)
-      e = launch_batch(params_of(segs[gi], gi), segs[gi].klass, segs[gi].pd, segs[gi].blocks,
+      e = launch_batch(params_of(segs[gi], gi), segs[gi].klass, segs[gi].pd, segs[gi].shape, segs[gi].blocks,
                        B.side[gi % BatchState::kSide]);
     for (int i = 0; i < ns && e == cudaSuccess; ++i) {
       e = cudaEventRecord(B.join[i], B.side[i]);
@@ -360,4 +447,29 @@ extern "C" myql_status myql_mc_price_batch(myql_ctx *ctx_, const myql_mc_job *jo
     stats->kernel_launches = ctx->launches;
   }
   return read_status(ctx, stats);
+}
+
+extern "C" myql_status myql_batch_last_plan(myql_ctx *ctx_, myql_batch_class_plan *out, size_t cap,
+                                            size_t *n_classes) {
+  CtxBase *ctx = reinterpret_cast<CtxBase *>(ctx_);
+  if (!ctx || !n_classes || (cap && !out)) return set_error(MYQL_ERR_INVALID_ARG, "null argument");
+  *n_classes = 0;
+  if (!ctx->batch) return MYQL_OK;
+  const BatchState &B = *static_cast<const BatchState *>(ctx->batch.get());
+  *n_classes = B.last_plan.size();
+  for (size_t i = 0; i < B.last_plan.size() && i < cap; ++i) out[i] = B.last_plan[i];
+  return MYQL_OK;
+}
+
+extern "C" myql_status myql_ctx_set_batch_shape(myql_ctx *ctx_, int block, int streams_per_thread, int unroll) {
+  CtxBase *ctx = reinterpret_cast<CtxBase *>(ctx_);
+  if (!ctx) return set_error(MYQL_ERR_INVALID_ARG, "null context");
+  const BatchShape sh{block, streams_per_thread, unroll};
+  if (block != 0 && !shape_ok(sh))
+    return set_error(MYQL_ERR_INVALID_ARG,
+                     "batch shape: block 64/128/256, streams per thread 1/2/4 (block x streams a multiple "
+                     "of 128), unroll 0 or 2; block 0 returns to the autotuner");
+  if (!ctx->batch) ctx->batch.reset(new BatchState);
+  static_cast<BatchState *>(ctx->batch.get())->forced = block ? sh : BatchShape{0, 0, 0};
+  return MYQL_OK;
 }

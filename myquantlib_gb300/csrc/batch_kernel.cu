@@ -1,20 +1,36 @@
 // batch_kernel.cu -- launchers of the per-class persistent batch kernels
-// (instantiated in batch_k_f01.cu and batch_k_f2.cu) and the per-job finalize.
+// (instantiated per block size in batch_k_b64.cu, batch_k_b128.cu, batch_k_b256.cu) and the
+// per-job finalize.
 #include "batch.cuh"
 
 namespace myql {
 
-cudaError_t launch_batch_f01(const BatchParams &B, int klass, bool pd, unsigned int blocks, cudaStream_t st);
-cudaError_t launch_batch_f2(const BatchParams &B, int klass, bool pd, unsigned int blocks, cudaStream_t st);
-int occupancy_batch_f01(int klass, bool pd);
-int occupancy_batch_f2(int klass, bool pd);
+cudaError_t batch_dispatch_b64(const BatchParams *B, int klass, bool pd, int unroll, unsigned int blocks,
+                               cudaStream_t st, int *occ);
+cudaError_t batch_dispatch_b128(const BatchParams *B, int klass, bool pd, int unroll, unsigned int blocks,
+                                cudaStream_t st, int *occ);
+cudaError_t batch_dispatch_b256(const BatchParams *B, int klass, bool pd, int unroll, unsigned int blocks,
+                                cudaStream_t st, int *occ);
 
-cudaError_t launch_batch(const BatchParams &B, int klass, bool pd, unsigned int blocks, cudaStream_t st) {
-  return klass < BK_F2_NV_NV ? launch_batch_f01(B, klass, pd, blocks, st) : launch_batch_f2(B, klass, pd, blocks, st);
+static cudaError_t batch_dispatch_any(const BatchParams *B, int klass, bool pd, const BatchShape &sh,
+                                      unsigned int blocks, cudaStream_t st, int *occ) {
+  switch (sh.block) {
+    case 64: return batch_dispatch_b64(B, klass, pd, sh.unroll, blocks, st, occ);
+    case 128: return batch_dispatch_b128(B, klass, pd, sh.unroll, blocks, st, occ);
+    case 256: return batch_dispatch_b256(B, klass, pd, sh.unroll, blocks, st, occ);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
-int batch_blocks_per_sm(int klass, bool pd) {
-  const int n = klass < BK_F2_NV_NV ? occupancy_batch_f01(klass, pd) : occupancy_batch_f2(klass, pd);
+cudaError_t launch_batch(const BatchParams &B, int klass, bool pd, const BatchShape &shape, unsigned int blocks,
+                         cudaStream_t st) {
+  if (blocks == 0) return cudaErrorInvalidValue;
+  return batch_dispatch_any(&B, klass, pd, shape, blocks, st, nullptr);
+}
+
+int batch_blocks_per_sm(int klass, bool pd, const BatchShape &shape) {
+  int n = 0;
+  if (batch_dispatch_any(nullptr, klass, pd, shape, 0, nullptr, &n) != cudaSuccess) return 1;
   return n > 0 ? n : 1;
 }
 

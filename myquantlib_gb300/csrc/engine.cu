@@ -546,12 +546,13 @@ myql_status ensure_streams(CtxBase *ctx, uint64_t seed, uint64_t first, uint64_t
 
 myql_status ensure_nci(CtxBase *ctx, const myql_heston_params &p, double dt_min, NciTable &tab) {
   const double d = 4.0 * p.kappa * p.theta / (p.sigma * p.sigma);
-  const int rows = nci_rows_wanted(p, dt_min);
+  const int cap = ctx->nci_rows_cap;
+  const int rows = cap ? std::min(cap, nci_rows_wanted(p, dt_min)) : nci_rows_wanted(p, dt_min);
   uint64_t key;
   std::memcpy(&key, &d, sizeof key);  // d > 0: the sign bit is free for the slope rule
   if (ctx->nci_slopes) key |= 1ull << 63;
   auto it = ctx->nci.find(key);
-  if (it == ctx->nci.end() || it->second.rows < rows) {
+  if (it == ctx->nci.end() || it->second.rows < rows || (cap && it->second.rows > cap)) {
     if (it != ctx->nci.end()) {
       it->second.main.release();
       it->second.tail.release();
@@ -791,6 +792,13 @@ myql_status myql_ctx_set_nci_slopes(myql_ctx *ctx, int mode) {
   if (!ctx) return set_error(MYQL_ERR_INVALID_ARG, "null context");
   if (mode != 0 && mode != 1) return set_error(MYQL_ERR_INVALID_ARG, "NCI slope mode is 0 or 1");
   ctx->nci_slopes = mode;
+  return MYQL_OK;
+}
+
+myql_status myql_ctx_set_nci_rows(myql_ctx *ctx, int max_rows) {
+  if (!ctx) return set_error(MYQL_ERR_INVALID_ARG, "null context");
+  if (max_rows < 0 || max_rows > 1024) return set_error(MYQL_ERR_INVALID_ARG, "NCI row cap is 0 or 1..1024");
+  ctx->nci_rows_cap = max_rows;
   return MYQL_OK;
 }
 

@@ -46,6 +46,7 @@ struct CtxBase {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   uint32_t loop_cap = kDefaultLoopCap;
   int nci_slopes = 0;  // NCI table cells: 0 the reference's, 1 exact slopes and a mean-preserving first cell
+  int nci_rows_cap = 0;  // at most this many NCI table rows (0: the sizing rule alone, at most 1024)
   uint32_t launches = 0;
   uint64_t records_cap_bytes = 2ull << 30;  // per-path record scratch per chunk
   // xoshiro stream-state table of the last (seed, n)

@@ -212,8 +212,10 @@ struct NoHook {
 
 // Simulates one path of one scenario; writes the tracker's terminal record.
 // With an active hook every path is stepped (no single-draw GBM European) and
-// the hook sees each step.
-template <int NF, int S1, int S2, bool PD, class Hook>
+// the hook sees each step.  UNROLL > 0 unrolls the time-step loop by that depth
+// (the batch autotuner's knob); 0 leaves the loop to the compiler.  The
+// arithmetic of every step is the same either way.
+template <int NF, int S1, int S2, bool PD, class Hook, int UNROLL = 0>
 __device__ __forceinline__ void sim_path_h(const SimParams &P, const ScenarioConst &C, Xo &rng,
                                            float (&out)[kMaxFields], unsigned int &caphits,
                                            unsigned int &fallbacks, Hook &hook) {
@@ -230,7 +232,7 @@ __device__ __forceinline__ void sim_path_h(const SimParams &P, const ScenarioCon
     if (P.jump_kind) X += jump_draw(P, C, rng, caphits);
   } else {
     const float dt = C.dt;
-    for (int k = 0; k < n; ++k) {
+    auto one_step = [&](int k) {
       const float G = inv_normal_bits(draw(rng));
       if (NF == 0) {
         X += fmaf(C.gbm_vol, G, C.gbm_drift);
@@ -265,6 +267,12 @@ __device__ __forceinline__ void sim_path_h(const SimParams &P, const ScenarioCon
         ts.step(P, k, dt, X);
       }
       if (Hook::active) hook.step_end(k + 1, X, va, vb, ts.acc, ts.tb >= 0.0f);
+    };
+    if constexpr (UNROLL > 0) {
+#pragma unroll UNROLL
+      for (int k = 0; k < n; ++k) one_step(k);
+    } else {
+      for (int k = 0; k < n; ++k) one_step(k);
     }
     if (!PD && (NF > 0 || Hook::active) && P.jump_kind) {
       const float J = jump_draw(P, C, rng, caphits);
@@ -276,12 +284,12 @@ __device__ __forceinline__ void sim_path_h(const SimParams &P, const ScenarioCon
   ts.finish(P, C, X, PD, out);
 }
 
-template <int NF, int S1, int S2, bool PD>
+template <int NF, int S1, int S2, bool PD, int UNROLL = 0>
 __device__ __forceinline__ void sim_path(const SimParams &P, const ScenarioConst &C, Xo &rng,
                                          float (&out)[kMaxFields], unsigned int &caphits,
                                          unsigned int &fallbacks) {
   NoHook h;
-  sim_path_h<NF, S1, S2, PD>(P, C, rng, out, caphits, fallbacks, h);
+  sim_path_h<NF, S1, S2, PD, NoHook, UNROLL>(P, C, rng, out, caphits, fallbacks, h);
 }
 
 template <int NF, int S1, int S2, bool PD>

@@ -440,6 +440,11 @@ class Engine:
         that keeps its exact mean, so the draw's conditional mean is unbiased."""
         _abi.check(self.lib.myql_ctx_set_nci_slopes(self.handle, int(mode)))
 
+    def set_nci_rows(self, max_rows: int):
+        """Upper bound on the SchemeNCI table rows (0: the sizing rule); Poisson counts beyond
+        the rows take the Wilson-Hilferty quantile and are counted in table_fallbacks."""
+        _abi.check(self.lib.myql_ctx_set_nci_rows(self.handle, int(max_rows)))
+
     def price(self, job: "_Job") -> tuple[np.ndarray, _abi.McStatsC]:
         out = np.zeros(2 * _abi.Q_COUNT * job.n_strikes, dtype=np.float64)
         st = _abi.McStatsC()
@@ -455,6 +460,19 @@ class Engine:
         st = _abi.McStatsC()
         _abi.check(self.lib.myql_mc_price_batch(self.handle, arr, n, ptrs, C.byref(st)))
         return [o.reshape(2 * _abi.Q_COUNT, 1) for o in outs], st
+
+    def batch_plan(self) -> list[dict]:
+        """Per kernel class of the last batch: the launch shape the autotuner picked (threads per
+        block, streams per thread, unroll depth, persistent grid) and its timings."""
+        cap = 64
+        arr = (_abi.BatchClassPlanC * cap)()
+        n = C.c_size_t()
+        _abi.check(self.lib.myql_batch_last_plan(self.handle, arr, cap, C.byref(n)))
+        return [{f: getattr(arr[i], f) for f, _ in _abi.BatchClassPlanC._fields_} for i in range(min(n.value, cap))]
+
+    def set_batch_shape(self, block: int = 0, streams_per_thread: int = 1, unroll: int = 0):
+        """Forces one launch shape on every batch class (block 0: the autotuner decides)."""
+        _abi.check(self.lib.myql_ctx_set_batch_shape(self.handle, block, streams_per_thread, unroll))
 
     # ---- neural control variate
     def cv_init(self, seed: int = 1):

@@ -122,3 +122,59 @@ def test_batch_rejects_strips_and_full(engine):
                    m.GreekMode.FULL, m.MonteCarloConfig(num_paths=1000, time_steps=10), 100.0, 0.02, 0.0)
     with pytest.raises(m._abi.MyqlError):
         engine.price_batch([j])
+
+
+SHAPES = [(128, 1, 0), (64, 2, 0), (256, 1, 0), (128, 2, 0), (256, 2, 0), (128, 1, 2), (64, 4, 0)]
+
+
+def test_every_launch_shape_gives_the_same_prices(engine):
+    """Threads per block, streams per thread and unroll depth change only the FP64 grouping of
+    the per-item sums: every shape returns the default shape's prices to 1e-12."""
+    jobs = jobs_of(mixed_requests())
+    base = None
+    try:
+        for sh in SHAPES:
+            engine.set_batch_shape(*sh)
+            outs, _ = engine.price_batch(jobs)
+            plan = engine.batch_plan()
+            assert {(p["block"], p["streams_per_thread"], p["unroll"]) for p in plan} == {sh}
+            assert all(p["tuned"] == -1 for p in plan)
+            if base is None:
+                base = outs
+                continue
+            for x, y in zip(outs, base):
+                np.testing.assert_allclose(x, y, rtol=1e-12, atol=1e-15)
+    finally:
+        engine.set_batch_shape(0)
+
+
+def test_autotuner_picks_a_shape_per_class(engine):
+    """A class with enough items is tuned over the launch shapes and grids on its leading items;
+    the choice is reported per class and is never slower there than the default shape."""
+    eng = m.Engine(0)
+    try:
+        rq = []
+        for k in range(12):   # 12 jobs x 2^17 streams: 12288 items of one class (Heston NV Asian)
+            rq.append(dispatch.Request(m.HestonModel(H), m.AsianOption(m.TrackerArithAsian, m.PayoffVanilla(), True,
+                                                                       95.0 + k, 1.0),
+                                       m.MonteCarloConfig(num_paths=1 << 17, time_steps=16, seed=k),
+                                       100.0, 0.02, 0.0, stepper=m.HestonStepper(m.SchemeNV, m.TrackerArithAsian)))
+        rq += mixed_requests()[:4]
+        jobs = jobs_of(rq)
+        outs, _ = eng.price_batch(jobs)
+        plan = eng.batch_plan()
+        big = [p for p in plan if p["factors"] == 1 and p["scheme1"] == 1 and p["path_dependent"] == 1]
+        assert len(big) == 1 and big[0]["tuned"] == 1 and big[0]["items"] == 12 * 1024
+        p = big[0]
+        assert (p["block"], p["streams_per_thread"], p["unroll"]) in SHAPES
+        assert 0 < p["tuned_ms"] <= p["default_ms"] * 1.0001 and p["grid"] > 0
+        assert all(q["tuned"] == 0 for q in plan if q is not p)   # too few items to tune
+        # the tuned shape prices what each request priced alone prices
+        for r, j, got in zip(rq, jobs, outs):
+            want, _ = eng.price(j)
+            assert abs(got[0, 0] - want[0, 0]) <= 2e-6 * abs(want[0, 0]) + 1e-3 * want[1, 0] + 1e-12
+        again, _ = eng.price_batch(jobs)       # cached choice, same graph: identical
+        for x, y in zip(outs, again):
+            assert np.array_equal(x, y)
+    finally:
+        eng.close()

@@ -628,7 +628,10 @@ def run_batch(args) -> dict:
                        "jobs": len(jobs), "path_steps_per_step": total, "l2": "flushed between steps"},
             "e2e": {"value": e2e, "unit": "paths*steps/s", "h2d_bytes_per_step": None,
                     "d2h_bytes_per_step": 8 * 20 * len(jobs)},
-            "gpu_launches": launches * args.steps, "clocks": clk.summary()}
+            "gpu_launches": launches * args.steps, "clocks": clk.summary(),
+            # per kernel class: the launch shape the batch autotuner picked and its timings
+            "tuner": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in p.items()}
+                      for p in eng.batch_plan()]}
     if not args.no_cpu:
         from oracle import oracle
         oracle.build(ref=False)

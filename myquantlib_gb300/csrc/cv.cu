@@ -29,6 +29,13 @@ struct CvState : ExtState {
   DevBuf fpart;                    // per-block price / hedge-ratio sums
   bool init = false;
   uint64_t adam_t = 0;
+  // the Adam loop of the last training shape, as one CUDA graph
+  cudaGraphExec_t train_graph = nullptr;
+  uint64_t train_key = 0;
+  uint32_t train_launches = 0;
+  ~CvState() {
+    if (train_graph) cudaGraphExecDestroy(train_graph);
+  }
 };
 
 uint64_t splitmix(uint64_t &s) {
@@ -530,29 +537,86 @@ myql_status myql_cv_train(myql_ctx *ctx_, const myql_mc_job *job, const myql_cv_
   double *loss = (double *)S.loss.p;
   const uint32_t iters = cfg->iterations;
   const auto t_train = std::chrono::steady_clock::now();
-  for (uint32_t it = 0; it < iters; ++it) {
-    const uint64_t b0 = (it * b_pb) % n_pb;
-    const uint64_t nb = std::min(b_pb, n_pb - b0);
-    const uint8_t *f = (const uint8_t *)S.p_feat.p + b0 * nh * kCvTileBytes;
-    const float *dm = (const float *)S.p_dM.p + b0 * nh * 128;
-    const float *Y = (const float *)S.p_Y.p + b0 * 128;
-    float *cvb = (float *)S.p_cv.p + b0 * 128;
-    s = forward(ctx, S, f, dm, nb * 128, nh, cvb, nullptr);
-    if (s != MYQL_OK) return s;
-    e = launch_cv_resid(Y, cvb, nb * 128, (float *)S.coef.p, loss + (size_t)it * kResidBlocks, (double *)S.rpart.p,
-                        ctx->stream);
-    if (e != cudaSuccess) return cuda_status(e, "cv_resid launch");
-    s = backward(ctx, S, f, dm, nb * 128, nh);
-    if (s != MYQL_OK) return s;
-    const double pi = 3.14159265358979323846;
-    const double lr = cfg->learning_rate * (0.05 + 0.95 * 0.5 * (1.0 + std::cos(pi * it / std::max(1u, iters))));
-    S.adam_t++;
-    e = launch_cv_adam((float *)S.params.p, (float *)S.adam_m.p, (float *)S.adam_v.p, (const float *)S.grad.p,
-                       (float)lr, (float)(1.0 - std::pow(0.9, (double)S.adam_t)),
-                       (float)(1.0 - std::pow(0.999, (double)S.adam_t)), ctx->stream);
-    if (e == cudaSuccess) e = launch_cv_pack((const float *)S.params.p, (uint8_t *)S.img.p, (float *)S.vec.p, ctx->stream);
-    if (e != cudaSuccess) return cuda_status(e, "cv_adam launch");
-    ctx->launches += 3;
+  // One Adam step: forward, residuals, backward, Adam, re-pack (7 to 8 launches).  The
+  // minibatch offsets, the cosine learning rate and the bias corrections depend on the
+  // step index alone (adam_t restarts at 0 with every training).
+  auto adam_loop = [&]() -> myql_status {
+    for (uint32_t it = 0; it < iters; ++it) {
+      const uint64_t b0 = (it * b_pb) % n_pb;
+      const uint64_t nb = std::min(b_pb, n_pb - b0);
+      const uint8_t *f = (const uint8_t *)S.p_feat.p + b0 * nh * kCvTileBytes;
+      const float *dm = (const float *)S.p_dM.p + b0 * nh * 128;
+      const float *Y = (const float *)S.p_Y.p + b0 * 128;
+      float *cvb = (float *)S.p_cv.p + b0 * 128;
+      myql_status s2 = forward(ctx, S, f, dm, nb * 128, nh, cvb, nullptr);
+      if (s2 != MYQL_OK) return s2;
+      cudaError_t e2 = launch_cv_resid(Y, cvb, nb * 128, (float *)S.coef.p, loss + (size_t)it * kResidBlocks,
+                                       (double *)S.rpart.p, ctx->stream);
+      if (e2 != cudaSuccess) return cuda_status(e2, "cv_resid launch");
+      s2 = backward(ctx, S, f, dm, nb * 128, nh);
+      if (s2 != MYQL_OK) return s2;
+      const double pi = 3.14159265358979323846;
+      const double lr = cfg->learning_rate * (0.05 + 0.95 * 0.5 * (1.0 + std::cos(pi * it / std::max(1u, iters))));
+      const double t = (double)(it + 1);
+      e2 = launch_cv_adam((float *)S.params.p, (float *)S.adam_m.p, (float *)S.adam_v.p, (const float *)S.grad.p,
+                          (float)lr, (float)(1.0 - std::pow(0.9, t)), (float)(1.0 - std::pow(0.999, t)), ctx->stream);
+      if (e2 == cudaSuccess)
+        e2 = launch_cv_pack((const float *)S.params.p, (uint8_t *)S.img.p, (float *)S.vec.p, ctx->stream);
+      if (e2 != cudaSuccess) return cuda_status(e2, "cv_adam launch");
+      ctx->launches += 3;
+    }
+    return MYQL_OK;
+  };
+  // The loop runs as one CUDA graph, captured on the first training of a shape (pilot
+  // paths, minibatch, hedge times, step count, learning rate, buffers) and replayed by the
+  // next training of the same shape: 7-8 launches per step become one graph launch.  Every
+  // buffer the loop touches is allocated, and the kernels' attributes set, before capture.
+  uint64_t key = 0xcbf29ce484222325ull;
+  auto mixk = [&](uint64_t v) { key = (key ^ v) * 0x100000001b3ull + (key >> 29); };
+  uint64_t lr_bits;
+  std::memcpy(&lr_bits, &cfg->learning_rate, 8);
+  for (uint64_t v : {P, (uint64_t)nh, bp, (uint64_t)iters, lr_bits})
+    mixk(v);
+  if (iters) {
+    // tile-major forward (fewer than 8 path blocks per SM): its row buffer at the largest such minibatch
+    const uint64_t tm_pb = std::min<uint64_t>(b_pb, (uint64_t)ctx->sm_count * 8 - 1);
+    e = S.gdm.ensure(tm_pb * nh * 128 * 4);
+    if (e == cudaSuccess) e = S.gpart.ensure((size_t)mlp_blocks(ctx, b_pb * nh) * kPCount * 4);
+    if (e == cudaSuccess) e = cv_prepare_kernels();
+    if (e != cudaSuccess) return cuda_status(e, "control-variate training set-up");
+  }
+  for (const DevBuf *b : {&S.p_feat, &S.p_dM, &S.p_Y, &S.p_cv, &S.coef, &S.loss, &S.params, &S.adam_m, &S.adam_v,
+                          &S.grad, &S.img, &S.vec, &S.gdm, &S.gpart, &S.rpart, &ctx->status})
+    mixk((uint64_t)(uintptr_t)b->p);
+  if (iters && (!S.train_graph || S.train_key != key)) {
+    if (S.train_graph) cudaGraphExecDestroy(S.train_graph);
+    S.train_graph = nullptr;
+    const uint32_t l0 = ctx->launches;
+    cudaGraph_t gr = nullptr;
+    e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_status(e, "control-variate training capture");
+    s = adam_loop();
+    cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &gr);
+    if (s != MYQL_OK) {
+      if (gr) cudaGraphDestroy(gr);
+      return s;
+    }
+    e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&S.train_graph, gr, 0);
+    if (gr) cudaGraphDestroy(gr);
+    if (e != cudaSuccess) {
+      S.train_graph = nullptr;
+      return cuda_status(e, "control-variate training graph");
+    }
+    S.train_key = key;
+    S.train_launches = ctx->launches - l0;
+    ctx->launches = l0;
+  }
+  if (iters) {
+    e = cudaGraphLaunch(S.train_graph, ctx->stream);
+    if (e != cudaSuccess) return cuda_status(e, "control-variate training graph launch");
+    ctx->launches += S.train_launches;
+    S.adam_t = iters;
   }
   // in-sample variance before / after, on the first min(P, 2^17) pilot paths (a diagnostic:
   // the out-of-sample ratio of myql_cv_price is the one that counts)

@@ -266,6 +266,7 @@ cudaError_t launch_cv_sim(const CvSimParams &P, int klass, cudaStream_t st);
 cudaError_t launch_mlmc_cv_level(const MlmcCvParams &Q, int klass, cudaStream_t st);
 cudaError_t launch_cv_mlp(const CvMlpParams &P, unsigned int blocks, cudaStream_t st);
 cudaError_t launch_cv_bwd(const CvMlpParams &P, unsigned int blocks, cudaStream_t st);
+cudaError_t cv_prepare_kernels();
 cudaError_t launch_cv_pack(const float *params, uint8_t *img, float *vec, cudaStream_t st);
 cudaError_t launch_cv_adam(float *params, float *m, float *v, const float *grad, float lr, float b1t, float b2t,
                            cudaStream_t st);

@@ -730,29 +730,44 @@ static void attr_set(std::atomic<unsigned long long> &done) {
   if (cudaGetDevice(&dev) == cudaSuccess && dev < 64) done.fetch_or(1ull << dev);
 }
 
+static std::atomic<unsigned long long> g_fwd_attr{0}, g_bwd_attr{0};
+
+static cudaError_t fwd_attributes() {
+  if (!attr_needed(g_fwd_attr)) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(dev::cv_mlp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(dev::cv_mlp_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
+  if (e == cudaSuccess) attr_set(g_fwd_attr);
+  return e;
+}
+
+static cudaError_t bwd_attributes() {
+  if (!attr_needed(g_bwd_attr)) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(dev::cv_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem);
+  if (e == cudaSuccess) attr_set(g_bwd_attr);
+  return e;
+}
+
+// The function attributes of both MLP kernels on the current device, set ahead of a
+// stream capture (no attribute call then happens while the training loop is captured).
+cudaError_t cv_prepare_kernels() {
+  cudaError_t e = fwd_attributes();
+  return e == cudaSuccess ? bwd_attributes() : e;
+}
+
 cudaError_t launch_cv_mlp(const CvMlpParams &P, unsigned int blocks, cudaStream_t st) {
-  static std::atomic<unsigned long long> attr{0};
-  if (attr_needed(attr)) {
-    cudaError_t e = cudaFuncSetAttribute(dev::cv_mlp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(dev::cv_mlp_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                               (int)cudaSharedmemCarveoutMaxShared);
-    if (e != cudaSuccess) return e;
-    attr_set(attr);
-  }
+  cudaError_t e = fwd_attributes();
+  if (e != cudaSuccess) return e;
   dev::cv_mlp_kernel<<<blocks, dev::kFwdThreads, kFwdSmem, st>>>(P);
   return cudaGetLastError();
 }
 
 cudaError_t launch_cv_bwd(const CvMlpParams &P, unsigned int blocks, cudaStream_t st) {
-  static std::atomic<unsigned long long> attr{0};
-  if (attr_needed(attr)) {
-    cudaError_t e = cudaFuncSetAttribute(dev::cv_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem);
-    if (e != cudaSuccess) return e;
-    attr_set(attr);
-  }
+  cudaError_t e = bwd_attributes();
+  if (e != cudaSuccess) return e;
   dev::cv_bwd_kernel<<<blocks, dev::kBwdThreads, kBwdSmem, st>>>(P);
-  cudaError_t e = cudaGetLastError();
+  e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   dev::cv_grad_reduce_kernel<<<(kPCount + 255) / 256, 256, 0, st>>>(P.gpart, blocks, P.grad);
   return cudaGetLastError();

@@ -727,11 +727,14 @@ def time_to_se(eng, m, kind: str, target: float, probe_paths: int = 1 << 22, top
         r, _ = eng.price(cv_jobs(m, kind, n, seed=sd)[0])
         return float(r[0, 0]), float(r[1, 0]), n
 
-    cv_last = {}
+    cv_last = {"sim_ms": 0.0, "mlp_ms": 0.0, "price_ms": 0.0}
 
     def cv_fn(n, sd):
         r = eng.cv_price(cv_jobs(m, kind, n, seed=sd)[0], cfg)
         cv_last["vr"] = r.variance_ratio
+        cv_last["sim_ms"] += r.simulate_ms
+        cv_last["mlp_ms"] += r.mlp_ms
+        cv_last["price_ms"] += r.total_ms
         return r.price, r.price_std_err, n
 
     torch.cuda.synchronize()
@@ -753,6 +756,12 @@ def time_to_se(eng, m, kind: str, target: float, probe_paths: int = 1 << 22, top
             "cv_pilot_paths": int(tr.paths), "cv_iterations": int(cfg.iterations),
             "cv_batch_paths": int(cfg.batch_paths), "cv_hedge_every": int(cfg.hedge_every),
             "variance_ratio": cv_last.get("vr"), "pricing_only_speedup": cv_last.get("vr", 0.0) * t_plain_path / t_cv_path,
+            # where the control variate's time goes (its own timers): pilot simulation and set-up,
+            # the Adam steps, then the pricing run's path simulation, MLP rows and the rest
+            "cv_breakdown_s": {"pilot_and_setup": (tr.total_ms - tr.train_ms) / 1e3, "adam_steps": tr.train_ms / 1e3,
+                               "price_simulate": cv_last["sim_ms"] / 1e3, "price_mlp": cv_last["mlp_ms"] / 1e3,
+                               "price_other": (cv_last["price_ms"] - cv_last["sim_ms"] - cv_last["mlp_ms"]) / 1e3,
+                               "host": t_cv - (tr.total_ms + cv_last["price_ms"]) / 1e3},
             "price_cv": c_mean, "price_plain": p_mean}
 
 

@@ -76,3 +76,33 @@ def test_directions_depend_on_the_seed_beyond_dimension_one():
     a, b = directions(50, 1), directions(50, 2)
     assert np.array_equal(a[:2], b[:2])      # van der Corput and the degree-1 polynomial are forced
     assert not np.array_equal(a[2:], b[2:])
+
+
+def t_value(xi, xj, m):
+    """The t of the first 2^m points of a 2-D projection: the smallest t such that every
+    elementary interval 2^-a x 2^-(m-t-a) holds exactly 2^t points."""
+    xi, xj = xi.astype(np.uint64), xj.astype(np.uint64)
+    for t in range(m + 1):
+        k = m - t
+        if all(np.all(np.bincount(((xi >> np.uint64(32 - a)) << np.uint64(k - a) |
+                                   (xj >> np.uint64(32 - (k - a)))).astype(np.int64),
+                                  minlength=1 << k) == (1 << t)) for a in range(k + 1)):
+            return t
+    return m
+
+
+def test_two_dimensional_projections_meet_the_sobol_t_bound():
+    """Every pair of the first 13 dimensions (polynomial degrees up to 5) is a (t, m, 2)-net
+    with t at most (s_i - 1) + (s_j - 1), the bound of Sobol's construction whatever the odd
+    initial direction numbers (dimension 0, van der Corput, counts as s = 1)."""
+    degrees = [1, 1, 2, 3, 3, 4, 4] + [5] * 6
+    V = directions(len(degrees))
+    m = 12
+    x = points(V, 1 << m)
+    ts = {}
+    for i in range(len(degrees)):
+        for j in range(i + 1, len(degrees)):
+            t = t_value(x[:, i], x[:, j], m)
+            ts[(i, j)] = t
+            assert t <= (degrees[i] - 1) + (degrees[j] - 1), (i, j, t)
+    assert ts[(0, 1)] == 0

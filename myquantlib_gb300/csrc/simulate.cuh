@@ -461,27 +461,28 @@ __device__ __forceinline__ void evolve_merged(const float (&v)[NS], float (&vn)[
                                               unsigned int &fallbacks) {
   bool same[NS];
   unsigned int nm = 0;
-  bool own = false;  // a v0-bumped scenario of this lane has not merged yet
 #pragma unroll
   for (int j = 0; j < NS; ++j) {
     same[j] = lockstep_merges(j) && v[j] == v[0];
     nm += same[j] ? 1u : 0u;
-    own |= lockstep_merges(j) && !same[j];
-  }
-  // A warp with an unmerged scenario on any lane evaluates every scenario in the shared
-  // interleaved inversion (one W, one summation loop) instead of running the unmerged
-  // scenarios' inversions one by one on the few lanes that need them.  The vote is only a
-  // choice of schedule: both branches give every scenario its own evaluation's value, and
-  // a lane outside the active mask votes for itself.
-  if (__any_sync(__activemask(), own)) {
-    evolve_lockstep<SCH_NCI, NS>(v, vn, d, P, fi, caphits, fallbacks);
-    return;
   }
   const float v3[3] = {v[0], v[3], v[4]};
   float o3[3];
   evolve_lockstep<SCH_NCI, 3, true>(v3, o3, d, P, fi, caphits, fallbacks, nm);
 #pragma unroll
-  for (int j = 0; j < NS; ++j) vn[j] = (j == 3 || j == 4) ? o3[j - 2] : o3[0];  // every other one merged
+  for (int j = 0; j < NS; ++j) {
+    if (j == 3 || j == 4) {
+      vn[j] = o3[j - 2];
+    } else if (j == 0 || same[j]) {
+      vn[j] = o3[0];
+    } else {
+      const FactorConst &f = P.sc[lockstep_sc(j)].f[fi];
+      const NciOne o = nci_step_one(f.w0 * v[j], f.w2, P.nci[fi], d.xp, d.U, d.x2, d.pos, P.loop_cap);
+      vn[j] = o.v;
+      caphits += o.caphits;
+      fallbacks += o.fallbacks;
+    }
+  }
 }
 
 // MERGE: the v0-bumped scenarios' variance paths merge into the base's (every

@@ -298,6 +298,27 @@ LOCKSTEP = {
 LOCKSTEP_CASES = [(n, 40) for n in LOCKSTEP] + [(n, 200) for n in ("bates_nci", "dbates_nci_nci")]
 
 
+@pytest.mark.parametrize("T", [0.25, 1.0, 4.0])
+def test_t_bumped_counts_shared_at_scale(engine, T):
+    """The lockstep kernel's records at the headline strip's scale: the Bates SchemeNCI model
+    and step size (200 a year), 2^20 paths of 50 to 800 steps.  The base and the T-bumped
+    scenarios, evolved together on shared draws (with the merged v0-bumped variance paths),
+    must equal requests that price T and T +- t_bump alone, bit for bit."""
+    model, stepper = m.BatesModel(_H_NCI, _MJ), m.BatesStepper(m.SchemeNCI)
+    steps = int(round(200 * T))
+    cfg = m.MonteCarloConfig(num_paths=1 << 20, time_steps=steps, seed=11, n_streams=1 << 20)
+    full = m.make_job(model, stepper, m.EuropeanOption([100.0], T), m.GreekMode.FULL, cfg, 100.0, 0.02, 0.0)
+    g = engine.paths(full)
+
+    def single(t):
+        return engine.paths(m.make_job(model, stepper, m.EuropeanOption([100.0], t), m.GreekMode.NONE, cfg,
+                                       100.0, 0.02, 0.0))[0]
+
+    np.testing.assert_array_equal(g[3], single(T + cfg.t_bump))
+    np.testing.assert_array_equal(g[4], single(T - cfg.t_bump))
+    np.testing.assert_array_equal(g[0], single(T))
+
+
 @pytest.mark.parametrize("name,steps", LOCKSTEP_CASES, ids=[f"{n}-{k}" for n, k in LOCKSTEP_CASES])
 def test_full_greek_scenarios_equal_single_scenario_runs(engine, name, steps):
     """Full Greeks of a European advance every bumped scenario of a path in lockstep

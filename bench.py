@@ -143,6 +143,17 @@ def read_traffic() -> float | None:
     return None
 
 
+def read_issued() -> float | None:
+    """Lane-operations the lockstep kernel issues per simulated scenario path-step, from the ncu
+    summary committed under profiles/ (warp instructions x active lanes / 32)."""
+    p = ROOT / "profiles" / "simulate_lockstep_bates_nci_small.md"
+    if p.exists():
+        for line in p.read_text().splitlines():
+            if line.startswith("issued_lane_ops_per_scenario_path_step:"):
+                return float(line.split(":", 1)[1])
+    return None
+
+
 def cpu_strip_pass(paths: int, cores: int) -> float:
     """Wall seconds of one pass of the reference's algorithm over the whole strip workload
     (8 maturities x 64 strikes, Full Greeks) at `paths` paths on `cores` OpenMP threads: the
@@ -349,6 +360,12 @@ def run_engine(args) -> dict:
             "xu": {"achieved": xu_ach / 1e9, "peak": xu_peak / 1e9, "frac": xu_frac, "ops_per_path_step": XU_PER_STEP},
             "simulate_ms_per_step": sim_ms, "payoff_ms_per_step": pay_ms,
             "traffic": read_traffic(),
+            "issued": None if read_issued() is None else {
+                "lane_ops_per_scenario_path_step": read_issued(),
+                "frac": alu_frac * read_issued() / ALU_PER_STEP,
+                "note": ("the lane-operations the kernel issues (ncu: warp instructions x active lanes), "
+                         "per second, against the same FP32 lane rate: what the hardware executes, where "
+                         "frac counts the contracted work")},
             "l2_gather": {"achieved": GATHER_BYTES * sim / (sim_ms / 1e3) / 1e9, "unit": "GB/s",
                           "note": ("16 B of NCI table per simulated scenario path-step, gathered from L2 (the "
                                    "18.5 MB table stays resident); an algorithmic rate, not DRAM traffic"),

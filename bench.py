@@ -952,10 +952,13 @@ def run_ncu_cv_case() -> None:
 
 
 def run_ncu_batch_case() -> None:
-    """A small batched case for ncu: the first 256 uneven requests at up to 2^16 paths, priced twice."""
+    """A small batched case for ncu: the first 256 uneven requests at up to 2^16 paths, priced twice,
+    on the default launch shape (the one the autotuner keeps on the full batch), so that the first
+    batch_kernel launch is a class kernel of the batch graph rather than a tuning candidate."""
     import myquantlib_gb300 as m
     from myquantlib_gb300 import workloads
     eng = m.Engine(0)
+    eng.set_batch_shape(128, 1, 0)
     rq = workloads.uneven_requests(256, max_log2_paths=16.0)
     jobs = [m.make_job(r.model, m.stepper_for(r.model, r.instrument, r.scheme), r.instrument, r.mode, r.cfg,
                        r.S0, r.r, r.q) for r in rq]

@@ -995,7 +995,8 @@ def main():
     ap.add_argument("--ncu-case", action="store_true",
                     help="profiling case: one maturity (T=1), 2^18 paths, two requests, no timing")
     ap.add_argument("--ncu-full", action="store_true",
-                    help="profiling case at the full 2^22 paths (for one-pass metrics only)")
+                    help="profiling case at the full 2^22 paths: for one-pass metrics (DRAM bytes, duration) "
+                         "captured on one kernel (-k) and one launch (-c 1) only")
     args = ap.parse_args()
     if args.ncu_case or args.ncu_full:
         if args.workload == "cv":

@@ -784,17 +784,20 @@ def time_to_se(eng, m, kind: str, target: float, probe_paths: int = 1 << 22, top
 
 def cv_report(eng, m) -> dict:
     """The time-to-relative-SE block: the Double Bates arithmetic Asian at 1e-3 and 1e-4 and the
-    Heston European at 1e-4, neural control variate against plain GPU Monte Carlo, plus the
-    European by randomized QMC; clocks sampled over the whole block."""
+    Heston European at 1e-4, neural control variate against plain GPU Monte Carlo, plus the same
+    workloads by randomized QMC; clocks sampled over the whole block."""
     for kind in ("asian", "european"):  # warm-up: tables, stream tables, first launches
         eng.price(cv_jobs(m, kind, 1 << 16)[0])
         eng.cv_train(cv_jobs(m, kind, 1 << 16)[0], cv_config(m, kind, pilot=1 << 16, iterations=10))
     eng.qmc_price(cv_jobs(m, "european", 1 << 19)[0], 16)
+    eng.qmc_price(cv_jobs(m, "asian", 1 << 19)[0], 16)
     with ClockSampler(eng.device) as clk:
         res = {"asian_1e-3": time_to_se(eng, m, "asian", 1e-3),
                "asian_1e-4": time_to_se(eng, m, "asian", 1e-4),
                "european_1e-4": time_to_se(eng, m, "european", 1e-4),
-               "european_qmc_1e-4": qmc_time_to_se(eng, m)}
+               "european_qmc_1e-4": qmc_time_to_se(eng, m, "european", 1e-4),
+               "asian_qmc_1e-3": qmc_time_to_se(eng, m, "asian", 1e-3),
+               "asian_qmc_1e-4": qmc_time_to_se(eng, m, "asian", 1e-4)}
     res["clocks"] = clk.summary()
     res["method"] = ("wall time through the public API, synchronised; each arm sized by an untimed probe "
                      "and topped up on fresh seeds until its estimated relative SE meets the target; the "
@@ -802,23 +805,25 @@ def cv_report(eng, m) -> dict:
     return res
 
 
-def qmc_time_to_se(eng, m, target: float = 1e-4, R: int = 16, probe_paths: int = 1 << 20) -> dict:
-    """The Heston European call of the control-variate comparison (SchemeNV, 100 steps) priced
-    by randomized quasi-Monte Carlo (Sobol + Brownian bridge, R digital shifts): wall time
-    to the relative standard error target against plain GPU Monte Carlo.  The probe fixes
-    the QMC error at one size; the timed run starts at the path count that the plain 1/sqrt(n)
-    rate gives for 0.8 x the target, rounded up to a power of two per replicate, and doubles the
-    points per replicate while the estimated error (R replicates, so itself noisy) is above
-    the target: every attempt is inside the timed region."""
+def qmc_time_to_se(eng, m, kind: str = "european", target: float = 1e-4, R: int = 16,
+                   probe_paths: int = 1 << 20) -> dict:
+    """A control-variate workload (the Heston European call, SchemeNV, 100 steps, or the Double
+    Bates arithmetic Asian, SchemeNCI factors and Merton jumps, 256 steps) priced by randomized
+    quasi-Monte Carlo (Sobol + Brownian bridge for the normals, Sobol uniforms for the NCI and jump
+    draws, R digital shifts): wall time to the relative standard error target against plain GPU
+    Monte Carlo.  The probe fixes the QMC error at one size; the timed run starts at the path count
+    that the plain 1/sqrt(n) rate gives for 0.8 x the target, rounded up to a power of two per
+    replicate, and doubles the points per replicate while the estimated error (R replicates, so
+    itself noisy) is above the target: every attempt is inside the timed region."""
     import torch
-    job, steps = cv_jobs(m, "european", probe_paths)
+    job, steps = cv_jobs(m, kind, probe_paths)
     q, _ = eng.qmc_price(job, R)
     need = probe_paths * (q[1, 0] / (0.8 * target * q[0, 0])) ** 2  # 1.25x margin on the noisy estimate
     pts = 2048
     while pts * R < need:  # a power of two per replicate: the balanced Sobol point sets
         pts *= 2
     n_q = pts * R
-    pj, _ = cv_jobs(m, "european", 1 << 22)
+    pj, _ = cv_jobs(m, kind, 1 << 22)
     raw, _ = eng.price(pj)
     n_plain = int((1 << 22) * (raw[1, 0] / (target * raw[0, 0])) ** 2) + 1
     torch.cuda.synchronize()
@@ -826,17 +831,18 @@ def qmc_time_to_se(eng, m, target: float = 1e-4, R: int = 16, probe_paths: int =
     attempts = 0
     while True:
         attempts += 1
-        q, _ = eng.qmc_price(cv_jobs(m, "european", n_q, seed=48)[0], R)
+        q, _ = eng.qmc_price(cv_jobs(m, kind, n_q, seed=48)[0], R)
         if q[1, 0] <= target * q[0, 0] or attempts == 6:
             break
         n_q *= 2
     t_q = time.perf_counter() - t0
     t0 = time.perf_counter()
-    raw, _ = eng.price(cv_jobs(m, "european", n_plain, seed=49)[0])
+    raw, _ = eng.price(cv_jobs(m, kind, n_plain, seed=49)[0])
     t_plain = time.perf_counter() - t0
-    return {"instrument": "Heston European call (SchemeNV, 100 steps)", "target_rel_se": target, "replicates": R,
-            "qmc_paths": n_q, "qmc_attempts": attempts, "qmc_s": t_q, "qmc_rel_se": q[1, 0] / q[0, 0],
-            "plain_paths": n_plain,
+    return {"instrument": ("Heston European call (SchemeNV, 100 steps)" if kind == "european" else
+                           "Double Bates arithmetic Asian call (SchemeNCI factors, Merton jumps, 256 steps)"),
+            "target_rel_se": target, "replicates": R, "qmc_paths": n_q, "qmc_attempts": attempts, "qmc_s": t_q,
+            "qmc_rel_se": q[1, 0] / q[0, 0], "plain_paths": n_plain,
             "plain_s": t_plain, "plain_rel_se": raw[1, 0] / raw[0, 0], "speedup": t_plain / t_q,
             "price_qmc": q[0, 0], "price_plain": raw[0, 0]}
 

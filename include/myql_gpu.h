@@ -355,11 +355,15 @@ myql_status myql_ml2r_price(myql_ctx *ctx, const myql_mc_job *job, const myql_ml
 /* Randomized quasi-Monte Carlo (the reference's future work, README.md:331):
  * Sobol points (Gray-code order; direction numbers from primitive polynomials by
  * the Bratley-Fox recurrence with seeded odd initial values), a Brownian bridge
- * per Brownian motion (spot and each CIR factor, bridge levels interleaved), and
- * n_replicates random digital shifts.  out: price rows as myql_mc_price (standard
- * error from the spread of the replicate estimates).  Models without jumps, every
- * factor on SchemeNV, GreekMode None, at most 512 steps, num_paths a multiple of
- * 2048 * n_replicates (n_replicates >= 2). */
+ * per Brownian motion (the spot and each SchemeNV factor, bridge levels
+ * interleaved), two Sobol uniforms per step for each SchemeNCI factor (its
+ * Poisson count and chi-squared table, by inversion) and for Merton jumps (the
+ * count and the normal of the jump sum, drawn per step for every instrument),
+ * and n_replicates random digital shifts.  out: price rows as myql_mc_price
+ * (standard error from the spread of the replicate estimates).  Factors on
+ * SchemeNV or SchemeNCI, no jumps or Merton jumps (SchemeExact and Kou jumps
+ * have no fixed number of draws per step), GreekMode None, at most 512 steps,
+ * num_paths a multiple of 2048 * n_replicates (n_replicates >= 2). */
 myql_status myql_qmc_price(myql_ctx *ctx, const myql_mc_job *job, uint32_t n_replicates, double *out,
                            myql_mc_stats *stats);
 /* The Sobol direction numbers of myql_qmc_price: out[d * 32 + k - 1] = V_k of

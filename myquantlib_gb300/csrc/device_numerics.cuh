@@ -487,9 +487,8 @@ __device__ __forceinline__ int poisson_inv(float lam, unsigned long long x, unsi
 // remaining mass is too (below the FP32 resolution of u), so the draw is in
 // the last 1e-8 of the distribution and k is returned; a draw that stops by
 // the ordinary test never gets there (its last term is at least about 1e-8).
-__device__ __forceinline__ int poisson_small(float mean, float exp_neg_mean, Xo &rng,
-                                             unsigned int cap, unsigned int &caphits) {
-  float u = u01_bits(draw(rng));
+__device__ __forceinline__ int poisson_small_u(float mean, float exp_neg_mean, float u, unsigned int cap,
+                                               unsigned int &caphits) {
   float p = exp_neg_mean;
   int k = 0;
   while (u > p) {
@@ -503,6 +502,11 @@ __device__ __forceinline__ int poisson_small(float mean, float exp_neg_mean, Xo 
     p = __fdividef(mean * p, (float)k);
   }
   return k;
+}
+
+__device__ __forceinline__ int poisson_small(float mean, float exp_neg_mean, Xo &rng,
+                                             unsigned int cap, unsigned int &caphits) {
+  return poisson_small_u(mean, exp_neg_mean, u01_bits(draw(rng)), cap, caphits);
 }
 
 // Exponential(rate) draw: -log(1 - U) / rate from one uniform.

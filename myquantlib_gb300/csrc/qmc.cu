@@ -14,12 +14,22 @@
 //   * R independent random digital shifts (one 32-bit XOR mask per replicate and
 //     dimension) give R unbiased replicate estimates; the price is their mean and
 //     the standard error comes from their spread.
-// Each factor is stepped with SchemeNV (one normal per step, VolSchemes.hpp:52-57),
-// the log-spot as in ASVJstepper.hpp:134-229, and the trackers of the path
-// kernels; the per-path records go through the engine's own payoff pass.
-// Fixed dimension per step is what QMC needs, so the schemes with a variable
-// number of draws per step (Exact, NCI's Poisson mixture) and the jump
-// policies are not offered.
+// QMC needs a fixed number of draws per step, and these steppers have one:
+//   * SchemeNV factors: one normal per step (VolSchemes.hpp:52-57), from a bridge
+//     like the spot's;
+//   * SchemeNCI factors: two uniforms per step (VolSchemes.hpp:334-370), the
+//     Poisson count's by inversion and the chi-squared table's, taken directly
+//     from two Sobol coordinates;
+//   * Merton jumps: two uniforms per step, the count's by sequential inversion
+//     and the normal of the jump sum (n mu + sqrt(n) delta Z, JumpPolicies.hpp:55-75);
+//     the jumps of every instrument are drawn per step, whose sum has the law of
+//     the one draw over T a European stepper makes.
+// The bridge dimensions come first (b * NG + c for bridge point b and Gaussian
+// motion c), then the per-step uniforms (n NG + k NU + u).  SchemeExact (a
+// rejection loop) and Kou jumps (one exponential per jump) have a variable number
+// of draws and are not offered.  The log-spot steps as in ASVJstepper.hpp:134-229,
+// with the trackers of the path kernels; the per-path records go through the
+// engine's own payoff pass.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -40,7 +50,10 @@ struct QmcParams {
   const int *br_mid, *br_left, *br_right;  // Brownian bridge, construction order
   const float *br_wl, *br_wr, *br_sd;
   unsigned long long n_pts;    // points per replicate
-  unsigned int D;              // dimensions per path = steps * (1 + factors)
+  unsigned int D;              // dimensions per path = steps * (NG + NU)
+  int sch[2];                  // scheme of each factor: SCH_NV or SCH_NCI
+  int jump;                    // 0 none, 1 Merton (per step)
+  int NG, NU;                  // Gaussian motions (spot + NV factors), uniforms per step
 };
 
 namespace dev {
@@ -52,6 +65,14 @@ __device__ __forceinline__ uint32_t sobol_coord(const uint32_t *V, uint32_t g) {
   return x;
 }
 
+// 64-bit draw of a shifted Sobol coordinate: the centre of its 2^-32 cell, so that
+// u01_bits, u01c_bits and inv_normal_bits of it are the coordinate's uniform.
+__device__ __forceinline__ unsigned long long qmc_draw(const QmcParams &Q, const uint32_t *shift, uint32_t g,
+                                                       unsigned int d) {
+  const uint32_t x = sobol_coord(Q.dirs + (size_t)d * kQmcBits, g) ^ __ldg(shift + d);
+  return ((unsigned long long)x << 32) | 0x80000000ull;
+}
+
 template <int NF, bool PD>
 __global__ void __launch_bounds__(kSimBlock) qmc_kernel(const __grid_constant__ QmcParams Q) {
   const SimParams &P = Q.P;
@@ -60,7 +81,8 @@ __global__ void __launch_bounds__(kSimBlock) qmc_kernel(const __grid_constant__ 
   const unsigned long long rep = i / Q.n_pts, pt = i % Q.n_pts;
   const uint32_t g = (uint32_t)(pt ^ (pt >> 1));  // Gray code
   const int n = P.n_steps;
-  constexpr int NC = 1 + NF;  // Brownian motions: the spot's, then one per factor
+  constexpr int NC = 1 + NF;  // at most: the spot's motion and one per NV factor
+  const int NG = Q.NG;
   const uint32_t *shift = Q.shift + rep * Q.D;
   float W[NC][kQmcMaxSteps + 1];
 #pragma unroll
@@ -70,42 +92,68 @@ __global__ void __launch_bounds__(kSimBlock) qmc_kernel(const __grid_constant__ 
     const float wl = Q.br_wl[b], wr = Q.br_wr[b], sd = Q.br_sd[b];
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
-      const unsigned int d = (unsigned int)b * NC + c;
-      const uint32_t x = sobol_coord(Q.dirs + (size_t)d * kQmcBits, g) ^ __ldg(shift + d);
-      const float z = inv_normal_bits(((unsigned long long)x << 32) | 0x80000000ull);
+      if (c >= NG) break;
+      const unsigned int d = (unsigned int)b * NG + c;
+      const float z = inv_normal_bits(qmc_draw(Q, shift, g, d));
       W[c][m] = fmaf(wl, W[c][l], fmaf(wr, W[c][r], sd * z));
     }
   }
   const ScenarioConst &C = P.sc[0];
-  float X = 0.0f, va = C.f[0].v0, vb = C.f[1].v0;
+  float X = 0.0f, v[2] = {C.f[0].v0, C.f[1].v0};
   TrackerState ts;
   ts.init(P, PD);
   const float dt = C.dt;
+  unsigned int caphits = 0, fallbacks = 0;
+  const unsigned int ubase = (unsigned int)n * NG;
   for (int k = 0; k < n; ++k) {
     const float G = W[0][k + 1] - W[0][k];
+    unsigned int du = ubase + (unsigned int)k * Q.NU;  // this step's uniforms
     if (NF == 0) {
       X += fmaf(C.gbm_vol, G, C.gbm_drift);
     } else {
-      const FactorConst &f0 = C.f[0];
-      const float Za = W[1][k + 1] - W[1][k];
-      const float ra = sqrt_approx(fmaf(f0.w0, va, f0.w1)) + f0.w2 * Za;
-      const float van = fmaf(f0.w0 * ra, ra, f0.w1);
-      if (NF == 1) {
-        const float root = sqrt_approx(f0.C3 * (va + van));
-        const float drift = fmaf(f0.C2, van, fmaf(f0.C1, va, f0.C0));
-        X += fmaf(root, G, drift);
-        va = van;
-      } else {
-        const FactorConst &f1 = C.f[1];
-        const float Zb = W[NC - 1][k + 1] - W[NC - 1][k];
-        const float rb = sqrt_approx(fmaf(f1.w0, vb, f1.w1)) + f1.w2 * Zb;
-        const float vbn = fmaf(f1.w0 * rb, rb, f1.w1);
-        const float root = sqrt_approx(fmaf(f0.C3, va + van, f1.C3 * (vb + vbn)));
-        const float drift = fmaf(f1.C2, vbn, fmaf(f1.C1, vb, fmaf(f0.C2, van, fmaf(f0.C1, va, f0.C0 + f1.C0))));
-        X += fmaf(root, G, drift);
-        va = van;
-        vb = vbn;
+      float vn[2] = {0.0f, 0.0f};
+      int gi = 1;  // next Gaussian motion (NV factors, in factor order)
+#pragma unroll
+      for (int f = 0; f < NF; ++f) {
+        const FactorConst &fc = C.f[f];
+        if (Q.sch[f] == SCH_NV) {
+          const float Z = gi == 1 ? W[1][k + 1] - W[1][k] : W[NC - 1][k + 1] - W[NC - 1][k];
+          ++gi;
+          const float rt = sqrt_approx(fmaf(fc.w0, v[f], fc.w1)) + fc.w2 * Z;
+          vn[f] = fmaf(fc.w0 * rt, rt, fc.w1);
+        } else {  // SchemeNCI: N ~ Poisson(C0 v) by inversion, then the table at the second uniform
+          const unsigned long long xp = qmc_draw(Q, shift, g, du), x2 = qmc_draw(Q, shift, g, du + 1);
+          du += 2;
+          const float lam = fc.w0 * v[f];
+          const float Wp = lam > kPoissonAsymMin ? inv_normal_bits(xp) : 0.0f;
+          const int N = poisson_core(lam, u01_bits(xp), Wp, xp, P.loop_cap, caphits);
+          vn[f] = nci_quantile(P.nci[f], N, x2, P.nci_u999, fallbacks) * fc.w2;
+        }
       }
+      if (NF == 1) {
+        const FactorConst &f0 = C.f[0];
+        const float root = sqrt_approx(f0.C3 * (v[0] + vn[0]));
+        const float drift = fmaf(f0.C2, vn[0], fmaf(f0.C1, v[0], f0.C0));
+        X += fmaf(root, G, drift);
+      } else {
+        const FactorConst &f0 = C.f[0];
+        const FactorConst &f1 = C.f[1];
+        const float root = sqrt_approx(fmaf(f0.C3, v[0] + vn[0], f1.C3 * (v[1] + vn[1])));
+        const float drift = fmaf(f1.C2, vn[1], fmaf(f1.C1, v[1], fmaf(f0.C2, vn[0], fmaf(f0.C1, v[0], f0.C0 + f1.C0))));
+        X += fmaf(root, G, drift);
+      }
+      v[0] = vn[0];
+      v[1] = vn[1];
+    }
+    if (Q.jump) {  // Merton, per step: count by sequential inversion, then one normal for the sum
+      const unsigned long long xc = qmc_draw(Q, shift, g, du), xz = qmc_draw(Q, shift, g, du + 1);
+      const int nj = poisson_small_u(C.jump_mean, C.jump_exp_neg_mean, u01_bits(xc), P.loop_cap, caphits);
+      float J = C.jump_comp;
+      if (nj > 0) {
+        const float fn = (float)nj;
+        J += fn * P.merton_mu + sqrtf(fn) * P.merton_delta * inv_normal_bits(xz);
+      }
+      X += J;
     }
     if (PD) ts.step(P, k, dt, X);
   }
@@ -113,6 +161,8 @@ __global__ void __launch_bounds__(kSimBlock) qmc_kernel(const __grid_constant__ 
   ts.finish(P, C, X, PD, out);
   const int F = P.n_fields;
   for (int f = 0; f < F; ++f) P.records[(size_t)f * P.rec_stride + i] = out[f];
+  if (caphits) atomicAdd(P.status, caphits);
+  if (fallbacks) atomicAdd(P.status + 1, fallbacks);
 }
 
 }  // namespace dev
@@ -256,11 +306,18 @@ extern "C" myql_status myql_qmc_price(myql_ctx *ctx_, const myql_mc_job *job, ui
   myql_status s = validate_job(*job);
   if (s != MYQL_OK) return s;
   const int nf = job->model.num_factors;
-  for (int f = 0; f < nf; ++f)
-    if (job->config.scheme[f] != MYQL_SCHEME_NV)
-      return set_error(MYQL_ERR_UNSUPPORTED, "quasi-Monte Carlo steps the CIR factors with SchemeNV only");
-  if (job->model.jump != MYQL_JUMP_NONE)
-    return set_error(MYQL_ERR_UNSUPPORTED, "quasi-Monte Carlo supports models without jumps");
+  int n_nv = 0, n_nci = 0;
+  for (int f = 0; f < nf; ++f) {
+    if (job->config.scheme[f] == MYQL_SCHEME_NV) ++n_nv;
+    else if (job->config.scheme[f] == MYQL_SCHEME_NCI) ++n_nci;
+    else
+      return set_error(MYQL_ERR_UNSUPPORTED,
+                       "quasi-Monte Carlo steps the CIR factors with SchemeNV or SchemeNCI (SchemeExact's "
+                       "rejection loop has no fixed number of draws)");
+  }
+  if (job->model.jump == MYQL_JUMP_KOU)
+    return set_error(MYQL_ERR_UNSUPPORTED,
+                     "quasi-Monte Carlo supports Merton jumps or none (Kou draws one exponential per jump)");
   if (job->config.greek_mode != MYQL_GREEKS_NONE)
     return set_error(MYQL_ERR_UNSUPPORTED, "quasi-Monte Carlo prices only (GreekMode None)");
   const uint64_t M = job->config.num_paths, R = n_replicates;
@@ -276,7 +333,8 @@ extern "C" myql_status myql_qmc_price(myql_ctx *ctx_, const myql_mc_job *job, ui
   if (e != cudaSuccess) return cuda_status(e, "cudaSetDevice");
   if (!ctx->qmc) ctx->qmc.reset(new QmcState);
   QmcState &S = *static_cast<QmcState *>(ctx->qmc.get());
-  const unsigned int D = (unsigned int)pl.steps * (unsigned int)(1 + nf);
+  const int NG = 1 + n_nv, NU = 2 * n_nci + (job->model.jump == MYQL_JUMP_MERTON ? 2 : 0);
+  const unsigned int D = (unsigned int)pl.steps * (unsigned int)(NG + NU);
   const uint64_t seed = job->config.seed;
   cudaStream_t st = ctx->stream;
   ctx->launches = 0;
@@ -346,6 +404,17 @@ extern "C" myql_status myql_qmc_price(myql_ctx *ctx_, const myql_mc_job *job, ui
   Q.br_sd = (const float *)(bb + 20 * n);
   Q.n_pts = M / R;
   Q.D = D;
+  Q.NG = NG;
+  Q.NU = NU;
+  Q.jump = job->model.jump == MYQL_JUMP_MERTON ? 1 : 0;
+  for (int f = 0; f < nf; ++f) {
+    Q.sch[f] = job->config.scheme[f] == MYQL_SCHEME_NCI ? dev::SCH_NCI : dev::SCH_NV;
+    if (Q.sch[f] == dev::SCH_NCI) {
+      s = ensure_nci(ctx, job->model.heston[f], (double)pl.sim.sc[0].dt, Q.P.nci[f]);
+      if (s != MYQL_OK) return s;
+    }
+  }
+  Q.P.loop_cap = ctx->loop_cap;
   cudaEvent_t sa = ctx->phase_event(), sb = ctx->phase_event();
   cudaEventRecord(sa, st);
   e = launch_qmc(Q, nf, pl.path_dep, st);

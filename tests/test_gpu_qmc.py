@@ -1,6 +1,7 @@
 """GPU tests of randomized quasi-Monte Carlo (myql_qmc_price): unbiased against the plain
-engine at the same time grid, against the reference's Fourier value, and with a variance
-gain at equal path counts; unsupported configurations are refused with their status."""
+engine at the same time grid (SchemeNV and SchemeNCI factors, Merton jumps), against the
+reference's Fourier values, and with a variance gain at equal path counts; unsupported
+configurations (SchemeExact, Kou jumps) are refused with their status."""
 import numpy as np
 import pytest
 
@@ -17,6 +18,11 @@ def job(model, stepper, instr, paths, steps, seed=7):
                       m.MonteCarloConfig(num_paths=paths, time_steps=steps, seed=seed), 100.0, 0.02, 0.0)
 
 
+HB = m.HestonParams(2.0, 0.05, 0.9, -0.6, 0.05)        # Feller violated: SchemeNCI only
+C4_F1 = m.HestonParams(2.0, 0.03, 0.4, -0.7, 0.03)     # the Double Bates Asian's factors
+C4_F2 = m.HestonParams(0.5, 0.02, 0.3, -0.3, 0.02)
+C4_JUMP = m.MertonParams(0.3, -0.05, 0.1)
+
 CASES = {
     "heston_call": (m.HestonModel(H1), m.HestonStepper(m.SchemeNV), lambda: m.EuropeanOption([90.0, 100.0, 110.0], 1.0), 64),
     "bs_arith_asian": (m.BlackScholesModel(0.2), m.BlackScholesStepper(m.TrackerArithAsian),
@@ -25,9 +31,20 @@ CASES = {
                      lambda: m.EuropeanOption(100.0, 1.0), 32),
     "heston_uo_call": (m.HestonModel(H1), m.HestonStepper(m.SchemeNV, m.TrackerBarrier),
                        lambda: m.UpAndOutCall(100.0, 130.0, 1.0), 64),
+    # SchemeNCI factors (Poisson and chi-squared uniforms from Sobol coordinates) and Merton jumps
+    "heston_nci_call": (m.HestonModel(HB), m.HestonStepper(m.SchemeNCI), lambda: m.EuropeanOption([90.0, 100.0, 110.0], 1.0), 64),
+    "bates_nci_asian": (m.BatesModel(HB, m.MertonParams(0.5, -0.1, 0.15)),
+                        m.BatesStepper(m.SchemeNCI, m.TrackerArithAsian),
+                        lambda: m.AsianOption(m.TrackerArithAsian, m.PayoffVanilla(), True, 100.0, 1.0), 64),
+    "dbates_nci_nci_asian": (m.DoubleBatesModel(C4_F1, C4_F2, C4_JUMP),
+                             m.DoubleBatesStepper(m.SchemeNCI, m.SchemeNCI, m.TrackerArithAsian),
+                             lambda: m.AsianOption(m.TrackerArithAsian, m.PayoffVanilla(), True, 100.0, 2.0), 64),
+    "dbates_nv_nci_call": (m.DoubleBatesModel(C4_F1, C4_F2, C4_JUMP), m.DoubleBatesStepper(m.SchemeNV, m.SchemeNCI),
+                           lambda: m.EuropeanOption(100.0, 1.0), 32),
 }
 # least variance ratio (plain variance / QMC variance, equal paths) each case must show
-GAIN = {"heston_call": 5.0, "bs_arith_asian": 20.0, "dheston_call": 5.0, "heston_uo_call": 1.0}
+GAIN = {"heston_call": 5.0, "bs_arith_asian": 20.0, "dheston_call": 5.0, "heston_uo_call": 1.0,
+        "heston_nci_call": 1.0, "bates_nci_asian": 1.0, "dbates_nci_nci_asian": 1.0, "dbates_nv_nci_call": 1.0}
 
 
 @pytest.mark.parametrize("name", list(CASES))
@@ -42,7 +59,12 @@ def test_qmc_unbiased_with_variance_gain(engine, name):
     var_plain = se_p ** 2 * (1 << 22) / paths
     ratio = var_plain / np.maximum(se_q ** 2, 1e-300)
     assert np.all(ratio > GAIN[name]), ratio
-    assert st.kernel_launches == 2 and st.paths == paths
+    assert st.paths == paths
+    # a second call reuses the tables (Sobol directions, bridge, NCI): the simulation and
+    # payoff launches only, and the same replicate estimates bit for bit
+    q2, st2 = engine.qmc_price(job(model, stepper, instr(), paths, steps), R)
+    assert st2.kernel_launches == 2
+    np.testing.assert_array_equal(q2, q)
 
 
 def test_qmc_heston_call_against_fourier(engine):
@@ -53,15 +75,30 @@ def test_qmc_heston_call_against_fourier(engine):
 
 
 def test_qmc_refuses_unsupported_configurations(engine):
-    bates = m.BatesModel(H1, m.MertonParams(0.5, -0.1, 0.15))
+    # Kou jumps (one exponential per jump) and SchemeExact (a rejection loop) have no fixed draw count
+    kou = m.BatesKouModel(H1, m.KouParams(0.5, 0.4, 10.0, 5.0))
     with pytest.raises(_abi.MyqlError) as e:
-        engine.qmc_price(job(bates, m.BatesStepper(m.SchemeNV), m.EuropeanOption(100.0, 1.0), 1 << 16, 16), 8)
+        engine.qmc_price(job(kou, m.BatesKouStepper(m.SchemeNV), m.EuropeanOption(100.0, 1.0), 1 << 16, 16), 8)
     assert e.value.status == _abi.ERR_UNSUPPORTED
     with pytest.raises(_abi.MyqlError) as e:
-        engine.qmc_price(job(m.HestonModel(H1), m.HestonStepper(m.SchemeNCI), m.EuropeanOption(100.0, 1.0),
+        engine.qmc_price(job(m.HestonModel(H1), m.HestonStepper(m.SchemeExact), m.EuropeanOption(100.0, 1.0),
                              1 << 16, 16), 8)
     assert e.value.status == _abi.ERR_UNSUPPORTED
     with pytest.raises(_abi.MyqlError) as e:
         engine.qmc_price(job(m.HestonModel(H1), m.HestonStepper(m.SchemeNV), m.EuropeanOption(100.0, 1.0),
                              3 * 2048, 16), 2)
     assert e.value.status == _abi.ERR_INVALID_ARG
+
+
+def test_qmc_bates_nci_call_against_fourier(engine):
+    """SchemeNCI with Merton jumps: the Bates call of the headline strip (T = 1, 200 steps) against
+    the reference's FP64 Fourier value (9.675798595347402, K 100.6349), on the NCI tables whose
+    cells keep the chi-squared mean (the reference's cells bias long paths slightly)."""
+    model = m.BatesModel(HB, m.MertonParams(0.5, -0.1, 0.15))
+    engine.set_nci_slopes(1)
+    try:
+        q, _ = engine.qmc_price(job(model, m.BatesStepper(m.SchemeNCI),
+                                    m.EuropeanOption(100.63492063492063, 1.0), 1 << 20, 200), 32)
+    finally:
+        engine.set_nci_slopes(0)
+    assert abs(q[0, 0] - 9.675798595347402) < 4 * q[1, 0] + 2e-3, (q[0, 0], q[1, 0])

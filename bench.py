@@ -805,46 +805,58 @@ def cv_report(eng, m) -> dict:
     return res
 
 
+def _pool_qmc(parts):
+    """Pools independent randomized-QMC estimates (price, standard error, points), weighted by
+    their point counts: at the c / sqrt(n) rate that weighting matches one run of all the points."""
+    n = sum(p for _, _, p in parts)
+    mean = sum(p * v for v, _, p in parts) / n
+    return mean, float(np.sqrt(sum((p * se) ** 2 for _, se, p in parts))) / n, n
+
+
 def qmc_time_to_se(eng, m, kind: str = "european", target: float = 1e-4, R: int = 16,
-                   probe_paths: int = 1 << 20) -> dict:
+                   probe_paths: int = 1 << 20, top_ups: int = 4) -> dict:
     """A control-variate workload (the Heston European call, SchemeNV, 100 steps, or the Double
     Bates arithmetic Asian, SchemeNCI factors and Merton jumps, 256 steps) priced by randomized
     quasi-Monte Carlo (Sobol + Brownian bridge for the normals, Sobol uniforms for the NCI and jump
     draws, R digital shifts): wall time to the relative standard error target against plain GPU
-    Monte Carlo.  The probe fixes the QMC error at one size; the timed run starts at the path count
-    that the plain 1/sqrt(n) rate gives for 0.8 x the target, rounded up to a power of two per
-    replicate, and doubles the points per replicate while the estimated error (R replicates, so
-    itself noisy) is above the target: every attempt is inside the timed region."""
+    Monte Carlo.  An untimed probe fixes the QMC error at one size.  The timed run prices the
+    point count that the plain 1/sqrt(n) rate gives for 0.9 x the target (a margin on the
+    R-replicate error estimate, itself noisy), in whole 2048-point blocks per replicate; while the
+    pooled error is still above the target it prices the shortfall on fresh seeds and pools the
+    runs (at most `top_ups` times), every run inside the timed region."""
     import torch
     job, steps = cv_jobs(m, kind, probe_paths)
     q, _ = eng.qmc_price(job, R)
-    need = probe_paths * (q[1, 0] / (0.8 * target * q[0, 0])) ** 2  # 1.25x margin on the noisy estimate
-    pts = 2048
-    while pts * R < need:  # a power of two per replicate: the balanced Sobol point sets
-        pts *= 2
-    n_q = pts * R
+    quantum = R * 2048
+
+    def size(n):  # whole 2048-point blocks per replicate
+        return max(-(-int(n) // quantum) * quantum, quantum)
+
+    n_q = size(probe_paths * (q[1, 0] / (0.9 * target * q[0, 0])) ** 2)
     pj, _ = cv_jobs(m, kind, 1 << 22)
     raw, _ = eng.price(pj)
     n_plain = int((1 << 22) * (raw[1, 0] / (target * raw[0, 0])) ** 2) + 1
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    attempts = 0
+    parts, n, runs = [], n_q, 0
     while True:
-        attempts += 1
-        q, _ = eng.qmc_price(cv_jobs(m, kind, n_q, seed=48)[0], R)
-        if q[1, 0] <= target * q[0, 0] or attempts == 6:
+        r, _ = eng.qmc_price(cv_jobs(m, kind, n, seed=48 + runs)[0], R)
+        parts.append((float(r[0, 0]), float(r[1, 0]), n))
+        runs += 1
+        mean, err, tot = _pool_qmc(parts)
+        if err <= target * mean or runs > top_ups:
             break
-        n_q *= 2
+        n = size(tot * ((err / (target * mean)) ** 2 - 1.0))
     t_q = time.perf_counter() - t0
     t0 = time.perf_counter()
     raw, _ = eng.price(cv_jobs(m, kind, n_plain, seed=49)[0])
     t_plain = time.perf_counter() - t0
     return {"instrument": ("Heston European call (SchemeNV, 100 steps)" if kind == "european" else
                            "Double Bates arithmetic Asian call (SchemeNCI factors, Merton jumps, 256 steps)"),
-            "target_rel_se": target, "replicates": R, "qmc_paths": n_q, "qmc_attempts": attempts, "qmc_s": t_q,
-            "qmc_rel_se": q[1, 0] / q[0, 0], "plain_paths": n_plain,
+            "target_rel_se": target, "replicates": R, "qmc_paths": tot, "qmc_runs": runs, "qmc_s": t_q,
+            "qmc_rel_se": err / mean, "plain_paths": n_plain,
             "plain_s": t_plain, "plain_rel_se": raw[1, 0] / raw[0, 0], "speedup": t_plain / t_q,
-            "price_qmc": q[0, 0], "price_plain": raw[0, 0]}
+            "price_qmc": mean, "price_plain": raw[0, 0]}
 
 
 def run_cv(args) -> dict:

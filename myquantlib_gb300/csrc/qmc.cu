@@ -2,9 +2,11 @@
 //
 // The reference lists quasi-Monte Carlo as future work (README.md:331).  Here a
 // path's normals come from a Sobol point instead of xoshiro draws:
-//   * Sobol points in Gray-code order (Antonov-Saleev), direction numbers from
-//     primitive polynomials over GF(2) by the Bratley-Fox recurrence (ACM TOMS
-//     659), dimension 0 the van der Corput sequence.  The initial direction
+//   * Sobol points in Gray-code order (Antonov-Saleev), generated a warp at a time:
+//     32 consecutive points share the Gray code's high bits, so one pass over 32
+//     dimensions builds their 32 x 32 coordinates in shared memory (SobolWarp);
+//     direction numbers from primitive polynomials over GF(2) by the Bratley-Fox
+//     recurrence (ACM TOMS 659), dimension 0 the van der Corput sequence.  The initial direction
 //     numbers m_1..m_s of each dimension are odd integers m_k < 2^k drawn from
 //     splitmix64 (a randomly initialised Sobol sequence, not a published table);
 //   * each Brownian motion of the step (the spot's and one per CIR factor) is
@@ -33,6 +35,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <utility>
 #include <vector>
 
 #include "engine.h"
@@ -45,7 +49,7 @@ constexpr int kQmcBits = 32;
 
 struct QmcParams {
   SimParams P;                 // plan constants (records, trackers, scenario 0)
-  const uint32_t *dirs;        // [D][32] direction numbers V_1..V_32
+  const uint32_t *dirs;        // [32][D] direction numbers V_1..V_32, bit-major
   const uint32_t *shift;       // [R][D] digital shifts
   const int *br_mid, *br_left, *br_right;  // Brownian bridge, construction order
   const float *br_wl, *br_wr, *br_sd;
@@ -58,32 +62,81 @@ struct QmcParams {
 
 namespace dev {
 
-__device__ __forceinline__ uint32_t sobol_coord(const uint32_t *V, uint32_t g) {
-  uint32_t x = 0;
-  for (int b = 0; g; ++b, g >>= 1)
-    if (g & 1u) x ^= __ldg(V + b);
-  return x;
+// One warp's Sobol coordinates, 32 dimensions at a time, in dimension order.  The 32 lanes
+// hold 32 consecutive points of one replicate, so the Gray code's bits >= 5 are the same
+// for the whole warp and only bits 0..4 differ.  A fill gives lane l dimension d0 + l: it
+// XORs the shift and the direction numbers of the shared high bits (coalesced loads from
+// the bit-major table), then walks the 32 low Gray values in Gray-code order (one XOR
+// each) and stores them in row l of the warp's 32 x 32 table; a draw is then one shared
+// load at (row d - d0, column of the lane's low Gray bits).  Columns are XOR-swizzled by
+// the row, so both the fill's stores and the draws' loads touch 32 distinct banks.
+__device__ __noinline__ void sobol_fill(uint32_t *tab, const uint32_t *V, const uint32_t *shift, uint32_t ghi,
+                                        unsigned int D, unsigned int d0, int lane) {
+  __syncwarp();  // every lane has read the previous block of dimensions
+  const unsigned int d = d0 + (unsigned int)lane;
+  if (d < D) {
+    uint32_t h = __ldg(shift + d);
+    for (uint32_t m = ghi; m; m &= m - 1u) h ^= __ldg(V + (size_t)(__ffs((int)m) - 1) * D + d);
+    uint32_t v[5];
+#pragma unroll
+    for (int b = 0; b < 5; ++b) v[b] = __ldg(V + (size_t)b * D + d);
+    uint32_t *row = tab + lane * 32;
+    row[lane] = h;  // Gray value 0
+#pragma unroll
+    for (int j = 1; j < 32; ++j) {
+      h ^= v[__ffs(j) - 1];
+      row[(j ^ (j >> 1)) ^ lane] = h;
+    }
+  }
+  __syncwarp();
 }
 
-// 64-bit draw of a shifted Sobol coordinate: the centre of its 2^-32 cell, so that
-// u01_bits, u01c_bits and inv_normal_bits of it are the coordinate's uniform.
-__device__ __forceinline__ unsigned long long qmc_draw(const QmcParams &Q, const uint32_t *shift, uint32_t g,
-                                                       unsigned int d) {
-  const uint32_t x = sobol_coord(Q.dirs + (size_t)d * kQmcBits, g) ^ __ldg(shift + d);
-  return ((unsigned long long)x << 32) | 0x80000000ull;
-}
+struct SobolWarp {
+  uint32_t *tab;          // [32][32] in shared memory
+  const uint32_t *V;      // bit-major direction numbers [32][D]
+  const uint32_t *shift;  // this replicate's shifts [D]
+  uint32_t ghi, glo;      // Gray code: the warp's bits >= 5, the lane's bits 0..4
+  unsigned int D, d0, pos;
+  int lane;
+
+  __device__ __forceinline__ void fill() { sobol_fill(tab, V, shift, ghi, D, d0, lane); }
+  // the next dimension's shifted coordinate as a 64-bit draw: the centre of its 2^-32 cell,
+  // so that u01_bits, u01c_bits and inv_normal_bits of it are the coordinate's uniform
+  __device__ __forceinline__ unsigned long long next() {
+    if (pos == 32u) {
+      d0 += 32u;
+      pos = 0u;
+      fill();
+    }
+    const uint32_t x = tab[pos * 32u + (glo ^ pos)];
+    ++pos;
+    return ((unsigned long long)x << 32) | 0x80000000ull;
+  }
+};
 
 template <int NF, bool PD>
 __global__ void __launch_bounds__(kSimBlock) qmc_kernel(const __grid_constant__ QmcParams Q) {
   const SimParams &P = Q.P;
   const unsigned long long i = blockIdx.x * (unsigned long long)kSimBlock + threadIdx.x;
-  if (i >= P.path_end) return;
+  // the grid covers path_end exactly (a multiple of 2048 paths) and n_pts is a multiple of
+  // 2048, so every warp is full and its 32 points are consecutive within one replicate
+  __shared__ uint32_t sobol_tab[kSimBlock / 32][32 * 32];
   const unsigned long long rep = i / Q.n_pts, pt = i % Q.n_pts;
   const uint32_t g = (uint32_t)(pt ^ (pt >> 1));  // Gray code
   const int n = P.n_steps;
   constexpr int NC = 1 + NF;  // at most: the spot's motion and one per NV factor
   const int NG = Q.NG;
-  const uint32_t *shift = Q.shift + rep * Q.D;
+  SobolWarp sob;
+  sob.tab = sobol_tab[threadIdx.x >> 5];
+  sob.V = Q.dirs;
+  sob.shift = Q.shift + rep * Q.D;
+  sob.ghi = g & ~31u;
+  sob.glo = g & 31u;
+  sob.D = Q.D;
+  sob.d0 = 0u;
+  sob.pos = 0u;
+  sob.lane = (int)(threadIdx.x & 31u);
+  sob.fill();
   float W[NC][kQmcMaxSteps + 1];
 #pragma unroll
   for (int c = 0; c < NC; ++c) W[c][0] = 0.0f;
@@ -93,8 +146,7 @@ __global__ void __launch_bounds__(kSimBlock) qmc_kernel(const __grid_constant__ 
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
       if (c >= NG) break;
-      const unsigned int d = (unsigned int)b * NG + c;
-      const float z = inv_normal_bits(qmc_draw(Q, shift, g, d));
+      const float z = inv_normal_bits(sob.next());  // dimension b * NG + c
       W[c][m] = fmaf(wl, W[c][l], fmaf(wr, W[c][r], sd * z));
     }
   }
@@ -104,10 +156,8 @@ __global__ void __launch_bounds__(kSimBlock) qmc_kernel(const __grid_constant__ 
   ts.init(P, PD);
   const float dt = C.dt;
   unsigned int caphits = 0, fallbacks = 0;
-  const unsigned int ubase = (unsigned int)n * NG;
-  for (int k = 0; k < n; ++k) {
+  for (int k = 0; k < n; ++k) {  // step k's uniforms are dimensions n NG + k NU + u
     const float G = W[0][k + 1] - W[0][k];
-    unsigned int du = ubase + (unsigned int)k * Q.NU;  // this step's uniforms
     if (NF == 0) {
       X += fmaf(C.gbm_vol, G, C.gbm_drift);
     } else {
@@ -122,8 +172,8 @@ __global__ void __launch_bounds__(kSimBlock) qmc_kernel(const __grid_constant__ 
           const float rt = sqrt_approx(fmaf(fc.w0, v[f], fc.w1)) + fc.w2 * Z;
           vn[f] = fmaf(fc.w0 * rt, rt, fc.w1);
         } else {  // SchemeNCI: N ~ Poisson(C0 v) by inversion, then the table at the second uniform
-          const unsigned long long xp = qmc_draw(Q, shift, g, du), x2 = qmc_draw(Q, shift, g, du + 1);
-          du += 2;
+          const unsigned long long xp = sob.next();
+          const unsigned long long x2 = sob.next();
           const float lam = fc.w0 * v[f];
           const float Wp = lam > kPoissonAsymMin ? inv_normal_bits(xp) : 0.0f;
           const int N = poisson_core(lam, u01_bits(xp), Wp, xp, P.loop_cap, caphits);
@@ -146,7 +196,8 @@ __global__ void __launch_bounds__(kSimBlock) qmc_kernel(const __grid_constant__ 
       v[1] = vn[1];
     }
     if (Q.jump) {  // Merton, per step: count by sequential inversion, then one normal for the sum
-      const unsigned long long xc = qmc_draw(Q, shift, g, du), xz = qmc_draw(Q, shift, g, du + 1);
+      const unsigned long long xc = sob.next();
+      const unsigned long long xz = sob.next();
       const int nj = poisson_small_u(C.jump_mean, C.jump_exp_neg_mean, u01_bits(xc), P.loop_cap, caphits);
       float J = C.jump_comp;
       if (nj > 0) {
@@ -226,27 +277,45 @@ bool primitive(uint32_t p, int s) {
   return true;
 }
 
-// direction numbers of D dimensions, [D][32]
+// The first `count` primitive polynomials (with their degrees) in order of degree, then of
+// coefficients, up to degree 20.  The search does not depend on the seed, so it runs once
+// per process and grows as larger dimension counts are asked for; callers get a copy.
+std::vector<std::pair<uint32_t, int>> primitive_polys(size_t count) {
+  static std::mutex mu;
+  static std::vector<std::pair<uint32_t, int>> polys;
+  static int next_s = 1;
+  static uint32_t next_low = 0;
+  std::lock_guard<std::mutex> lock(mu);
+  while (polys.size() < count && next_s <= 20) {
+    const uint32_t p = (1u << next_s) | (next_low << 1) | 1u;  // x^s + a_1 x^(s-1) + ... + 1
+    if (primitive(p, next_s)) polys.push_back({p, next_s});
+    if (++next_low == 1u << (next_s - 1)) {
+      next_low = 0;
+      ++next_s;
+    }
+  }
+  return std::vector<std::pair<uint32_t, int>>(polys.begin(), polys.begin() + std::min(count, polys.size()));
+}
+
+// direction numbers of D dimensions, [D][32]; dimension d >= 1 takes the d-th primitive
+// polynomial, and the seed's splitmix stream draws its initial m_1..m_s in that order
 std::vector<uint32_t> sobol_directions(unsigned int D, uint64_t seed) {
   std::vector<uint32_t> V((size_t)D * kQmcBits, 0u);
   for (int k = 1; k <= kQmcBits; ++k) V[k - 1] = 1u << (kQmcBits - k);  // van der Corput
-  unsigned int d = 1;
+  const std::vector<std::pair<uint32_t, int>> polys = primitive_polys(D - 1);
   uint64_t rs = seed ^ 0xD1B54A32D192ED03ull;
-  for (int s = 1; d < D && s <= 20; ++s) {
-    for (uint32_t low = 0; d < D && low < (1u << (s - 1)); ++low) {
-      const uint32_t p = (1u << s) | (low << 1) | 1u;  // x^s + a_1 x^(s-1) + ... + 1
-      if (!primitive(p, s)) continue;
-      std::vector<uint64_t> m(kQmcBits + 1, 0);
-      for (int k = 1; k <= s && k <= kQmcBits; ++k) m[k] = ((splitmix(rs) % (1ull << (k - 1))) << 1) | 1ull;
-      for (int k = s + 1; k <= kQmcBits; ++k) {
-        uint64_t v = m[k - s] ^ (m[k - s] << s);
-        for (int j = 1; j < s; ++j)
-          if (p >> (s - j) & 1u) v ^= m[k - j] << j;  // coefficient a_j of x^(s-j)
-        m[k] = v;
-      }
-      for (int k = 1; k <= kQmcBits; ++k) V[(size_t)d * kQmcBits + k - 1] = (uint32_t)(m[k] << (kQmcBits - k));
-      ++d;
+  uint64_t m[kQmcBits + 1];
+  for (unsigned int d = 1; d < D && d - 1 < polys.size(); ++d) {
+    const uint32_t p = polys[d - 1].first;
+    const int s = polys[d - 1].second;
+    for (int k = 1; k <= s && k <= kQmcBits; ++k) m[k] = ((splitmix(rs) % (1ull << (k - 1))) << 1) | 1ull;
+    for (int k = s + 1; k <= kQmcBits; ++k) {
+      uint64_t v = m[k - s] ^ (m[k - s] << s);
+      for (int j = 1; j < s; ++j)
+        if (p >> (s - j) & 1u) v ^= m[k - j] << j;  // coefficient a_j of x^(s-j)
+      m[k] = v;
     }
+    for (int k = 1; k <= kQmcBits; ++k) V[(size_t)d * kQmcBits + k - 1] = (uint32_t)(m[k] << (kQmcBits - k));
   }
   return V;
 }
@@ -345,8 +414,11 @@ extern "C" myql_status myql_qmc_price(myql_ctx *ctx_, const myql_mc_job *job, ui
     const std::vector<uint32_t> V = sobol_directions(D, seed);
     if ((size_t)D * kQmcBits > V.size() || V[(size_t)(D - 1) * kQmcBits] == 0u)
       return set_error(MYQL_ERR_TOO_LARGE, "too many quasi-Monte Carlo dimensions");
-    e = S.dirs.ensure(V.size() * 4);
-    if (e == cudaSuccess) e = cudaMemcpy(S.dirs.p, V.data(), V.size() * 4, cudaMemcpyHostToDevice);
+    std::vector<uint32_t> Vt(V.size());  // bit-major on the device: a warp's dimensions are contiguous
+    for (unsigned int d = 0; d < D; ++d)
+      for (int k = 0; k < kQmcBits; ++k) Vt[(size_t)k * D + d] = V[(size_t)d * kQmcBits + k];
+    e = S.dirs.ensure(Vt.size() * 4);
+    if (e == cudaSuccess) e = cudaMemcpy(S.dirs.p, Vt.data(), Vt.size() * 4, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_status(e, "Sobol directions");
     S.dirs_D = D;
     S.dirs_seed = seed;

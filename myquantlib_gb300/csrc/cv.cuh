@@ -56,6 +56,7 @@ constexpr uint32_t kImgBytes = kImgW1x64 + 16384;
 constexpr uint32_t kImgFwdBytes = kImgW1x64;  // W1, W2, W3
 // FP32 vectors beside the images: b1, b2, b3, w4 (128 each), b4
 constexpr int kVecB1 = 0, kVecB2 = 128, kVecB3 = 256, kVecW4 = 384, kVecB4 = 512, kVecCount = 516;
+constexpr int kHalfBias = 384;  // 0.5 x (b1, b2, b3), kept in shared memory by the MLP kernels
 
 constexpr unsigned long long kCvWaitNs = 2000000000ull;  // bounded waits: 2 s
 

@@ -37,8 +37,10 @@ __device__ __forceinline__ uint8_t *align1024(uint8_t *p) {
   return p + (((a + 1023u) & ~1023u) - a);
 }
 
-// z (TMEM, columns [32 c0, 32 c1) of this thread's row) + bias -> SiLU -> BF16 IMG128 row of H
-__device__ __forceinline__ void epi_hidden(uint32_t tm_row, const float *bias, uint8_t *H, uint32_t row, int c0 = 0,
+// z (TMEM, columns [32 c0, 32 c1) of this thread's row) + bias -> SiLU -> BF16 IMG128 row of H.
+// hb = 0.5 x the layer's bias (16-byte aligned, shared): the bias, the halving and SiLU's
+// final fma run on column pairs (packed FP32), with the values of the scalar form.
+__device__ __forceinline__ void epi_hidden(uint32_t tm_row, const float *hb, uint8_t *H, uint32_t row, int c0 = 0,
                                            int c1 = 4) {
 #pragma unroll 1
   for (int c = c0; c < c1; c += 2) {
@@ -46,12 +48,15 @@ __device__ __forceinline__ void epi_hidden(uint32_t tm_row, const float *bias, u
     tc::tmem_ld64(tm_row + (uint32_t)(c * 32), v);  // columns [32 c, 32 c + 64): one round trip
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
+      const float4 b0 = *reinterpret_cast<const float4 *>(hb + c * 32 + q * 8);
+      const float4 b1 = *reinterpret_cast<const float4 *>(hb + c * 32 + q * 8 + 4);
+      const float2 bp[4] = {make_float2(b0.x, b0.y), make_float2(b0.z, b0.w), make_float2(b1.x, b1.y),
+                            make_float2(b1.z, b1.w)};
       uint32_t w[4];
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
-        const int k = c * 32 + q * 8 + 2 * e;
-        __nv_bfloat162 p = __floats2bfloat162_rn(tc::silu(v[q * 8 + 2 * e] + bias[k]),
-                                                 tc::silu(v[q * 8 + 2 * e + 1] + bias[k + 1]));
+        const float2 s = tc::silu2_half_bias(make_float2(v[q * 8 + 2 * e], v[q * 8 + 2 * e + 1]), bp[e]);
+        __nv_bfloat162 p = __floats2bfloat162_rn(s.x, s.y);
         w[e] = *reinterpret_cast<uint32_t *>(&p);
       }
       *reinterpret_cast<uint4 *>(H + tc::img128_offset(row, (uint32_t)(c * 32 + q * 8), 128)) =
@@ -60,20 +65,27 @@ __device__ __forceinline__ void epi_hidden(uint32_t tm_row, const float *bias, u
   }
 }
 
-// output layer over columns [32 c0, 32 c1): sum_k silu(z3_k + b3_k) w4_k (+ b4 when c0 == 0)
-__device__ __forceinline__ float epi_out(uint32_t tm_row, const float *vec, int c0 = 0, int c1 = 4) {
-  float g = c0 == 0 ? vec[kVecB4] : 0.0f;
+// output layer over columns [32 c0, 32 c1): sum_k silu(z3_k + b3_k) w4_k (+ b4 when c0 == 0),
+// from hb3 = 0.5 b3, on column pairs with four partial sums (a fixed order: deterministic)
+__device__ __forceinline__ float epi_out(uint32_t tm_row, const float *vec, const float *hb3, int c0 = 0,
+                                         int c1 = 4) {
+  float2 ga = make_float2(c0 == 0 ? vec[kVecB4] : 0.0f, 0.0f), gb = make_float2(0.0f, 0.0f);
 #pragma unroll 1
   for (int c = c0; c < c1; c += 2) {
     float v[64];
     tc::tmem_ld64(tm_row + (uint32_t)(c * 32), v);
 #pragma unroll
-    for (int i = 0; i < 64; ++i) {
+    for (int i = 0; i < 64; i += 4) {
       const int k = c * 32 + i;
-      g = fmaf(tc::silu(v[i] + vec[kVecB3 + k]), vec[kVecW4 + k], g);
+      const float4 h4 = *reinterpret_cast<const float4 *>(hb3 + k);
+      const float4 w4 = *reinterpret_cast<const float4 *>(vec + kVecW4 + k);
+      const float2 s0 = tc::silu2_half_bias(make_float2(v[i], v[i + 1]), make_float2(h4.x, h4.y));
+      const float2 s1 = tc::silu2_half_bias(make_float2(v[i + 2], v[i + 3]), make_float2(h4.z, h4.w));
+      ga = tc::ffma2(s0, make_float2(w4.x, w4.y), ga);
+      gb = tc::ffma2(s1, make_float2(w4.z, w4.w), gb);
     }
   }
-  return g;
+  return (ga.x + ga.y) + (gb.x + gb.y);
 }
 
 // D[128 x N] (TMEM) = A (IMG128, [128][K]) * B (IMG128, [N][K])^T, K = 128, both K-major
@@ -160,7 +172,8 @@ __global__ void __launch_bounds__(kFwdThreads, 1) cv_mlp_kernel(const __grid_con
   extern __shared__ uint8_t dyn[];
   __shared__ __align__(8) uint64_t bar_w, bar_x[kFwdGroups], bar_mma[kFwdGroups];
   __shared__ uint32_t tmem_base;
-  __shared__ float vec[kVecCount];
+  __shared__ __align__(16) float vec[kVecCount];
+  __shared__ __align__(16) float hbias[kHalfBias];
   uint8_t *sm = align1024(dyn);
   uint8_t *sW1 = sm + kImgW1, *sW2 = sm + kImgW2, *sW3 = sm + kImgW3;
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -171,6 +184,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1) cv_mlp_kernel(const __grid_con
   uint8_t *sH = sm + kFwdH + (uint32_t)grp * 32768u;
   uint8_t *sX = sm + kFwdX + (uint32_t)grp * kCvTileBytes;
   for (int i = tid; i < kVecCount; i += kFwdThreads) vec[i] = P.vec[i];
+  for (int i = tid; i < kHalfBias; i += kFwdThreads) hbias[i] = 0.5f * P.vec[kVecB1 + i];
   if (tid == 0) {
     tc::mbar_init(&bar_w, 1);
     for (int g = 0; g < kFwdGroups; ++g) {
@@ -256,21 +270,21 @@ __global__ void __launch_bounds__(kFwdThreads, 1) cv_mlp_kernel(const __grid_con
       tc::bulk_g2s(sX, P.feat + tile_of(t + 1) * kCvTileBytes, kCvTileBytes, &bar_x[grp]);
       x_pending = true;
     }
-    epi_hidden(tm_row, vec + kVecB1, sH, row);
+    epi_hidden(tm_row, hbias, sH, row);
     before_mma();
     if (elected) {
       mma_k128(tm, sH, sW2, 128, 0u);
       tc::mma_commit(&bar_mma[grp]);
     }
     if (!mma_wait()) { err = true; break; }
-    epi_hidden(tm_row, vec + kVecB2, sH, row);
+    epi_hidden(tm_row, hbias + 128, sH, row);
     before_mma();
     if (elected) {
       mma_k128(tm, sH, sW3, 128, 0u);
       tc::mma_commit(&bar_mma[grp]);
     }
     if (!mma_wait()) { err = true; break; }
-    const float g = epi_out(tm_row, vec);
+    const float g = epi_out(tm_row, vec, hbias + 256);
     const unsigned long long r = tile * 128ull + row;
     if (P.g_out) P.g_out[r] = g;
     if (P.tile_major) {
@@ -329,7 +343,8 @@ __global__ void __launch_bounds__(kBwdThreads, 1) cv_bwd_kernel(const __grid_con
   extern __shared__ uint8_t dyn[];
   __shared__ __align__(8) uint64_t bar_w, bar_mma;
   __shared__ uint32_t tmem_base;
-  __shared__ float vec[kVecCount];
+  __shared__ __align__(16) float vec[kVecCount];
+  __shared__ __align__(16) float hbias[kHalfBias];
   uint8_t *sm = align1024(dyn);
   // [W1x64 16K][W2 32K][W3 32K][X64 16K][H1 32K][H2 32K][D 32K]
   uint8_t *sW1 = sm, *sW2 = sm + 16384, *sW3 = sm + 49152, *sX = sm + 81920, *sH1 = sm + 98304;
@@ -338,6 +353,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1) cv_bwd_kernel(const __grid_con
   const uint32_t row = (uint32_t)(tid & 127);
   const int half = warp >> 2, c0 = 2 * half, c1 = 2 * half + 2;
   for (int i = tid; i < kVecCount; i += kBwdThreads) vec[i] = P.vec[i];
+  for (int i = tid; i < kHalfBias; i += kBwdThreads) hbias[i] = 0.5f * P.vec[kVecB1 + i];
   // padding chunks of the x image stay zero
   for (int i = tid; i < 128 * 6; i += kBwdThreads)
     *reinterpret_cast<uint4 *>(sX + tc::img128_offset((uint32_t)(i / 6), (uint32_t)((2 + i % 6) * 8), 128)) =
@@ -398,7 +414,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1) cv_bwd_kernel(const __grid_con
       tc::mma_commit(&bar_mma);
     }
     if (!block_wait(&bar_mma, phase)) { err = true; break; }
-    epi_hidden(T0 + lane_off, vec + kVecB1, sH1, row, c0, c1);
+    epi_hidden(T0 + lane_off, hbias, sH1, row, c0, c1);
     block_sync_async();
     // F2: z2 = h1 W2^T
     if (tid == 0) {
@@ -406,7 +422,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1) cv_bwd_kernel(const __grid_con
       tc::mma_commit(&bar_mma);
     }
     if (!block_wait(&bar_mma, phase)) { err = true; break; }
-    epi_hidden(T0 + lane_off, vec + kVecB2, sH2, row, c0, c1);
+    epi_hidden(T0 + lane_off, hbias + 128, sH2, row, c0, c1);
     block_sync_async();
     // F3: z3 = h2 W3^T
     if (tid == 0) {

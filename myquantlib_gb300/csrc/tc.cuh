@@ -167,6 +167,17 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
                :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(b)) : "memory");
 }
 
+// Packed FP32 pairs (sm_100 and later): one instruction for two lanes of IEEE fma / mul,
+// each lane rounded exactly as the scalar instruction would.
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
+  float2 r;
+  asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "mov.b64 rc, {%6, %7};\n\tfma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return r;
+}
+
 // SiLU through tanh.approx: x * sigmoid(x) = 0.5 x (1 + tanh(x / 2)).
 __device__ __forceinline__ float tanh_fast(float x) {
   float y;
@@ -176,6 +187,12 @@ __device__ __forceinline__ float tanh_fast(float x) {
 __device__ __forceinline__ float silu(float z) {
   const float h = 0.5f * z;
   return fmaf(h, tanh_fast(h), h);
+}
+// silu(z + b) of two columns from hb = 0.5 b: h = fma(z, 0.5, hb) is exactly 0.5 (z + b)
+// (scaling by 2^-1 commutes with rounding), so each lane equals silu(z + b) bit for bit
+__device__ __forceinline__ float2 silu2_half_bias(float2 z, float2 hb) {
+  const float2 h = ffma2(z, make_float2(0.5f, 0.5f), hb);
+  return ffma2(h, make_float2(tanh_fast(h.x), tanh_fast(h.y)), h);
 }
 // d silu / dz = s (1 + z (1 - s)), s = sigmoid(z) = 0.5 (1 + tanh(z / 2))
 __device__ __forceinline__ float silu_grad(float z) {

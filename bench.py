@@ -714,7 +714,9 @@ def time_to_se(eng, m, kind: str, target: float, probe_paths: int = 1 << 22, top
     other pilot paths).  In the timed region each arm prices the path count its probe gives
     for the target and, while its estimated relative error is still above the target, prices
     more paths on fresh seeds and pools them (at most `top_ups` times).  The control
-    variate's timed region includes its own pilot simulation and training."""
+    variate's timed region includes its own pilot simulation and training.  A third arm runs
+    the same control variate on randomized QMC paths (myql_cv_qmc_price, 16 digital shifts),
+    sized in whole 2048-point blocks per replicate from its own untimed probe."""
     import torch
     job, steps = cv_jobs(m, kind, probe_paths)
     torch.cuda.synchronize()
@@ -754,6 +756,28 @@ def time_to_se(eng, m, kind: str, target: float, probe_paths: int = 1 << 22, top
         cv_last["price_ms"] += r.total_ms
         return r.price, r.price_std_err, n
 
+    # the same network on randomized QMC paths: sized like qmc_time_to_se from its own probe
+    R, quantum = 16, 16 * 2048
+    qprobe = eng.cv_qmc_price(cv_jobs(m, kind, 1 << 20, seed=44)[0], cfg, R)
+    n_cvq = max(-(-int((1 << 20) * (qprobe.price_std_err / (0.9 * target * qprobe.price)) ** 2) // quantum) * quantum,
+                quantum)
+    cvq_last = {"sim_ms": 0.0, "mlp_ms": 0.0, "price_ms": 0.0}
+
+    def run_cvq():
+        parts, n, runs = [], n_cvq, 0
+        while True:
+            r = eng.cv_qmc_price(cv_jobs(m, kind, n, seed=3000 + runs)[0], cfg, R)
+            cvq_last["vr"] = r.variance_ratio
+            cvq_last["sim_ms"] += r.simulate_ms
+            cvq_last["mlp_ms"] += r.mlp_ms
+            cvq_last["price_ms"] += r.total_ms
+            parts.append((r.price, r.price_std_err, n))
+            runs += 1
+            mean, err, tot = _pool_qmc(parts)
+            if err <= target * mean or runs > top_ups:
+                return mean, err, tot, runs
+            n = max(-(-int(tot * ((err / (target * mean)) ** 2 - 1.0)) // quantum) * quantum, quantum)
+
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     p_mean, p_err, p_n, p_rounds = run_arm(n_plain, plain_fn, 1000)
@@ -762,6 +786,10 @@ def time_to_se(eng, m, kind: str, target: float, probe_paths: int = 1 << 22, top
     tr = eng.cv_train(cv_jobs(m, kind, 1 << 16, seed=45)[0], cfg)
     c_mean, c_err, c_n, c_rounds = run_arm(n_cv, cv_fn, 2000)
     t_cv = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    trq = eng.cv_train(cv_jobs(m, kind, 1 << 16, seed=46)[0], cfg)
+    q_mean, q_err, q_n, q_runs = run_cvq()
+    t_cvq = time.perf_counter() - t0
     t_plain_path = t_plain / p_n
     t_cv_path = (t_cv - tr.total_ms / 1e3) / c_n
     return {"instrument": "Double Bates arithmetic Asian call" if kind == "asian" else "Heston European call",
@@ -779,7 +807,16 @@ def time_to_se(eng, m, kind: str, target: float, probe_paths: int = 1 << 22, top
                                "price_simulate": cv_last["sim_ms"] / 1e3, "price_mlp": cv_last["mlp_ms"] / 1e3,
                                "price_other": (cv_last["price_ms"] - cv_last["sim_ms"] - cv_last["mlp_ms"]) / 1e3,
                                "host": t_cv - (tr.total_ms + cv_last["price_ms"]) / 1e3},
-            "price_cv": c_mean, "price_plain": p_mean}
+            "price_cv": c_mean, "price_plain": p_mean,
+            # the control variate on randomized QMC paths (R = 16 digital shifts), pilot and
+            # training inside its timed region as above
+            "cv_qmc": {"s": t_cvq, "speedup": t_plain / t_cvq, "points": q_n, "runs": q_runs,
+                       "rel_se": q_err / q_mean, "price": q_mean, "replicate_variance_ratio": cvq_last.get("vr"),
+                       "breakdown_s": {"pilot_and_training": trq.total_ms / 1e3,
+                                       "price_simulate": cvq_last["sim_ms"] / 1e3,
+                                       "price_mlp": cvq_last["mlp_ms"] / 1e3,
+                                       "price_other": (cvq_last["price_ms"] - cvq_last["sim_ms"]
+                                                       - cvq_last["mlp_ms"]) / 1e3}}}
 
 
 def cv_report(eng, m) -> dict:

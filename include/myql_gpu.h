@@ -452,6 +452,15 @@ myql_status myql_cv_train(myql_ctx *ctx, const myql_mc_job *job, const myql_cv_c
 /* Prices job (its own seed, paths and streams) with the context's network. */
 myql_status myql_cv_price(myql_ctx *ctx, const myql_mc_job *job, const myql_cv_config *cfg,
                           myql_cv_result *res);
+/* Prices job with the context's network on randomized quasi-Monte Carlo paths
+ * (the Sobol points, bridges and digital shifts of myql_qmc_price, same
+ * restrictions: SchemeNV / SchemeNCI factors, no jumps or Merton jumps, at most
+ * 512 steps, num_paths a multiple of 2048 * n_replicates, n_replicates >= 2).
+ * price / plain_price: the means of the n_replicates replicate estimates of the
+ * control-variate and the plain estimator; the standard errors and
+ * variance_ratio come from their spreads. */
+myql_status myql_cv_qmc_price(myql_ctx *ctx, const myql_mc_job *job, const myql_cv_config *cfg,
+                              uint32_t n_replicates, myql_cv_result *res);
 /* Network parameters (MYQL_CV_PARAMS floats): fresh initialisation, read, write. */
 myql_status myql_cv_init(myql_ctx *ctx, uint64_t seed);
 myql_status myql_cv_get_params(myql_ctx *ctx, float *params, size_t n);

@@ -156,6 +156,8 @@ _SIGS = {
     "myql_probe_peak": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
     "myql_cv_train": (C.c_int, [C.c_void_p, C.POINTER(McJobC), C.POINTER(CvConfigC), C.POINTER(CvResultC)]),
     "myql_cv_price": (C.c_int, [C.c_void_p, C.POINTER(McJobC), C.POINTER(CvConfigC), C.POINTER(CvResultC)]),
+    "myql_cv_qmc_price": (C.c_int, [C.c_void_p, C.POINTER(McJobC), C.POINTER(CvConfigC), C.c_uint32,
+                                    C.POINTER(CvResultC)]),
     "myql_cv_init": (C.c_int, [C.c_void_p, C.c_uint64]),
     "myql_cv_get_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_size_t]),
     "myql_cv_set_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_size_t]),

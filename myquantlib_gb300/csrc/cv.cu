@@ -14,6 +14,7 @@
 
 #include "cv.cuh"
 #include "engine.h"
+#include "qmc.cuh"
 
 namespace myql {
 static_assert(kPCount == MYQL_CV_PARAMS, "parameter blob size");
@@ -726,6 +727,118 @@ myql_status myql_cv_price(myql_ctx *ctx_, const myql_mc_job *job, const myql_cv_
   res->plain_std_err = std::sqrt(vy / n);
   res->price = mz;
   res->price_std_err = std::sqrt(vz / n);
+  res->variance_ratio = vz > 0.0 ? vy / vz : 0.0;
+  res->paths = M;
+  res->simulate_ms = sim_ms;
+  res->mlp_ms = mlp_ms;
+  res->total_ms = ms_since(t0);
+  res->kernel_launches = ctx->launches;
+  return MYQL_OK;
+}
+
+// The trained control variate on randomized QMC paths (myql_qmc_price's Sobol points,
+// bridges and digital shifts): R replicates of the control-variate estimator, each the mean
+// of Y - C over its points, with the standard error from their spread.  Y - C stays unbiased
+// under the digitally shifted points, whose every point is uniform on the unit cube.
+myql_status myql_cv_qmc_price(myql_ctx *ctx_, const myql_mc_job *job, const myql_cv_config *cfg,
+                              uint32_t n_replicates, myql_cv_result *res) {
+  CtxBase *ctx = reinterpret_cast<CtxBase *>(ctx_);
+  if (!ctx || !job || !res) return set_error(MYQL_ERR_INVALID_ARG, "null argument");
+  myql_status s = check_job(*job);
+  if (s == MYQL_OK) s = check_cfg(cfg);
+  if (s != MYQL_OK) return s;
+  CvState &S = state(ctx);
+  if (!S.init) return set_error(MYQL_ERR_INVALID_ARG, "train the control variate first (myql_cv_train)");
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return cuda_status(e, "cudaSetDevice");
+  const auto t0 = std::chrono::steady_clock::now();
+  ctx->launches = 0;
+  Plan pl;
+  CvSimParams C;
+  int klass = 0;
+  s = cv_plan(ctx, *job, *cfg, pl, C, klass);
+  if (s != MYQL_OK) return s;
+  const uint64_t M = job->config.num_paths, R = n_replicates;
+  QmcCvParams Q;
+  std::memset(&Q, 0, sizeof Q);
+  s = qmc_prepare(ctx, *job, pl, R, Q.Q);
+  if (s != MYQL_OK) return s;
+  Q.Q.P.status = C.sim.status;
+  Q.pay = C.pay;
+  Q.df = C.df;
+  Q.hedge_every = C.hedge_every;
+  Q.n_hedge = C.n_hedge;
+  Q.fc = C.fc;
+  const uint32_t nh = (uint32_t)C.n_hedge;
+  const uint64_t n_pts = M / R;
+  // chunk: whole 2048-point blocks with at most ~4 GiB of features
+  uint64_t chunk = (4ull << 30) / ((uint64_t)nh * (kCvTileBytes / 128 + 4));
+  chunk = std::min<uint64_t>(std::max<uint64_t>(chunk / 2048 * 2048, 2048), M);
+  const uint64_t pbs = chunk / 128;
+  e = S.feat.ensure(pbs * nh * kCvTileBytes);
+  if (e == cudaSuccess) e = S.dM.ensure(pbs * nh * 128 * 4);
+  if (e == cudaSuccess) e = S.Y.ensure(chunk * 4);
+  if (e == cudaSuccess) e = S.cv.ensure(chunk * 4);
+  if (e == cudaSuccess) e = S.sums.ensure(R * 4 * sizeof(double));
+  if (e == cudaSuccess) e = cudaMemsetAsync(S.sums.p, 0, R * 4 * sizeof(double), ctx->stream);
+  if (e != cudaSuccess) return cuda_status(e, "control-variate QMC buffers");
+  Q.feat = (uint8_t *)S.feat.p;
+  Q.dM = (float *)S.dM.p;
+  Q.Y = (float *)S.Y.p;
+  ctx->phase_reset();
+  cudaEvent_t ev[3];
+  for (int i = 0; i < 3; ++i) ev[i] = ctx->phase_event();
+  float sim_ms = 0.0f, mlp_ms = 0.0f;
+  for (uint64_t b = 0; b < M; b += chunk) {
+    const uint64_t n = std::min(chunk, M - b);  // a multiple of 2048, as are b and n_pts
+    Q.path_begin = b;
+    e = cudaEventRecord(ev[0], ctx->stream);
+    if (e == cudaSuccess) e = launch_qmc_cv(Q, n, pl.nf, ctx->stream);
+    if (e != cudaSuccess) return cuda_status(e, "qmc_cv launch");
+    ctx->launches++;
+    e = cudaEventRecord(ev[1], ctx->stream);
+    if (e != cudaSuccess) return cuda_status(e, "event");
+    s = forward(ctx, S, (const uint8_t *)S.feat.p, (const float *)S.dM.p, n, nh, (float *)S.cv.p, nullptr);
+    if (s != MYQL_OK) return s;
+    e = cudaEventRecord(ev[2], ctx->stream);
+    // the chunk's share of each replicate, into that replicate's sums
+    for (uint64_t r = b / n_pts; e == cudaSuccess && r * n_pts < b + n; ++r) {
+      const uint64_t lo = std::max(b, r * n_pts), hi = std::min(b + n, (r + 1) * n_pts);
+      e = launch_cv_reduce((const float *)S.Y.p + (lo - b), (const float *)S.cv.p + (lo - b), hi - lo,
+                           (double *)S.sums.p + 4 * r, (double *)S.fpart.p, ctx->stream);
+      ctx->launches += 2;
+    }
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[2]);
+    float a = 0.0f, c = 0.0f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&a, ev[0], ev[1]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&c, ev[1], ev[2]);
+    if (e != cudaSuccess) return cuda_status(e, "control-variate QMC chunk");
+    sim_ms += a;
+    mlp_ms += c;
+  }
+  std::vector<double> sums(R * 4);
+  e = cudaMemcpyAsync(sums.data(), S.sums.p, sums.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e != cudaSuccess) return cuda_status(e, "control-variate QMC sums");
+  s = wait_status(ctx);
+  if (s != MYQL_OK) return s;
+  // replicate estimates of the plain and the control-variate estimator
+  double sy = 0.0, syy = 0.0, sz = 0.0, szz = 0.0;
+  for (uint64_t r = 0; r < R; ++r) {
+    const double y = sums[4 * r] / (double)n_pts, z = sums[4 * r + 2] / (double)n_pts;
+    sy += y;
+    syy += y * y;
+    sz += z;
+    szz += z * z;
+  }
+  const double Rd = (double)R;
+  const double my = sy / Rd, mz = sz / Rd;
+  const double vy = std::max(syy / Rd - my * my, 0.0) * Rd / (Rd - 1.0);
+  const double vz = std::max(szz / Rd - mz * mz, 0.0) * Rd / (Rd - 1.0);
+  std::memset(res, 0, sizeof *res);
+  res->plain_price = my;
+  res->plain_std_err = std::sqrt(vy / Rd);
+  res->price = mz;
+  res->price_std_err = std::sqrt(vz / Rd);
   res->variance_ratio = vz > 0.0 ? vy / vz : 0.0;
   res->paths = M;
   res->simulate_ms = sim_ms;

@@ -39,179 +39,51 @@
 #include <utility>
 #include <vector>
 
-#include "engine.h"
-#include "simulate.cuh"
+#include "qmc.cuh"
 
 namespace myql {
-
-constexpr int kQmcMaxSteps = 512;
-constexpr int kQmcBits = 32;
-
-struct QmcParams {
-  SimParams P;                 // plan constants (records, trackers, scenario 0)
-  const uint32_t *dirs;        // [32][D] direction numbers V_1..V_32, bit-major
-  const uint32_t *shift;       // [R][D] digital shifts
-  const int *br_mid, *br_left, *br_right;  // Brownian bridge, construction order
-  const float *br_wl, *br_wr, *br_sd;
-  unsigned long long n_pts;    // points per replicate
-  unsigned int D;              // dimensions per path = steps * (NG + NU)
-  int sch[2];                  // scheme of each factor: SCH_NV or SCH_NCI
-  int jump;                    // 0 none, 1 Merton (per step)
-  int NG, NU;                  // Gaussian motions (spot + NV factors), uniforms per step
-};
-
 namespace dev {
-
-// One warp's Sobol coordinates, 32 dimensions at a time, in dimension order.  The 32 lanes
-// hold 32 consecutive points of one replicate, so the Gray code's bits >= 5 are the same
-// for the whole warp and only bits 0..4 differ.  A fill gives lane l dimension d0 + l: it
-// XORs the shift and the direction numbers of the shared high bits (coalesced loads from
-// the bit-major table), then walks the 32 low Gray values in Gray-code order (one XOR
-// each) and stores them in row l of the warp's 32 x 32 table; a draw is then one shared
-// load at (row d - d0, column of the lane's low Gray bits).  Columns are XOR-swizzled by
-// the row, so both the fill's stores and the draws' loads touch 32 distinct banks.
-__device__ __noinline__ void sobol_fill(uint32_t *tab, const uint32_t *V, const uint32_t *shift, uint32_t ghi,
-                                        unsigned int D, unsigned int d0, int lane) {
-  __syncwarp();  // every lane has read the previous block of dimensions
-  const unsigned int d = d0 + (unsigned int)lane;
-  if (d < D) {
-    uint32_t h = __ldg(shift + d);
-    for (uint32_t m = ghi; m; m &= m - 1u) h ^= __ldg(V + (size_t)(__ffs((int)m) - 1) * D + d);
-    uint32_t v[5];
-#pragma unroll
-    for (int b = 0; b < 5; ++b) v[b] = __ldg(V + (size_t)b * D + d);
-    uint32_t *row = tab + lane * 32;
-    row[lane] = h;  // Gray value 0
-#pragma unroll
-    for (int j = 1; j < 32; ++j) {
-      h ^= v[__ffs(j) - 1];
-      row[(j ^ (j >> 1)) ^ lane] = h;
-    }
-  }
-  __syncwarp();
-}
-
-struct SobolWarp {
-  uint32_t *tab;          // [32][32] in shared memory
-  const uint32_t *V;      // bit-major direction numbers [32][D]
-  const uint32_t *shift;  // this replicate's shifts [D]
-  uint32_t ghi, glo;      // Gray code: the warp's bits >= 5, the lane's bits 0..4
-  unsigned int D, d0, pos;
-  int lane;
-
-  __device__ __forceinline__ void fill() { sobol_fill(tab, V, shift, ghi, D, d0, lane); }
-  // the next dimension's shifted coordinate as a 64-bit draw: the centre of its 2^-32 cell,
-  // so that u01_bits, u01c_bits and inv_normal_bits of it are the coordinate's uniform
-  __device__ __forceinline__ unsigned long long next() {
-    if (pos == 32u) {
-      d0 += 32u;
-      pos = 0u;
-      fill();
-    }
-    const uint32_t x = tab[pos * 32u + (glo ^ pos)];
-    ++pos;
-    return ((unsigned long long)x << 32) | 0x80000000ull;
-  }
-};
 
 template <int NF, bool PD>
 __global__ void __launch_bounds__(kSimBlock) qmc_kernel(const __grid_constant__ QmcParams Q) {
-  const SimParams &P = Q.P;
-  const unsigned long long i = blockIdx.x * (unsigned long long)kSimBlock + threadIdx.x;
   // the grid covers path_end exactly (a multiple of 2048 paths) and n_pts is a multiple of
   // 2048, so every warp is full and its 32 points are consecutive within one replicate
   __shared__ uint32_t sobol_tab[kSimBlock / 32][32 * 32];
-  const unsigned long long rep = i / Q.n_pts, pt = i % Q.n_pts;
-  const uint32_t g = (uint32_t)(pt ^ (pt >> 1));  // Gray code
-  const int n = P.n_steps;
-  constexpr int NC = 1 + NF;  // at most: the spot's motion and one per NV factor
-  const int NG = Q.NG;
-  SobolWarp sob;
-  sob.tab = sobol_tab[threadIdx.x >> 5];
-  sob.V = Q.dirs;
-  sob.shift = Q.shift + rep * Q.D;
-  sob.ghi = g & ~31u;
-  sob.glo = g & 31u;
-  sob.D = Q.D;
-  sob.d0 = 0u;
-  sob.pos = 0u;
-  sob.lane = (int)(threadIdx.x & 31u);
-  sob.fill();
-  float W[NC][kQmcMaxSteps + 1];
-#pragma unroll
-  for (int c = 0; c < NC; ++c) W[c][0] = 0.0f;
-  for (int b = 0; b < n; ++b) {
-    const int m = Q.br_mid[b], l = Q.br_left[b], r = Q.br_right[b];
-    const float wl = Q.br_wl[b], wr = Q.br_wr[b], sd = Q.br_sd[b];
-#pragma unroll
-    for (int c = 0; c < NC; ++c) {
-      if (c >= NG) break;
-      const float z = inv_normal_bits(sob.next());  // dimension b * NG + c
-      W[c][m] = fmaf(wl, W[c][l], fmaf(wr, W[c][r], sd * z));
-    }
-  }
-  const ScenarioConst &C = P.sc[0];
-  float X = 0.0f, v[2] = {C.f[0].v0, C.f[1].v0};
-  TrackerState ts;
-  ts.init(P, PD);
-  const float dt = C.dt;
+  const SimParams &P = Q.P;
+  const unsigned long long i = blockIdx.x * (unsigned long long)kSimBlock + threadIdx.x;
+  SobolWarp sob = sobol_warp(Q, sobol_tab[threadIdx.x >> 5], i);
   unsigned int caphits = 0, fallbacks = 0;
-  for (int k = 0; k < n; ++k) {  // step k's uniforms are dimensions n NG + k NU + u
-    const float G = W[0][k + 1] - W[0][k];
-    if (NF == 0) {
-      X += fmaf(C.gbm_vol, G, C.gbm_drift);
-    } else {
-      float vn[2] = {0.0f, 0.0f};
-      int gi = 1;  // next Gaussian motion (NV factors, in factor order)
-#pragma unroll
-      for (int f = 0; f < NF; ++f) {
-        const FactorConst &fc = C.f[f];
-        if (Q.sch[f] == SCH_NV) {
-          const float Z = gi == 1 ? W[1][k + 1] - W[1][k] : W[NC - 1][k + 1] - W[NC - 1][k];
-          ++gi;
-          const float rt = sqrt_approx(fmaf(fc.w0, v[f], fc.w1)) + fc.w2 * Z;
-          vn[f] = fmaf(fc.w0 * rt, rt, fc.w1);
-        } else {  // SchemeNCI: N ~ Poisson(C0 v) by inversion, then the table at the second uniform
-          const unsigned long long xp = sob.next();
-          const unsigned long long x2 = sob.next();
-          const float lam = fc.w0 * v[f];
-          const float Wp = lam > kPoissonAsymMin ? inv_normal_bits(xp) : 0.0f;
-          const int N = poisson_core(lam, u01_bits(xp), Wp, xp, P.loop_cap, caphits);
-          vn[f] = nci_quantile(P.nci[f], N, x2, P.nci_u999, fallbacks) * fc.w2;
-        }
-      }
-      if (NF == 1) {
-        const FactorConst &f0 = C.f[0];
-        const float root = sqrt_approx(f0.C3 * (v[0] + vn[0]));
-        const float drift = fmaf(f0.C2, vn[0], fmaf(f0.C1, v[0], f0.C0));
-        X += fmaf(root, G, drift);
-      } else {
-        const FactorConst &f0 = C.f[0];
-        const FactorConst &f1 = C.f[1];
-        const float root = sqrt_approx(fmaf(f0.C3, v[0] + vn[0], f1.C3 * (v[1] + vn[1])));
-        const float drift = fmaf(f1.C2, vn[1], fmaf(f1.C1, v[1], fmaf(f0.C2, vn[0], fmaf(f0.C1, v[0], f0.C0 + f1.C0))));
-        X += fmaf(root, G, drift);
-      }
-      v[0] = vn[0];
-      v[1] = vn[1];
-    }
-    if (Q.jump) {  // Merton, per step: count by sequential inversion, then one normal for the sum
-      const unsigned long long xc = sob.next();
-      const unsigned long long xz = sob.next();
-      const int nj = poisson_small_u(C.jump_mean, C.jump_exp_neg_mean, u01_bits(xc), P.loop_cap, caphits);
-      float J = C.jump_comp;
-      if (nj > 0) {
-        const float fn = (float)nj;
-        J += fn * P.merton_mu + sqrtf(fn) * P.merton_delta * inv_normal_bits(xz);
-      }
-      X += J;
-    }
-    if (PD) ts.step(P, k, dt, X);
-  }
   float out[kMaxFields];
-  ts.finish(P, C, X, PD, out);
+  NoHook h;
+  qmc_path<NF, PD>(Q, sob, out, caphits, fallbacks, h);
   const int F = P.n_fields;
   for (int f = 0; f < F; ++f) P.records[(size_t)f * P.rec_stride + i] = out[f];
+  if (caphits) atomicAdd(P.status, caphits);
+  if (fallbacks) atomicAdd(P.status + 1, fallbacks);
+}
+
+// The control variate's Sobol paths: as cv_sim_kernel (features at the hedge times, centred
+// martingale increments, the discounted payoff in place), one thread per point.
+template <int NF>
+__global__ void __launch_bounds__(kSimBlock) qmc_cv_kernel(const __grid_constant__ QmcCvParams C) {
+  __shared__ uint32_t sobol_tab[kSimBlock / 32][32 * 32];
+  const SimParams &P = C.Q.P;
+  const unsigned long long li = blockIdx.x * (unsigned long long)kSimBlock + threadIdx.x;  // launch-local
+  SobolWarp sob = sobol_warp(C.Q, sobol_tab[threadIdx.x >> 5], C.path_begin + li);
+  const unsigned long long pb = li >> 7;
+  CvHook h;
+  h.P = &C.fc;
+  h.lane = (uint32_t)(li & 127u);
+  h.tile0 = C.feat + pb * (unsigned long long)C.n_hedge * kCvTileBytes;
+  h.dm0 = C.dM + pb * (unsigned long long)C.n_hedge * 128ull + h.lane;
+  h.he = C.hedge_every;
+  h.n = P.n_steps;
+  h.dt = P.sc[0].dt;
+  unsigned int caphits = 0, fallbacks = 0;
+  float r[kMaxFields];
+  qmc_path<NF, true>(C.Q, sob, r, caphits, fallbacks, h);
+  const PathView v = record_view(C.pay, r);
+  C.Y[li] = (float)C.df * scenario_tri(C.pay, v, (float)C.pay.strikes[0], false).v;
   if (caphits) atomicAdd(P.status, caphits);
   if (fallbacks) atomicAdd(P.status + 1, fallbacks);
 }
@@ -227,6 +99,19 @@ static cudaError_t launch_qmc(const QmcParams &Q, int nf, bool pd, cudaStream_t 
     case 3: dev::qmc_kernel<1, true><<<grid, kSimBlock, 0, st>>>(Q); break;
     case 4: dev::qmc_kernel<2, false><<<grid, kSimBlock, 0, st>>>(Q); break;
     case 5: dev::qmc_kernel<2, true><<<grid, kSimBlock, 0, st>>>(Q); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+// n_paths: a multiple of 2048 (whole warps of one replicate, whole 128-path tiles)
+cudaError_t launch_qmc_cv(const QmcCvParams &P, unsigned long long n_paths, int nf, cudaStream_t st) {
+  if (n_paths == 0 || n_paths % 2048 != 0 || P.path_begin % 2048 != 0) return cudaErrorInvalidValue;
+  const unsigned int grid = (unsigned int)(n_paths / kSimBlock);
+  switch (nf) {
+    case 0: dev::qmc_cv_kernel<0><<<grid, kSimBlock, 0, st>>>(P); break;
+    case 1: dev::qmc_cv_kernel<1><<<grid, kSimBlock, 0, st>>>(P); break;
+    case 2: dev::qmc_cv_kernel<2><<<grid, kSimBlock, 0, st>>>(P); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
@@ -368,47 +253,33 @@ extern "C" myql_status myql_qmc_directions(uint32_t D, uint64_t seed, uint32_t *
   return MYQL_OK;
 }
 
-extern "C" myql_status myql_qmc_price(myql_ctx *ctx_, const myql_mc_job *job, uint32_t n_replicates,
-                                      double *out, myql_mc_stats *stats) {
-  CtxBase *ctx = reinterpret_cast<CtxBase *>(ctx_);
-  if (!ctx || !job || !out) return set_error(MYQL_ERR_INVALID_ARG, "null argument");
-  myql_status s = validate_job(*job);
-  if (s != MYQL_OK) return s;
-  const int nf = job->model.num_factors;
+myql_status qmc_prepare(CtxBase *ctx, const myql_mc_job &job, const Plan &pl, uint64_t R, QmcParams &Q) {
+  const int nf = job.model.num_factors;
   int n_nv = 0, n_nci = 0;
   for (int f = 0; f < nf; ++f) {
-    if (job->config.scheme[f] == MYQL_SCHEME_NV) ++n_nv;
-    else if (job->config.scheme[f] == MYQL_SCHEME_NCI) ++n_nci;
+    if (job.config.scheme[f] == MYQL_SCHEME_NV) ++n_nv;
+    else if (job.config.scheme[f] == MYQL_SCHEME_NCI) ++n_nci;
     else
       return set_error(MYQL_ERR_UNSUPPORTED,
                        "quasi-Monte Carlo steps the CIR factors with SchemeNV or SchemeNCI (SchemeExact's "
                        "rejection loop has no fixed number of draws)");
   }
-  if (job->model.jump == MYQL_JUMP_KOU)
+  if (job.model.jump == MYQL_JUMP_KOU)
     return set_error(MYQL_ERR_UNSUPPORTED,
                      "quasi-Monte Carlo supports Merton jumps or none (Kou draws one exponential per jump)");
-  if (job->config.greek_mode != MYQL_GREEKS_NONE)
-    return set_error(MYQL_ERR_UNSUPPORTED, "quasi-Monte Carlo prices only (GreekMode None)");
-  const uint64_t M = job->config.num_paths, R = n_replicates;
+  const uint64_t M = job.config.num_paths;
   if (R < 2 || M % (R * 2048ull) != 0)
     return set_error(MYQL_ERR_INVALID_ARG, "quasi-Monte Carlo needs >= 2 replicates and num_paths a multiple "
                                            "of 2048 x replicates");
   if (M / R > (1ull << 32)) return set_error(MYQL_ERR_TOO_LARGE, "at most 2^32 points per replicate");
-  Plan pl;
-  s = make_plan(*job, pl, true);
-  if (s != MYQL_OK) return s;
   if (pl.steps > kQmcMaxSteps) return set_error(MYQL_ERR_UNSUPPORTED, "quasi-Monte Carlo takes at most 512 steps");
-  cudaError_t e = cudaSetDevice(ctx->device);
-  if (e != cudaSuccess) return cuda_status(e, "cudaSetDevice");
   if (!ctx->qmc) ctx->qmc.reset(new QmcState);
   QmcState &S = *static_cast<QmcState *>(ctx->qmc.get());
-  const int NG = 1 + n_nv, NU = 2 * n_nci + (job->model.jump == MYQL_JUMP_MERTON ? 2 : 0);
+  const int NG = 1 + n_nv, NU = 2 * n_nci + (job.model.jump == MYQL_JUMP_MERTON ? 2 : 0);
   const unsigned int D = (unsigned int)pl.steps * (unsigned int)(NG + NU);
-  const uint64_t seed = job->config.seed;
+  const uint64_t seed = job.config.seed;
   cudaStream_t st = ctx->stream;
-  ctx->launches = 0;
-  ctx->phase_reset();
-  e = cudaEventRecord(ctx->ev0, st);
+  cudaError_t e = cudaSuccess;
   // tables: direction numbers, shifts, bridge
   if (S.dirs_D != D || S.dirs_seed != seed) {
     const std::vector<uint32_t> V = sobol_directions(D, seed);
@@ -445,26 +316,8 @@ extern "C" myql_status myql_qmc_price(myql_ctx *ctx_, const myql_mc_job *job, ui
     if (e != cudaSuccess) return cuda_status(e, "Brownian bridge");
     S.bridge_n = n;
   }
-  // buffers: records (one scenario), strikes, tile partials
-  const int nk = (int)job->instrument.n_strikes;
-  const uint64_t tiles = M / 2048;
-  e = ctx->records.ensure(M * pl.n_fields * 4);
-  if (e == cudaSuccess) e = ctx->strikes.ensure(nk * sizeof(double));
-  if (e == cudaSuccess) e = ctx->partials.ensure(tiles * (uint64_t)nk * 2 * kQ * sizeof(double));
-  if (e == cudaSuccess) e = ctx->status.ensure(16);
-  if (e == cudaSuccess) e = cudaMemsetAsync(ctx->status.p, 0, 16, st);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(ctx->strikes.p, job->instrument.strikes, nk * sizeof(double), cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return cuda_status(e, "quasi-Monte Carlo buffers");
-  QmcParams Q;
   std::memset(&Q, 0, sizeof Q);
   Q.P = pl.sim;
-  Q.P.records = (float *)ctx->records.p;
-  Q.P.status = (unsigned int *)ctx->status.p;
-  Q.P.rec_stride = M;
-  Q.P.path_begin = 0;
-  Q.P.path_end = M;
-  Q.P.rec_offset = 0;
   Q.dirs = (const uint32_t *)S.dirs.p;
   Q.shift = (const uint32_t *)S.shift.p;
   const uint8_t *bb = (const uint8_t *)S.bridge.p;
@@ -478,15 +331,58 @@ extern "C" myql_status myql_qmc_price(myql_ctx *ctx_, const myql_mc_job *job, ui
   Q.D = D;
   Q.NG = NG;
   Q.NU = NU;
-  Q.jump = job->model.jump == MYQL_JUMP_MERTON ? 1 : 0;
+  Q.jump = job.model.jump == MYQL_JUMP_MERTON ? 1 : 0;
   for (int f = 0; f < nf; ++f) {
-    Q.sch[f] = job->config.scheme[f] == MYQL_SCHEME_NCI ? dev::SCH_NCI : dev::SCH_NV;
+    Q.sch[f] = job.config.scheme[f] == MYQL_SCHEME_NCI ? dev::SCH_NCI : dev::SCH_NV;
     if (Q.sch[f] == dev::SCH_NCI) {
-      s = ensure_nci(ctx, job->model.heston[f], (double)pl.sim.sc[0].dt, Q.P.nci[f]);
+      myql_status s = ensure_nci(ctx, job.model.heston[f], (double)pl.sim.sc[0].dt, Q.P.nci[f]);
       if (s != MYQL_OK) return s;
     }
   }
   Q.P.loop_cap = ctx->loop_cap;
+  return MYQL_OK;
+}
+
+extern "C" myql_status myql_qmc_price(myql_ctx *ctx_, const myql_mc_job *job, uint32_t n_replicates,
+                                      double *out, myql_mc_stats *stats) {
+  CtxBase *ctx = reinterpret_cast<CtxBase *>(ctx_);
+  if (!ctx || !job || !out) return set_error(MYQL_ERR_INVALID_ARG, "null argument");
+  myql_status s = validate_job(*job);
+  if (s != MYQL_OK) return s;
+  if (job->config.greek_mode != MYQL_GREEKS_NONE)
+    return set_error(MYQL_ERR_UNSUPPORTED, "quasi-Monte Carlo prices only (GreekMode None)");
+  const uint64_t M = job->config.num_paths, R = n_replicates;
+  Plan pl;
+  s = make_plan(*job, pl, true);
+  if (s != MYQL_OK) return s;
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return cuda_status(e, "cudaSetDevice");
+  cudaStream_t st = ctx->stream;
+  ctx->launches = 0;
+  ctx->phase_reset();
+  e = cudaEventRecord(ctx->ev0, st);
+  if (e != cudaSuccess) return cuda_status(e, "event");
+  QmcParams Q;
+  s = qmc_prepare(ctx, *job, pl, R, Q);
+  if (s != MYQL_OK) return s;
+  const int n = pl.steps, nf = job->model.num_factors;
+  // buffers: records (one scenario), strikes, tile partials
+  const int nk = (int)job->instrument.n_strikes;
+  const uint64_t tiles = M / 2048;
+  e = ctx->records.ensure(M * pl.n_fields * 4);
+  if (e == cudaSuccess) e = ctx->strikes.ensure(nk * sizeof(double));
+  if (e == cudaSuccess) e = ctx->partials.ensure(tiles * (uint64_t)nk * 2 * kQ * sizeof(double));
+  if (e == cudaSuccess) e = ctx->status.ensure(16);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ctx->status.p, 0, 16, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(ctx->strikes.p, job->instrument.strikes, nk * sizeof(double), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_status(e, "quasi-Monte Carlo buffers");
+  Q.P.records = (float *)ctx->records.p;
+  Q.P.status = (unsigned int *)ctx->status.p;
+  Q.P.rec_stride = M;
+  Q.P.path_begin = 0;
+  Q.P.path_end = M;
+  Q.P.rec_offset = 0;
   cudaEvent_t sa = ctx->phase_event(), sb = ctx->phase_event();
   cudaEventRecord(sa, st);
   e = launch_qmc(Q, nf, pl.path_dep, st);

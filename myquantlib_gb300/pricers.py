@@ -517,6 +517,14 @@ class Engine:
         _abi.check(self.lib.myql_cv_price(self.handle, C.byref(job.c), C.byref(cfg), C.byref(res)))
         return res
 
+    def cv_qmc_price(self, job: "_Job", cfg: "_abi.CvConfigC", n_replicates: int = 16) -> "_abi.CvResultC":
+        """The trained control variate on randomized QMC paths (myql_cv_qmc_price): replicate
+        means of the control-variate and plain estimators, standard errors from their spread."""
+        res = _abi.CvResultC()
+        _abi.check(self.lib.myql_cv_qmc_price(self.handle, C.byref(job.c), C.byref(cfg), n_replicates,
+                                              C.byref(res)))
+        return res
+
     def mlmc_price(self, job: "_Job", mlmc_cfg: "_abi.MlmcConfigC") -> "_abi.MlmcResultC":
         """MultiLevelMonteCarloPricer::calculate (MultiLevelMonteCarloPricer.hpp:46-238)."""
         res = _abi.MlmcResultC()

@@ -169,3 +169,52 @@ def test_cv_training_and_pricing_are_reproducible(engine):
     pj = double_bates_asian_job(1 << 17, seed=9)
     a, b = engine.cv_price(pj, cfg), engine.cv_price(pj, cfg)
     assert a.price == b.price and a.price_std_err == b.price_std_err
+
+
+# ---------------------------------------------------------------- the control variate on QMC paths
+def test_cv_qmc_simulates_the_qmc_pricer_paths(engine):
+    """myql_cv_qmc_price steps the points of myql_qmc_price: its plain replicate means give the
+    QMC price of the same job (FP32 payoffs summed in another order: equal to ~1e-6)."""
+    cfg = cv_cfg(8, iterations=20, pilot=1 << 14)
+    engine.cv_train(double_bates_asian_job(1 << 14, seed=5), cfg)
+    job = double_bates_asian_job(1 << 17, seed=21)
+    q, _ = engine.qmc_price(double_bates_asian_job(1 << 17, seed=21), 16)
+    res = engine.cv_qmc_price(job, cfg, 16)
+    assert abs(res.plain_price - q[0, 0]) < 1e-5 * q[0, 0], (res.plain_price, q[0, 0])
+    assert abs(res.plain_std_err - q[1, 0]) < 1e-3 * q[1, 0], (res.plain_std_err, q[1, 0])
+
+
+def test_cv_qmc_heston_european_unbiased_and_gains(engine):
+    cfg = cv_cfg(5)
+    engine.cv_train(heston_call_job(1 << 16), cfg)
+    res = engine.cv_qmc_price(heston_call_job(1 << 18), cfg, 16)
+    assert abs(res.price - FOURIER_C1) < 4 * res.price_std_err + 1e-3, (res.price, res.price_std_err)
+    # against the control variate on pseudo-random paths of the same count
+    ps = engine.cv_price(heston_call_job(1 << 18), cfg)
+    assert res.price_std_err < 0.5 * ps.price_std_err, (res.price_std_err, ps.price_std_err)
+
+
+def test_cv_qmc_double_bates_asian_against_plain_engine(engine):
+    cfg = cv_cfg(8)
+    engine.cv_train(double_bates_asian_job(1 << 16, seed=5), cfg)
+    res = engine.cv_qmc_price(double_bates_asian_job(1 << 18), cfg, 16)
+    raw, _ = engine.price(double_bates_asian_job(1 << 20, seed=77))
+    ref, ref_se = raw[0, 0], raw[1, 0]
+    assert abs(res.price - ref) < 4 * np.hypot(res.price_std_err, ref_se), (res.price, ref, res.price_std_err, ref_se)
+    ps = engine.cv_price(double_bates_asian_job(1 << 18), cfg)
+    assert res.price_std_err < ps.price_std_err, (res.price_std_err, ps.price_std_err)
+
+
+def test_cv_qmc_refuses_what_qmc_refuses(engine):
+    from myquantlib_gb300 import _abi
+    cfg = cv_cfg(5, iterations=5, pilot=1 << 12)
+    engine.cv_train(heston_call_job(1 << 12), cfg)
+    with pytest.raises(_abi.MyqlError) as e:
+        engine.cv_qmc_price(heston_call_job(3 * 2048), cfg, 2)
+    assert e.value.status == _abi.ERR_INVALID_ARG
+    exact = m.make_job(m.HestonModel(m.HestonParams(1.5, 0.04, 0.3, -0.7, 0.04)), m.HestonStepper(m.SchemeExact),
+                       m.EuropeanOption(100.0, 1.0), m.GreekMode.NONE,
+                       m.MonteCarloConfig(num_paths=1 << 15, time_steps=16, seed=1), 100.0, 0.02, 0.0)
+    with pytest.raises(_abi.MyqlError) as e:
+        engine.cv_qmc_price(exact, cfg, 16)
+    assert e.value.status == _abi.ERR_UNSUPPORTED

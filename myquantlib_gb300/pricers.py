@@ -834,14 +834,17 @@ class NeuralCVPricer:
     `train(S0, r, q, instrument)` fits the network on pilot paths of the model;
     `calculate(S0, r, q, instrument)` prices with it and also reports the plain
     Monte Carlo estimator of the same paths.  Scalar European / Asian instruments.
+    With qmc_replicates = R > 0 the pricing paths are randomized QMC (R digital
+    shifts, myql_cv_qmc_price) and the standard errors come from the replicates.
     """
 
     def __init__(self, model, stepper: ASVJStepper | None = None, cfg: MonteCarloConfig | None = None,
-                 cv: ControlVariateConfig | None = None, engine: Engine | None = None):
+                 cv: ControlVariateConfig | None = None, engine: Engine | None = None, qmc_replicates: int = 0):
         self.model, self.stepper = model, stepper
         self.cfg = cfg or MonteCarloConfig()
         self.cv = cv or ControlVariateConfig()
         self.engine = engine
+        self.qmc_replicates = qmc_replicates
         self.train_result = None
 
     def _job(self, S0, r, q, instr):
@@ -856,6 +859,10 @@ class NeuralCVPricer:
         eng = self.engine or default_engine()
         if self.train_result is None:
             self.train(S0, r, q, instr)
-        res = eng.cv_price(self._job(S0, r, q, instr), self.cv.c())
+        job = self._job(S0, r, q, instr)
+        if self.qmc_replicates:
+            res = eng.cv_qmc_price(job, self.cv.c(), self.qmc_replicates)
+        else:
+            res = eng.cv_price(job, self.cv.c())
         return ControlVariateResult(res.price, res.price_std_err, res.plain_price, res.plain_std_err,
                                     res.variance_ratio, self.train_result, res)

@@ -485,8 +485,83 @@ __device__ __forceinline__ void evolve_merged(const float (&v)[NS], float (&vn)[
   }
 }
 
-// MERGE: the v0-bumped scenarios' variance paths merge into the base's (every
+// One time step of every simulated scenario of one path: the loop body of the lockstep
+// kernels.  MERGE: the v0-bumped scenarios' variance paths merge into the base's (every
 // factor on NCI, and P.lock_merge: the host found their NCI constants equal).
+template <int NF, int S1, int S2, int NSIM, bool MERGE>
+__device__ __forceinline__ void lockstep_step(const SimParams &P, Xo &rng, float (&X)[NSIM], float (&va)[NSIM],
+                                              float (&vb)[NSIM], unsigned int &caphits,
+                                              unsigned int &fallbacks) {
+  const float G = inv_normal_bits(draw(rng));
+  FactorDraws<S1> da;
+  FactorDraws<S2> db;
+  factor_draws<S1>(da, rng, P, 0);
+  if (NF == 2) factor_draws<S2>(db, rng, P, 1);
+  float van[NSIM], vbn[NSIM];
+  if constexpr (MERGE) {
+    evolve_merged<NSIM>(va, van, da, P, 0, caphits, fallbacks);
+    if constexpr (NF == 2) evolve_merged<NSIM>(vb, vbn, db, P, 1, caphits, fallbacks);
+  } else {
+    evolve_lockstep<S1, NSIM>(va, van, da, P, 0, caphits, fallbacks);
+    if (NF == 2) evolve_lockstep<S2, NSIM>(vb, vbn, db, P, 1, caphits, fallbacks);
+  }
+#pragma unroll
+  for (int j = 0; j < NSIM; ++j) {
+    const ScenarioConst &C = P.sc[lockstep_sc(j)];
+    if (NF == 1) {
+      const FactorConst &f = C.f[0];
+      const float vn = van[j];
+      const float root = sqrt_approx(f.C3 * (va[j] + vn));
+      const float drift = fmaf(f.C2, vn, fmaf(f.C1, va[j], f.C0));
+      X[j] += fmaf(root, G, drift);
+      va[j] = vn;
+    } else {
+      const FactorConst &f0 = C.f[0];
+      const FactorConst &f1 = C.f[1];
+      const float root = sqrt_approx(fmaf(f0.C3, va[j] + van[j], f1.C3 * (vb[j] + vbn[j])));
+      const float drift = fmaf(f1.C2, vbn[j], fmaf(f1.C1, vb[j], fmaf(f0.C2, van[j],
+                               fmaf(f0.C1, va[j], f0.C0 + f1.C0))));
+      X[j] += fmaf(root, G, drift);
+      va[j] = van[j];
+      vb[j] = vbn[j];
+    }
+  }
+}
+
+template <int NSIM>
+__device__ __forceinline__ void lockstep_start(const SimParams &P, float (&X)[NSIM], float (&va)[NSIM],
+                                               float (&vb)[NSIM]) {
+#pragma unroll
+  for (int j = 0; j < NSIM; ++j) {
+    X[j] = 0.0f;
+    va[j] = P.sc[lockstep_sc(j)].f[0].v0;
+    vb[j] = P.sc[lockstep_sc(j)].f[1].v0;
+  }
+}
+
+// Path end: one jump over each scenario's (bumped) maturity, drawn from the state after
+// the last step (the base scenario's draws advance the stream), then the records,
+// the two rho scenarios derived from the base.
+template <int NSIM>
+__device__ __forceinline__ void lockstep_finish(const SimParams &P, Xo &rng, float (&X)[NSIM], size_t col,
+                                                unsigned int &caphits) {
+  if (P.jump_kind) {
+    Xo after = rng;
+#pragma unroll
+    for (int j = 0; j < NSIM; ++j) {
+      Xo r = after;
+      X[j] += jump_draw(P, P.sc[lockstep_sc(j)], r, caphits);
+      if (j == 0) rng = r;
+    }
+  }
+  const size_t F = (size_t)P.n_fields;
+#pragma unroll
+  for (int j = 0; j < NSIM; ++j)
+    P.records[(size_t)lockstep_sc(j) * F * P.rec_stride + col] = X[j];
+  P.records[(size_t)SC_RUP * F * P.rec_stride + col] = X[0] + P.sc[SC_RUP].x_shift;
+  P.records[(size_t)SC_RDN * F * P.rec_stride + col] = X[0] + P.sc[SC_RDN].x_shift;
+}
+
 template <int NF, int S1, int S2, int NSIM, bool MERGE = false>
 __global__ void __launch_bounds__(kSimBlock) simulate_lockstep_kernel(
     const __grid_constant__ SimParams P) {
@@ -503,67 +578,10 @@ __global__ void __launch_bounds__(kSimBlock) simulate_lockstep_kernel(
   unsigned int caphits = 0, fallbacks = 0;
   const int n = P.n_steps;
   for (unsigned long long i = P.path_begin + s; i < P.path_end; i += S) {
-    const size_t col = (size_t)(i - P.rec_offset);
     float X[NSIM], va[NSIM], vb[NSIM];
-#pragma unroll
-    for (int j = 0; j < NSIM; ++j) {
-      X[j] = 0.0f;
-      va[j] = P.sc[lockstep_sc(j)].f[0].v0;
-      vb[j] = P.sc[lockstep_sc(j)].f[1].v0;
-    }
-    for (int k = 0; k < n; ++k) {
-      const float G = inv_normal_bits(draw(rng));
-      FactorDraws<S1> da;
-      FactorDraws<S2> db;
-      factor_draws<S1>(da, rng, P, 0);
-      if (NF == 2) factor_draws<S2>(db, rng, P, 1);
-      float van[NSIM], vbn[NSIM];
-      if constexpr (MERGE) {
-        evolve_merged<NSIM>(va, van, da, P, 0, caphits, fallbacks);
-        if constexpr (NF == 2) evolve_merged<NSIM>(vb, vbn, db, P, 1, caphits, fallbacks);
-      } else {
-        evolve_lockstep<S1, NSIM>(va, van, da, P, 0, caphits, fallbacks);
-        if (NF == 2) evolve_lockstep<S2, NSIM>(vb, vbn, db, P, 1, caphits, fallbacks);
-      }
-#pragma unroll
-      for (int j = 0; j < NSIM; ++j) {
-        const ScenarioConst &C = P.sc[lockstep_sc(j)];
-        if (NF == 1) {
-          const FactorConst &f = C.f[0];
-          const float vn = van[j];
-          const float root = sqrt_approx(f.C3 * (va[j] + vn));
-          const float drift = fmaf(f.C2, vn, fmaf(f.C1, va[j], f.C0));
-          X[j] += fmaf(root, G, drift);
-          va[j] = vn;
-        } else {
-          const FactorConst &f0 = C.f[0];
-          const FactorConst &f1 = C.f[1];
-          const float root = sqrt_approx(fmaf(f0.C3, va[j] + van[j], f1.C3 * (vb[j] + vbn[j])));
-          const float drift = fmaf(f1.C2, vbn[j], fmaf(f1.C1, vb[j], fmaf(f0.C2, van[j],
-                                   fmaf(f0.C1, va[j], f0.C0 + f1.C0))));
-          X[j] += fmaf(root, G, drift);
-          va[j] = van[j];
-          vb[j] = vbn[j];
-        }
-      }
-    }
-    // One jump over each scenario's (bumped) maturity, drawn from the state after
-    // the last step; the base scenario's draws advance the stream.
-    if (P.jump_kind) {
-      Xo after = rng;
-#pragma unroll
-      for (int j = 0; j < NSIM; ++j) {
-        Xo r = after;
-        X[j] += jump_draw(P, P.sc[lockstep_sc(j)], r, caphits);
-        if (j == 0) rng = r;
-      }
-    }
-    const size_t F = (size_t)P.n_fields;
-#pragma unroll
-    for (int j = 0; j < NSIM; ++j)
-      P.records[(size_t)lockstep_sc(j) * F * P.rec_stride + col] = X[j];
-    P.records[(size_t)SC_RUP * F * P.rec_stride + col] = X[0] + P.sc[SC_RUP].x_shift;
-    P.records[(size_t)SC_RDN * F * P.rec_stride + col] = X[0] + P.sc[SC_RDN].x_shift;
+    lockstep_start<NSIM>(P, X, va, vb);
+    for (int k = 0; k < n; ++k) lockstep_step<NF, S1, S2, NSIM, MERGE>(P, rng, X, va, vb, caphits, fallbacks);
+    lockstep_finish<NSIM>(P, rng, X, (size_t)(i - P.rec_offset), caphits);
   }
   P.states[s] = rng.a;
   P.states[(size_t)S + s] = rng.b;

@@ -17,11 +17,14 @@
 namespace myql {
 namespace dev {
 
-template <int SPEC, class FLD>
+// PRE: field 0 is staged as e^X already (the strip path of SPEC = 1, which computes it once
+// per path instead of once per strike lane); the product with S0 stays here, where the
+// compiler may fuse it with the strike's subtraction exactly as for the unstaged record
+template <int SPEC, bool PRE = false, class FLD>
 __device__ __forceinline__ PathView make_view(const PayoffParams &P, FLD fld, int sc) {
   PathView v;
   const float X = fld(sc, 0);
-  v.S = P.S0 * __expf(X);
+  v.S = P.S0 * (PRE ? X : __expf(X));
   v.Y = 0.0f;
   v.hit[0] = v.hit[1] = v.hit[2] = -1.0f;
   if (SPEC == 1) return v;
@@ -47,11 +50,11 @@ __device__ __forceinline__ PathView make_view(const PayoffParams &P, FLD fld, in
 
 // Per-path estimators of every quantity for strike K (MonteCarloPricer.hpp:261-276
 // and :316-409), from the increments of each scenario.
-template <int SPEC, class FLD>
+template <int SPEC, bool PRE = false, class FLD>
 __device__ __forceinline__ void path_quantities(const PayoffParams &P, FLD fld, float K,
                                                 float (&q)[kQ]) {
   const bool bumps = P.mode != 0;
-  const Tri b = scenario_tri<SPEC>(P, make_view<SPEC>(P, fld, 0), K, bumps);
+  const Tri b = scenario_tri<SPEC>(P, make_view<SPEC, PRE>(P, fld, 0), K, bumps);
   q[0] = b.v;
   if (!bumps) return;
   q[1] = (b.dp - b.dm) * P.inv_2h;
@@ -59,30 +62,32 @@ __device__ __forceinline__ void path_quantities(const PayoffParams &P, FLD fld, 
   if (P.mode == 1) return;
   const int nv = P.n_factors >= 2 ? 2 : 1;
   for (int fct = 0; fct < nv; ++fct) {
-    const Tri u = scenario_tri<SPEC>(P, make_view<SPEC>(P, fld, fct == 0 ? SC_VUP0 : SC_VUP1), K, true);
-    const Tri d = scenario_tri<SPEC>(P, make_view<SPEC>(P, fld, fct == 0 ? SC_VDN0 : SC_VDN1), K, true);
+    const Tri u = scenario_tri<SPEC>(P, make_view<SPEC, PRE>(P, fld, fct == 0 ? SC_VUP0 : SC_VUP1), K, true);
+    const Tri d = scenario_tri<SPEC>(P, make_view<SPEC, PRE>(P, fld, fct == 0 ? SC_VDN0 : SC_VDN1), K, true);
     q[fct == 0 ? 3 : 4] = (u.v - d.v) * P.vega_c[fct];
     q[fct == 0 ? 7 : 8] = ((u.dp - u.dm) - (d.dp - d.dm)) * P.vanna_c[fct];
   }
   {
-    const Tri u = scenario_tri<SPEC>(P, make_view<SPEC>(P, fld, SC_TUP), K, true);
-    const Tri d = scenario_tri<SPEC>(P, make_view<SPEC>(P, fld, SC_TDN), K, true);
+    const Tri u = scenario_tri<SPEC>(P, make_view<SPEC, PRE>(P, fld, SC_TUP), K, true);
+    const Tri d = scenario_tri<SPEC>(P, make_view<SPEC, PRE>(P, fld, SC_TDN), K, true);
     q[5] = ((u.v - d.v) + (u.v * P.dfm1_tup - d.v * P.dfm1_tdn)) * P.theta_c;
     const float du = u.dp - u.dm, dd = d.dp - d.dm;
     q[9] = ((du - dd) + (du * P.dfm1_tup - dd * P.dfm1_tdn)) * P.charm_c;
   }
   {
-    const Tri u = scenario_tri<SPEC>(P, make_view<SPEC>(P, fld, SC_RUP), K, false);
-    const Tri d = scenario_tri<SPEC>(P, make_view<SPEC>(P, fld, SC_RDN), K, false);
+    const Tri u = scenario_tri<SPEC>(P, make_view<SPEC, PRE>(P, fld, SC_RUP), K, false);
+    const Tri d = scenario_tri<SPEC>(P, make_view<SPEC, PRE>(P, fld, SC_RDN), K, false);
     q[6] = ((u.v - d.v) + (u.v * P.dfm1_rup - d.v * P.dfm1_rdn)) * P.rho_c;
   }
 }
 
 __device__ __forceinline__ int active_q(int mode) { return mode == 0 ? 1 : (mode == 1 ? 3 : kQ); }
 
+// SPEC = 1 stages one record field per scenario (European terminal log-spots), so its
+// blocks take a quarter of the staging memory and more of them fit on an SM.
 template <int SPEC>
-__global__ void __launch_bounds__(kPayoffBlock) payoff_reduce_kernel(const __grid_constant__ PayoffParams P) {
-  __shared__ float stage[kPayoffBlock / 32][kMaxScenarios * kMaxFields][33];
+__global__ void __launch_bounds__(kPayoffBlock, SPEC == 1 ? 8 : 0) payoff_reduce_kernel(const __grid_constant__ PayoffParams P) {
+  __shared__ float stage[kPayoffBlock / 32][kMaxScenarios * (SPEC == 1 ? 1 : kMaxFields)][33];
   __shared__ double red[kPayoffBlock / 32][2 * kQ][32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned long long tile = blockIdx.x;
@@ -146,7 +151,10 @@ __global__ void __launch_bounds__(kPayoffBlock) payoff_reduce_kernel(const __gri
   const unsigned long long w1 = min(w0 + per_warp, t1);
   for (unsigned long long b0 = w0; b0 < w1; b0 += 32) {
     const unsigned long long i = b0 + lane;
-    for (int j = 0; j < nsf; ++j) stage[warp][j][lane] = i < w1 ? P.records[(size_t)j * stride + i] : 0.0f;
+    for (int j = 0; j < nsf; ++j) {
+      const float x = i < w1 ? P.records[(size_t)j * stride + i] : 0.0f;
+      stage[warp][j][lane] = SPEC == 1 ? __expf(x) : x;
+    }
     __syncwarp();
     const int nb = (int)min((unsigned long long)32, w1 - b0);
     float s1[kQ], s2[kQ];
@@ -158,7 +166,7 @@ __global__ void __launch_bounds__(kPayoffBlock) payoff_reduce_kernel(const __gri
         float q[kQ];
 #pragma unroll
         for (int k = 0; k < kQ; ++k) q[k] = 0.0f;
-        path_quantities<SPEC>(P, fld, K, q);
+        path_quantities<SPEC, SPEC == 1>(P, fld, K, q);
 #pragma unroll
         for (int k = 0; k < kQ; ++k) {
           s1[k] += q[k];
@@ -213,7 +221,7 @@ __global__ void finalize_kernel(const FinalizeParams P) {
 cudaError_t launch_payoff(const PayoffParams &P, unsigned long long n_tiles, cudaStream_t stream) {
   if (n_tiles == 0) return cudaSuccess;
   const dim3 grid((unsigned int)n_tiles, P.n_strikes == 1 ? 1u : (unsigned int)((P.n_strikes + 31) / 32));
-  if (P.kind == 0 && P.payoff == 0 && P.tracker == TRK_EUROPEAN)
+  if (P.kind == 0 && P.payoff == 0 && P.tracker == TRK_EUROPEAN && P.n_sc * P.n_fields <= kMaxScenarios)
     dev::payoff_reduce_kernel<1><<<grid, kPayoffBlock, 0, stream>>>(P);
   else
     dev::payoff_reduce_kernel<0><<<grid, kPayoffBlock, 0, stream>>>(P);

@@ -1021,6 +1021,16 @@ def run_ncu_batch_case() -> None:
         eng.price_batch(jobs)
 
 
+def run_ncu_qmc_case() -> None:
+    """A small randomized-QMC case for ncu: the Double Bates Asian of the control-variate
+    comparison (SchemeNCI factors, Merton jumps, 256 steps) on 2^19 Sobol points in 16 replicates
+    (about 600 MB of records and tables on the device), priced twice."""
+    import myquantlib_gb300 as m
+    eng = m.Engine(0)
+    for _ in range(2):
+        eng.qmc_price(cv_jobs(m, "asian", 1 << 19)[0], 16)
+
+
 def run_ncu_case(full: bool = False) -> None:
     """One maturity (T = 1) of the workload, priced twice, for an ncu capture: 2^18 paths (a few
     hundred MB on the device), or the full 2^22 paths for one-pass metrics."""
@@ -1042,10 +1052,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-cv", action="store_true", help="skip the time-to-relative-SE block of the strip line")
     ap.add_argument("--fourier-seeds", type=int, default=8, help="seeds of the multi-seed Fourier check")
-    ap.add_argument("--workload", choices=["strip", "batch", "cv", "mlmc", "c1"], default="strip",
+    ap.add_argument("--workload", choices=["strip", "batch", "cv", "mlmc", "c1", "qmc"], default="strip",
                     help="strip: the Bates Full-Greeks strip (headline); batch: uneven requests in one launch; "
                          "cv: time-to-relative-SE of the neural control variate against plain MC; mlmc: MLMC "
-                         "with and without the control variate; c1: plain Heston NV European (configuration 1)")
+                         "with and without the control variate; c1: plain Heston NV European (configuration 1); "
+                         "qmc: randomized QMC (profiling case only, with --ncu-case)")
     ap.add_argument("--batch-jobs", type=int, default=4096)
     ap.add_argument("--ncu-case", action="store_true",
                     help="profiling case: one maturity (T=1), 2^18 paths, two requests, no timing")
@@ -1062,9 +1073,13 @@ def main():
             run_ncu_c1_case()
         elif args.workload == "mlmc":
             run_ncu_mlmc_case()
+        elif args.workload == "qmc":
+            run_ncu_qmc_case()
         else:
             run_ncu_case(full=args.ncu_full)
         return
+    if args.workload == "qmc":
+        ap.error("--workload qmc is a profiling case: use it with --ncu-case")
     if args.impl == "reference":
         line = run_reference(args)
     else:

@@ -18,6 +18,31 @@ struct Xo {
   unsigned long long a, b, c, d;
 };
 
+// Packed FP32 pairs (sm_100 and later): each lane rounds as the scalar instruction.
+namespace pk {
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
+  float2 r;
+  asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "mov.b64 rc, {%6, %7};\n\tfma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return r;
+}
+__device__ __forceinline__ float2 fmul2(float2 a, float2 b) {
+  float2 r;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "mul.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+__device__ __forceinline__ float2 fadd2(float2 a, float2 b) {
+  float2 r;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "add.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+}  // namespace pk
+
 __device__ __forceinline__ unsigned long long rotl64(unsigned long long x, int k) {
   return (x << k) | (x >> (64 - k));
 }
@@ -455,10 +480,21 @@ __device__ __forceinline__ void poisson_eval_n(const float (&lam)[NS], float U,
       }
       nf = (float)n;
       const float r = rcp_approx(nf);
+      if constexpr (NS == 3) {  // means 1 and 2 on packed FP32 pairs
+        p[0] *= lam[0] * r;
+        F[0] += p[0];
+        const float2 pp = pk::fmul2(make_float2(p[1], p[2]), pk::fmul2(make_float2(lam[1], lam[2]), make_float2(r, r)));
+        const float2 ff = pk::fadd2(make_float2(F[1], F[2]), pp);
+        p[1] = pp.x;
+        p[2] = pp.y;
+        F[1] = ff.x;
+        F[2] = ff.y;
+      } else {
 #pragma unroll
-      for (int j = 0; j < NS; ++j) {
-        p[j] *= lam[j] * r;
-        F[j] += p[j];
+        for (int j = 0; j < NS; ++j) {
+          p[j] *= lam[j] * r;
+          F[j] += p[j];
+        }
       }
     }
   }

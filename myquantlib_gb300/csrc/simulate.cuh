@@ -350,6 +350,7 @@ __global__ void __launch_bounds__(kSimBlock) simulate_kernel(const __grid_consta
 // run per scenario.  Every scenario's arithmetic is the per-scenario kernel's,
 // so its record is bit-identical.
 
+
 // Simulated scenarios of a European Full request in lockstep order: base,
 // v0 (or factor-0 v0) up / down, T up / down, then factor-1 v0 up / down.
 __host__ __device__ constexpr int lockstep_sc(int j) { return j < 5 ? j : j + 2; }
@@ -410,21 +411,49 @@ __device__ __forceinline__ void evolve_lockstep(const float (&v)[NS], float (&vn
   } else {
     float lam[NS];
     int N[NS];
+    constexpr bool PAIR = NS == 3;  // scenarios 1 and 2 (T up, T down) on packed pairs
+    if constexpr (PAIR) {
+      lam[0] = P.sc[sc(0)].f[fi].w0 * v[0];
+      const float2 l = pk::fmul2(make_float2(P.sc[sc(1)].f[fi].w0, P.sc[sc(2)].f[fi].w0), make_float2(v[1], v[2]));
+      lam[1] = l.x;
+      lam[2] = l.y;
+    } else {
 #pragma unroll
-    for (int j = 0; j < NS; ++j) lam[j] = P.sc[sc(j)].f[fi].w0 * v[j];
+      for (int j = 0; j < NS; ++j) lam[j] = P.sc[sc(j)].f[fi].w0 * v[j];
+    }
     poisson_eval_n<NS>(lam, d.U, d.xp, P.loop_cap, caphits, N);
     const NciTable &tab = P.nci[fi];
     float4 c[NS];
 #pragma unroll
     for (int j = 0; j < NS; ++j) c[j] = nci_cell(tab, N[j], d.pos);
+    float q[NS];
+    if constexpr (PAIR) {
+      q[0] = nci_cubic(c[0], d.pos.t);
+      const float2 t2 = make_float2(d.pos.t, d.pos.t);
+      float2 h = pk::ffma2(make_float2(c[1].w, c[2].w), t2, make_float2(c[1].z, c[2].z));
+      h = pk::ffma2(h, t2, make_float2(c[1].y, c[2].y));
+      h = pk::ffma2(h, t2, make_float2(c[1].x, c[2].x));
+      q[1] = h.x;
+      q[2] = h.y;
+    } else {
+#pragma unroll
+      for (int j = 0; j < NS; ++j) q[j] = nci_cubic(c[j], d.pos.t);
+    }
 #pragma unroll
     for (int j = 0; j < NS; ++j) {
-      float q = nci_cubic(c[j], d.pos.t);
       if (N[j] >= tab.rows) {
         fallbacks += (SUB && j == 0) ? 1 + merged : 1;
-        q = nci_beyond(tab, N[j], d.x2);
+        q[j] = nci_beyond(tab, N[j], d.x2);
       }
-      vn[j] = q * P.sc[sc(j)].f[fi].w2;
+    }
+    if constexpr (PAIR) {
+      vn[0] = q[0] * P.sc[sc(0)].f[fi].w2;
+      const float2 w = pk::fmul2(make_float2(q[1], q[2]), make_float2(P.sc[sc(1)].f[fi].w2, P.sc[sc(2)].f[fi].w2));
+      vn[1] = w.x;
+      vn[2] = w.y;
+    } else {
+#pragma unroll
+      for (int j = 0; j < NS; ++j) vn[j] = q[j] * P.sc[sc(j)].f[fi].w2;
     }
   }
 }
@@ -504,6 +533,32 @@ __device__ __forceinline__ void lockstep_step(const SimParams &P, Xo &rng, float
   } else {
     evolve_lockstep<S1, NSIM>(va, van, da, P, 0, caphits, fallbacks);
     if (NF == 2) evolve_lockstep<S2, NSIM>(vb, vbn, db, P, 1, caphits, fallbacks);
+  }
+  if constexpr (NF == 1) {
+    // scenarios 1..NSIM-1 in pairs on packed FP32 (each lane rounds as the scalar form)
+    {
+      const FactorConst &f = P.sc[0].f[0];
+      const float vn = van[0];
+      const float root = sqrt_approx(f.C3 * (va[0] + vn));
+      const float drift = fmaf(f.C2, vn, fmaf(f.C1, va[0], f.C0));
+      X[0] += fmaf(root, G, drift);
+      va[0] = vn;
+    }
+#pragma unroll
+    for (int j = 1; j + 1 < NSIM; j += 2) {
+      const FactorConst &f = P.sc[lockstep_sc(j)].f[0], &g = P.sc[lockstep_sc(j + 1)].f[0];
+      const float2 v0 = make_float2(va[j], va[j + 1]), v1 = make_float2(van[j], van[j + 1]);
+      const float2 c3 = pk::fmul2(make_float2(f.C3, g.C3), pk::fadd2(v0, v1));
+      const float2 root = make_float2(sqrt_approx(c3.x), sqrt_approx(c3.y));
+      const float2 drift = pk::ffma2(make_float2(f.C2, g.C2), v1,
+                                      pk::ffma2(make_float2(f.C1, g.C1), v0, make_float2(f.C0, g.C0)));
+      const float2 x = pk::fadd2(make_float2(X[j], X[j + 1]), pk::ffma2(root, make_float2(G, G), drift));
+      X[j] = x.x;
+      X[j + 1] = x.y;
+      va[j] = v1.x;
+      va[j + 1] = v1.y;
+    }
+    return;
   }
 #pragma unroll
   for (int j = 0; j < NSIM; ++j) {

@@ -19,6 +19,8 @@
 #include <cuda_bf16.h>
 #include <cstdint>
 
+#include "device_numerics.cuh"
+
 namespace myql {
 namespace tc {
 
@@ -167,16 +169,8 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
                :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(b)) : "memory");
 }
 
-// Packed FP32 pairs (sm_100 and later): one instruction for two lanes of IEEE fma / mul,
-// each lane rounded exactly as the scalar instruction would.
-__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
-  float2 r;
-  asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
-      "mov.b64 rc, {%6, %7};\n\tfma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
-      : "=f"(r.x), "=f"(r.y)
-      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
-  return r;
-}
+// Packed FP32 pairs: the engine's helpers (device_numerics.cuh)
+using dev::pk::ffma2;
 
 // SiLU through tanh.approx: x * sigmoid(x) = 0.5 x (1 + tanh(x / 2)).
 __device__ __forceinline__ float tanh_fast(float x) {

@@ -12,6 +12,7 @@
 // finalize_kernel sums the tile partials in a fixed order (deterministic) and
 // applies compute_stats (MonteCarloPricer.hpp:448-457).
 #include "engine_types.h"
+#include "device_numerics.cuh"
 #include "payoff.cuh"
 
 namespace myql {
@@ -57,8 +58,12 @@ __device__ __forceinline__ void path_quantities(const PayoffParams &P, FLD fld, 
   const Tri b = scenario_tri<SPEC>(P, make_view<SPEC, PRE>(P, fld, 0), K, bumps);
   q[0] = b.v;
   if (!bumps) return;
-  q[1] = (b.dp - b.dm) * P.inv_2h;
-  q[2] = (b.dp + b.dm) * P.inv_h2;
+  {  // delta and gamma as one packed pair: (dp - dm) / 2h, (dp + dm) / h^2
+    const float2 dg = pk::fmul2(pk::fadd2(make_float2(b.dp, b.dp), make_float2(-b.dm, b.dm)),
+                                make_float2(P.inv_2h, P.inv_h2));
+    q[1] = dg.x;
+    q[2] = dg.y;
+  }
   if (P.mode == 1) return;
   const int nv = P.n_factors >= 2 ? 2 : 1;
   for (int fct = 0; fct < nv; ++fct) {
@@ -167,10 +172,16 @@ __global__ void __launch_bounds__(kPayoffBlock, SPEC == 1 ? 8 : 0) payoff_reduce
 #pragma unroll
         for (int k = 0; k < kQ; ++k) q[k] = 0.0f;
         path_quantities<SPEC, SPEC == 1>(P, fld, K, q);
+        static_assert(kQ % 2 == 0, "quantities in pairs");
 #pragma unroll
-        for (int k = 0; k < kQ; ++k) {
-          s1[k] += q[k];
-          s2[k] = fmaf(q[k], q[k], s2[k]);
+        for (int k = 0; k < kQ; k += 2) {  // packed FP32 pairs: each lane rounds as the scalar form
+          const float2 qq = make_float2(q[k], q[k + 1]);
+          const float2 a1 = pk::fadd2(make_float2(s1[k], s1[k + 1]), qq);
+          const float2 a2 = pk::ffma2(qq, qq, make_float2(s2[k], s2[k + 1]));
+          s1[k] = a1.x;
+          s1[k + 1] = a1.y;
+          s2[k] = a2.x;
+          s2[k + 1] = a2.y;
         }
       }
     }

@@ -759,7 +759,7 @@ def time_to_se(eng, m, kind: str, target: float, probe_paths: int = 1 << 22, top
     # the same network on randomized QMC paths: sized like qmc_time_to_se from its own probe
     R, quantum = 16, 16 * 2048
     qprobe = eng.cv_qmc_price(cv_jobs(m, kind, 1 << 20, seed=44)[0], cfg, R)
-    n_cvq = max(-(-int((1 << 20) * (qprobe.price_std_err / (0.9 * target * qprobe.price)) ** 2) // quantum) * quantum,
+    n_cvq = max(-(-int((1 << 20) * (qprobe.price_std_err / (0.85 * target * qprobe.price)) ** 2) // quantum) * quantum,
                 quantum)
     cvq_last = {"sim_ms": 0.0, "mlp_ms": 0.0, "price_ms": 0.0}
 
@@ -857,7 +857,7 @@ def qmc_time_to_se(eng, m, kind: str = "european", target: float = 1e-4, R: int 
     quasi-Monte Carlo (Sobol + Brownian bridge for the normals, Sobol uniforms for the NCI and jump
     draws, R digital shifts): wall time to the relative standard error target against plain GPU
     Monte Carlo.  An untimed probe fixes the QMC error at one size.  The timed run prices the
-    point count that the plain 1/sqrt(n) rate gives for 0.9 x the target (a margin on the
+    point count that the plain 1/sqrt(n) rate gives for 0.85 x the target (a margin on the
     R-replicate error estimate, itself noisy), in whole 2048-point blocks per replicate; while the
     pooled error is still above the target it prices the shortfall on fresh seeds and pools the
     runs (at most `top_ups` times), every run inside the timed region."""
@@ -869,7 +869,7 @@ def qmc_time_to_se(eng, m, kind: str = "european", target: float = 1e-4, R: int 
     def size(n):  # whole 2048-point blocks per replicate
         return max(-(-int(n) // quantum) * quantum, quantum)
 
-    n_q = size(probe_paths * (q[1, 0] / (0.9 * target * q[0, 0])) ** 2)
+    n_q = size(probe_paths * (q[1, 0] / (0.85 * target * q[0, 0])) ** 2)
     pj, _ = cv_jobs(m, kind, 1 << 22)
     raw, _ = eng.price(pj)
     n_plain = int((1 << 22) * (raw[1, 0] / (target * raw[0, 0])) ** 2) + 1

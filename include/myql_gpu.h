@@ -366,8 +366,10 @@ myql_status myql_ml2r_price(myql_ctx *ctx, const myql_mc_job *job, const myql_ml
  * num_paths a multiple of 2048 * n_replicates (n_replicates >= 2). */
 myql_status myql_qmc_price(myql_ctx *ctx, const myql_mc_job *job, uint32_t n_replicates, double *out,
                            myql_mc_stats *stats);
-/* The Sobol direction numbers of myql_qmc_price: out[d * 32 + k - 1] = V_k of
- * dimension d (host computation; needs no GPU). */
+/* Sobol direction numbers: out[d * 32 + k - 1] = V_k of dimension d, the initial
+ * values m_1..m_s of each dimension drawn from `seed` (host computation; needs no
+ * GPU).  myql_qmc_price and myql_cv_qmc_price use seed 0's for every job; the
+ * job's seed draws their digital shifts. */
 myql_status myql_qmc_directions(uint32_t D, uint64_t seed, uint32_t *out);
 
 /* One evaluate_level call of the MLMC pricer (MultiLevelMonteCarloPricer.hpp:244-341)

@@ -6,13 +6,17 @@
 //     32 consecutive points share the Gray code's high bits, so one pass over 32
 //     dimensions builds their 32 x 32 coordinates in shared memory (SobolWarp);
 //     direction numbers from primitive polynomials over GF(2) by the Bratley-Fox
-//     recurrence (ACM TOMS 659), dimension 0 the van der Corput sequence.  The initial direction
-//     numbers m_1..m_s of each dimension are odd integers m_k < 2^k drawn from
-//     splitmix64 (a randomly initialised Sobol sequence, not a published table);
-//   * each Brownian motion of the step (the spot's and one per CIR factor) is
-//     built by a Brownian bridge on the step grid, coarse points first, and the
-//     bridge levels of all motions are interleaved so that the first Sobol
-//     dimensions carry the paths' coarse shape;
+//     recurrence (ACM TOMS 659), dimension 0 the van der Corput sequence.  The
+//     initial direction numbers m_1..m_s of each dimension are odd integers
+//     m_k < 2^k drawn from splitmix64 with a fixed seed (a randomly initialised
+//     Sobol sequence, not a published table), the same for every job;
+//   * each Gaussian motion (the spot's and one per SchemeNV factor) is built by
+//     a Brownian bridge on the step grid in segments of 32 steps: first its
+//     values at the segment boundaries (breadth first, end point first), so
+//     that the lowest Sobol dimensions carry the paths' coarse shape, then per
+//     segment the interior of its bridge (breadth first); the motions
+//     interleave at every bridge point.  A thread holds one segment's values
+//     at a time (a whole-path bridge in local memory spilled to DRAM);
 //   * R independent random digital shifts (one 32-bit XOR mask per replicate and
 //     dimension) give R unbiased replicate estimates; the price is their mean and
 //     the standard error comes from their spread.
@@ -26,8 +30,9 @@
 //     and the normal of the jump sum (n mu + sqrt(n) delta Z, JumpPolicies.hpp:55-75);
 //     the jumps of every instrument are drawn per step, whose sum has the law of
 //     the one draw over T a European stepper makes.
-// The bridge dimensions come first (b * NG + c for bridge point b and Gaussian
-// motion c), then the per-step uniforms (n NG + k NU + u).  SchemeExact (a
+// Dimension order: the boundary points (NG per point), then per segment its
+// interior bridge points (NG each) followed by its steps' uniforms (NU each), so
+// a path consumes its dimensions strictly in order.  SchemeExact (a
 // rejection loop) and Kou jumps (one exponential per jump) have a variable number
 // of draws and are not offered.  The log-spot steps as in ASVJstepper.hpp:134-229,
 // with the trackers of the path kernels; the per-path records go through the
@@ -210,36 +215,47 @@ struct Bridge {
   std::vector<float> wl, wr, sd;
 };
 
-// Brownian bridge on the unit step grid 0..n, coarse points first (breadth first)
-Bridge brownian_bridge(int n) {
+// Brownian bridge schedule on the unit step grid 0..n in segments of kQmcSeg steps.
+// First the bridge over the segment boundaries 0, L, 2L, .., n (breadth first, indices in
+// segments, the end point first), then per segment the bridge over its interior points
+// (breadth first, in steps from the segment's start).  n entries in all.
+Bridge segmented_bridge(int n) {
+  const int L = kQmcSeg, ns = (n + L - 1) / L;
+  auto pos = [&](int s) { return std::min(s * L, n); };
   Bridge B;
-  B.mid.push_back(n);
+  auto push = [&](int m, int l, int r, double tm, double tl, double tr) {
+    B.mid.push_back(m);
+    B.left.push_back(l);
+    B.right.push_back(r);
+    B.wl.push_back((float)((tr - tm) / (tr - tl)));
+    B.wr.push_back((float)((tm - tl) / (tr - tl)));
+    B.sd.push_back((float)std::sqrt((tm - tl) * (tr - tm) / (tr - tl)));
+  };
+  auto breadth_first = [&](int a, int b, auto t) {  // interior points of (a, b), t(index) = step
+    std::vector<std::pair<int, int>> q{{a, b}};
+    for (size_t h = 0; h < q.size(); ++h) {
+      const int l = q[h].first, r = q[h].second;
+      if (r - l < 2) continue;
+      const int m = (l + r) / 2;
+      push(m, l, r, t(m), t(l), t(r));
+      q.push_back({l, m});
+      q.push_back({m, r});
+    }
+  };
+  B.mid.push_back(ns);  // the end point: W(n) ~ N(0, n)
   B.left.push_back(0);
   B.right.push_back(0);
   B.wl.push_back(0.0f);
   B.wr.push_back(0.0f);
   B.sd.push_back((float)std::sqrt((double)n));
-  std::vector<std::pair<int, int>> q{{0, n}};
-  for (size_t h = 0; h < q.size(); ++h) {
-    const int l = q[h].first, r = q[h].second;
-    if (r - l < 2) continue;
-    const int m = (l + r) / 2;
-    B.mid.push_back(m);
-    B.left.push_back(l);
-    B.right.push_back(r);
-    B.wl.push_back((float)((double)(r - m) / (double)(r - l)));
-    B.wr.push_back((float)((double)(m - l) / (double)(r - l)));
-    B.sd.push_back((float)std::sqrt((double)(m - l) * (double)(r - m) / (double)(r - l)));
-    q.push_back({l, m});
-    q.push_back({m, r});
-  }
+  breadth_first(0, ns, [&](int s) { return (double)pos(s); });
+  for (int s = 0; s < ns; ++s) breadth_first(0, pos(s + 1) - pos(s), [](int k) { return (double)k; });
   return B;
 }
 
 struct QmcState : ExtState {
   DevBuf dirs, shift, bridge;
   unsigned int dirs_D = 0;
-  uint64_t dirs_seed = 0;
   int bridge_n = -1;
 };
 
@@ -281,8 +297,10 @@ myql_status qmc_prepare(CtxBase *ctx, const myql_mc_job &job, const Plan &pl, ui
   cudaStream_t st = ctx->stream;
   cudaError_t e = cudaSuccess;
   // tables: direction numbers, shifts, bridge
-  if (S.dirs_D != D || S.dirs_seed != seed) {
-    const std::vector<uint32_t> V = sobol_directions(D, seed);
+  // one point set per dimension count (direction numbers from kQmcDirectionSeed); the
+  // job's seed draws the digital shifts, which alone make the replicates independent
+  if (S.dirs_D != D) {
+    const std::vector<uint32_t> V = sobol_directions(D, kQmcDirectionSeed);
     if ((size_t)D * kQmcBits > V.size() || V[(size_t)(D - 1) * kQmcBits] == 0u)
       return set_error(MYQL_ERR_TOO_LARGE, "too many quasi-Monte Carlo dimensions");
     std::vector<uint32_t> Vt(V.size());  // bit-major on the device: a warp's dimensions are contiguous
@@ -292,7 +310,6 @@ myql_status qmc_prepare(CtxBase *ctx, const myql_mc_job &job, const Plan &pl, ui
     if (e == cudaSuccess) e = cudaMemcpy(S.dirs.p, Vt.data(), Vt.size() * 4, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_status(e, "Sobol directions");
     S.dirs_D = D;
-    S.dirs_seed = seed;
   }
   std::vector<uint32_t> sh((size_t)R * D);
   uint64_t ss = seed ^ 0x8BB84B93962EACC9ull;
@@ -303,7 +320,7 @@ myql_status qmc_prepare(CtxBase *ctx, const myql_mc_job &job, const Plan &pl, ui
   if (e != cudaSuccess) return cuda_status(e, "digital shifts");
   const int n = pl.steps;
   if (S.bridge_n != n) {
-    const Bridge B = brownian_bridge(n);
+    const Bridge B = segmented_bridge(n);
     std::vector<uint8_t> blob((size_t)n * 24);
     std::memcpy(blob.data(), B.mid.data(), n * 4);
     std::memcpy(blob.data() + 4 * n, B.left.data(), n * 4);

@@ -9,12 +9,14 @@ namespace myql {
 
 constexpr int kQmcMaxSteps = 512;
 constexpr int kQmcBits = 32;
+constexpr int kQmcSeg = 32;  // steps per bridge segment
+constexpr uint64_t kQmcDirectionSeed = 0;  // initial direction numbers of the pricers' point sets
 
 struct QmcParams {
   SimParams P;                 // plan constants (records, trackers, scenario 0)
   const uint32_t *dirs;        // [32][D] direction numbers V_1..V_32, bit-major
   const uint32_t *shift;       // [R][D] digital shifts
-  const int *br_mid, *br_left, *br_right;  // Brownian bridge, construction order
+  const int *br_mid, *br_left, *br_right;  // segmented Brownian bridge schedule (n entries)
   const float *br_wl, *br_wr, *br_sd;
   unsigned long long n_pts;    // points per replicate
   unsigned int D;              // dimensions per path = steps * (NG + NU)
@@ -111,28 +113,32 @@ __device__ __forceinline__ SobolWarp sobol_warp(const QmcParams &Q, uint32_t *ta
   return sob;
 }
 
-// One path of the replicated point set, scenario 0: the Brownian bridges of its Gaussian
-// motions, then the steps with their per-step uniforms, in dimension order.  The hook sees
-// every step as in sim_path_h (begin, diffusion, jump, step_end, finish).  Writes the
-// tracker's terminal record.
+// One path of the replicated point set, scenario 0, in dimension order.  The Brownian bridge
+// of each Gaussian motion comes in segments of kQmcSeg steps: first its values at the segment
+// boundaries (the coarse shape of the path, the lowest dimensions), then segment by segment
+// the interior of the segment's bridge followed by the segment's steps with their per-step
+// uniforms.  Only one segment's values are held at a time.  The hook sees every step as in
+// sim_path_h (begin, diffusion, jump, step_end, finish).  Writes the tracker's terminal record.
 template <int NF, bool PD, class Hook>
 __device__ __forceinline__ void qmc_path(const QmcParams &Q, SobolWarp &sob, float (&out)[kMaxFields],
                                          unsigned int &caphits, unsigned int &fallbacks, Hook &hook) {
   const SimParams &P = Q.P;
   const int n = P.n_steps;
   constexpr int NC = 1 + NF;  // at most: the spot's motion and one per NV factor
+  constexpr int kSegs = kQmcMaxSteps / kQmcSeg;
   const int NG = Q.NG;
-  float W[NC][kQmcMaxSteps + 1];
+  const int ns = (n + kQmcSeg - 1) / kQmcSeg;
+  float Wc[NC][kSegs + 1];  // values at the segment boundaries
 #pragma unroll
-  for (int c = 0; c < NC; ++c) W[c][0] = 0.0f;
-  for (int b = 0; b < n; ++b) {
+  for (int c = 0; c < NC; ++c) Wc[c][0] = 0.0f;
+  for (int b = 0; b < ns; ++b) {
     const int m = Q.br_mid[b], l = Q.br_left[b], r = Q.br_right[b];
     const float wl = Q.br_wl[b], wr = Q.br_wr[b], sd = Q.br_sd[b];
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
       if (c >= NG) break;
-      const float z = inv_normal_bits(sob.next());  // dimension b * NG + c
-      W[c][m] = fmaf(wl, W[c][l], fmaf(wr, W[c][r], sd * z));
+      const float z = inv_normal_bits(sob.next());
+      Wc[c][m] = fmaf(wl, Wc[c][l], fmaf(wr, Wc[c][r], sd * z));
     }
   }
   const ScenarioConst &C = P.sc[0];
@@ -141,61 +147,82 @@ __device__ __forceinline__ void qmc_path(const QmcParams &Q, SobolWarp &sob, flo
   ts.init(P, PD);
   if (Hook::active) hook.begin(v[0], v[1]);
   const float dt = C.dt;
-  for (int k = 0; k < n; ++k) {  // step k's uniforms are dimensions n NG + k NU + u
-    const float G = W[0][k + 1] - W[0][k];
-    if (NF == 0) {
-      X += fmaf(C.gbm_vol, G, C.gbm_drift);
-      if (Hook::active) hook.diffusion(C.gbm_vol, G, C.gbm_drift);
-    } else {
-      float vn[2] = {0.0f, 0.0f};
-      int gi = 1;  // next Gaussian motion (NV factors, in factor order)
+  int e = ns;  // next bridge schedule entry
+  for (int sg = 0; sg < ns; ++sg) {
+    const int k0 = sg * kQmcSeg, len = min(kQmcSeg, n - k0);
+    float W[NC][kQmcSeg + 1];  // this segment's values, from its start
 #pragma unroll
-      for (int f = 0; f < NF; ++f) {
-        const FactorConst &fc = C.f[f];
-        if (Q.sch[f] == SCH_NV) {
-          const float Z = gi == 1 ? W[1][k + 1] - W[1][k] : W[NC - 1][k + 1] - W[NC - 1][k];
-          ++gi;
-          const float rt = sqrt_approx(fmaf(fc.w0, v[f], fc.w1)) + fc.w2 * Z;
-          vn[f] = fmaf(fc.w0 * rt, rt, fc.w1);
-        } else {  // SchemeNCI: N ~ Poisson(C0 v) by inversion, then the table at the second uniform
-          const unsigned long long xp = sob.next();
-          const unsigned long long x2 = sob.next();
-          const float lam = fc.w0 * v[f];
-          const float Wp = lam > kPoissonAsymMin ? inv_normal_bits(xp) : 0.0f;
-          const int N = poisson_core(lam, u01_bits(xp), Wp, xp, P.loop_cap, caphits);
-          vn[f] = nci_quantile(P.nci[f], N, x2, P.nci_u999, fallbacks) * fc.w2;
-        }
+    for (int c = 0; c < NC; ++c) {
+      W[c][0] = Wc[c][sg];
+      W[c][len] = Wc[c][sg + 1];
+    }
+    for (int b = 0; b < len - 1; ++b, ++e) {
+      const int m = Q.br_mid[e], l = Q.br_left[e], r = Q.br_right[e];
+      const float wl = Q.br_wl[e], wr = Q.br_wr[e], sd = Q.br_sd[e];
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        if (c >= NG) break;
+        const float z = inv_normal_bits(sob.next());
+        W[c][m] = fmaf(wl, W[c][l], fmaf(wr, W[c][r], sd * z));
       }
-      float root, drift;
-      if (NF == 1) {
-        const FactorConst &f0 = C.f[0];
-        root = sqrt_approx(f0.C3 * (v[0] + vn[0]));
-        drift = fmaf(f0.C2, vn[0], fmaf(f0.C1, v[0], f0.C0));
+    }
+    for (int kk = 0; kk < len; ++kk) {  // the segment's steps, each with its NU uniforms
+      const int k = k0 + kk;
+      const float G = W[0][kk + 1] - W[0][kk];
+      if (NF == 0) {
+        X += fmaf(C.gbm_vol, G, C.gbm_drift);
+        if (Hook::active) hook.diffusion(C.gbm_vol, G, C.gbm_drift);
       } else {
-        const FactorConst &f0 = C.f[0];
-        const FactorConst &f1 = C.f[1];
-        root = sqrt_approx(fmaf(f0.C3, v[0] + vn[0], f1.C3 * (v[1] + vn[1])));
-        drift = fmaf(f1.C2, vn[1], fmaf(f1.C1, v[1], fmaf(f0.C2, vn[0], fmaf(f0.C1, v[0], f0.C0 + f1.C0))));
+        float vn[2] = {0.0f, 0.0f};
+        int gi = 1;  // next Gaussian motion (NV factors, in factor order)
+  #pragma unroll
+        for (int f = 0; f < NF; ++f) {
+          const FactorConst &fc = C.f[f];
+          if (Q.sch[f] == SCH_NV) {
+            const float Z = gi == 1 ? W[1][kk + 1] - W[1][kk] : W[NC - 1][kk + 1] - W[NC - 1][kk];
+            ++gi;
+            const float rt = sqrt_approx(fmaf(fc.w0, v[f], fc.w1)) + fc.w2 * Z;
+            vn[f] = fmaf(fc.w0 * rt, rt, fc.w1);
+          } else {  // SchemeNCI: N ~ Poisson(C0 v) by inversion, then the table at the second uniform
+            const unsigned long long xp = sob.next();
+            const unsigned long long x2 = sob.next();
+            const float lam = fc.w0 * v[f];
+            const float Wp = lam > kPoissonAsymMin ? inv_normal_bits(xp) : 0.0f;
+            const int N = poisson_core(lam, u01_bits(xp), Wp, xp, P.loop_cap, caphits);
+            vn[f] = nci_quantile(P.nci[f], N, x2, P.nci_u999, fallbacks) * fc.w2;
+          }
+        }
+        float root, drift;
+        if (NF == 1) {
+          const FactorConst &f0 = C.f[0];
+          root = sqrt_approx(f0.C3 * (v[0] + vn[0]));
+          drift = fmaf(f0.C2, vn[0], fmaf(f0.C1, v[0], f0.C0));
+        } else {
+          const FactorConst &f0 = C.f[0];
+          const FactorConst &f1 = C.f[1];
+          root = sqrt_approx(fmaf(f0.C3, v[0] + vn[0], f1.C3 * (v[1] + vn[1])));
+          drift = fmaf(f1.C2, vn[1], fmaf(f1.C1, v[1], fmaf(f0.C2, vn[0], fmaf(f0.C1, v[0], f0.C0 + f1.C0))));
+        }
+        X += fmaf(root, G, drift);
+        if (Hook::active) hook.diffusion(root, G, drift);
+        v[0] = vn[0];
+        v[1] = vn[1];
       }
-      X += fmaf(root, G, drift);
-      if (Hook::active) hook.diffusion(root, G, drift);
-      v[0] = vn[0];
-      v[1] = vn[1];
-    }
-    if (Q.jump) {  // Merton, per step: count by sequential inversion, then one normal for the sum
-      const unsigned long long xc = sob.next();
-      const unsigned long long xz = sob.next();
-      const int nj = poisson_small_u(C.jump_mean, C.jump_exp_neg_mean, u01_bits(xc), P.loop_cap, caphits);
-      float J = C.jump_comp;
-      if (nj > 0) {
-        const float fn = (float)nj;
-        J += fn * P.merton_mu + sqrtf(fn) * P.merton_delta * inv_normal_bits(xz);
+      if (Q.jump) {  // Merton, per step: count by sequential inversion, then one normal for the sum
+        const unsigned long long xc = sob.next();
+        const unsigned long long xz = sob.next();
+        const int nj = poisson_small_u(C.jump_mean, C.jump_exp_neg_mean, u01_bits(xc), P.loop_cap, caphits);
+        float J = C.jump_comp;
+        if (nj > 0) {
+          const float fn = (float)nj;
+          J += fn * P.merton_mu + sqrtf(fn) * P.merton_delta * inv_normal_bits(xz);
+        }
+        X += J;
+        if (Hook::active) hook.jump(J);
       }
-      X += J;
-      if (Hook::active) hook.jump(J);
+      if (PD) ts.step(P, k, dt, X);
+      if (Hook::active) hook.step_end(k + 1, X, v[0], v[1], ts.acc, ts.tb >= 0.0f);
     }
-    if (PD) ts.step(P, k, dt, X);
-    if (Hook::active) hook.step_end(k + 1, X, v[0], v[1], ts.acc, ts.tb >= 0.0f);
   }
   if (Hook::active) hook.finish();
   ts.finish(P, C, X, PD, out);

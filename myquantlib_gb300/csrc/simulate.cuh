@@ -536,6 +536,7 @@ __device__ __forceinline__ void lockstep_step(const SimParams &P, Xo &rng, float
   }
   if constexpr (NF == 1) {
     // scenarios 1..NSIM-1 in pairs on packed FP32 (each lane rounds as the scalar form)
+    static_assert(NSIM % 2 == 1, "the base and pairs of bumped scenarios");
     {
       const FactorConst &f = P.sc[0].f[0];
       const float vn = van[0];
@@ -558,19 +559,10 @@ __device__ __forceinline__ void lockstep_step(const SimParams &P, Xo &rng, float
       va[j] = v1.x;
       va[j + 1] = v1.y;
     }
-    return;
-  }
+  } else {
 #pragma unroll
-  for (int j = 0; j < NSIM; ++j) {
-    const ScenarioConst &C = P.sc[lockstep_sc(j)];
-    if (NF == 1) {
-      const FactorConst &f = C.f[0];
-      const float vn = van[j];
-      const float root = sqrt_approx(f.C3 * (va[j] + vn));
-      const float drift = fmaf(f.C2, vn, fmaf(f.C1, va[j], f.C0));
-      X[j] += fmaf(root, G, drift);
-      va[j] = vn;
-    } else {
+    for (int j = 0; j < NSIM; ++j) {
+      const ScenarioConst &C = P.sc[lockstep_sc(j)];
       const FactorConst &f0 = C.f[0];
       const FactorConst &f1 = C.f[1];
       const float root = sqrt_approx(fmaf(f0.C3, va[j] + van[j], f1.C3 * (vb[j] + vbn[j])));

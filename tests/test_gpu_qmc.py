@@ -102,3 +102,22 @@ def test_qmc_bates_nci_call_against_fourier(engine):
     finally:
         engine.set_nci_slopes(0)
     assert abs(q[0, 0] - 9.675798595347402) < 4 * q[1, 0] + 2e-3, (q[0, 0], q[1, 0])
+
+
+@pytest.mark.parametrize("steps", [1, 33, 512])
+def test_qmc_segment_edges_unbiased(engine, steps):
+    """The segmented bridge at its edges: one step (a single one-step segment), 33 steps (a last
+    segment of one step) and the 512-step maximum (16 full segments), against the plain engine."""
+    model, stepper = m.HestonModel(H1), m.HestonStepper(m.SchemeNV, m.TrackerArithAsian)
+    instr = lambda: m.AsianOption(m.TrackerArithAsian, m.PayoffVanilla(), True, 100.0, 1.0)  # noqa: E731
+    q, _ = engine.qmc_price(job(model, stepper, instr(), 1 << 18, steps), 16)
+    p, _ = engine.price(job(model, stepper, instr(), 1 << 21, steps, seed=11))
+    assert abs(q[0, 0] - p[0, 0]) < 4.0 * np.hypot(q[1, 0], p[1, 0]), (steps, q[0, 0], p[0, 0], q[1, 0], p[1, 0])
+    assert q[1, 0] < p[1, 0] * np.sqrt((1 << 21) / (1 << 18)), (q[1, 0], p[1, 0])  # no worse than plain MC
+
+
+def test_qmc_refuses_more_than_512_steps(engine):
+    with pytest.raises(_abi.MyqlError) as e:
+        engine.qmc_price(job(m.HestonModel(H1), m.HestonStepper(m.SchemeNV), m.EuropeanOption(100.0, 1.0),
+                             1 << 15, 513), 16)
+    assert e.value.status == _abi.ERR_UNSUPPORTED

@@ -9,7 +9,8 @@
 //   * strips: a warp stages 32 paths' records in shared memory and each lane
 //     owns one strike of a 32-strike chunk (gridDim.y chunks), so the payoff
 //     work is one evaluation per (path, strike) with no per-strike reduction.
-// finalize_kernel sums the tile partials in a fixed order (deterministic) and
+// finalize_kernel sums the tile partials, a warp per (strike, quantity), in a fixed order
+// (deterministic) and
 // applies compute_stats (MonteCarloPricer.hpp:448-457).
 #include "engine_types.h"
 #include "device_numerics.cuh"
@@ -206,20 +207,27 @@ __global__ void __launch_bounds__(kPayoffBlock, SPEC == 1 ? 8 : 0) payoff_reduce
   }
 }
 
-// One thread per (strike, quantity): fixed-order FP64 sum over tiles, then
-// mean * df and sqrt((E[x^2] - E[x]^2) / M) * df (MonteCarloPricer.hpp:448-457).
-__global__ void finalize_kernel(const FinalizeParams P) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= P.n_strikes * kQ) return;
-  const int k = idx / kQ, q = idx % kQ;
+// One warp per (strike, quantity): lane l sums tiles l, l + 32, ... in order, a fixed
+// shuffle tree adds the lanes (deterministic for a given tile count), then mean * df and
+// sqrt((E[x^2] - E[x]^2) / M) * df (MonteCarloPricer.hpp:448-457).
+constexpr int kFinalizeBlock = 256;
+__global__ void __launch_bounds__(kFinalizeBlock) finalize_kernel(const FinalizeParams P) {
+  const int w = (int)((blockIdx.x * kFinalizeBlock + threadIdx.x) >> 5), lane = (int)(threadIdx.x & 31u);
+  if (w >= P.n_strikes * kQ) return;  // whole warps
+  const int k = w / kQ, q = w % kQ;
   double s = 0.0, ss = 0.0;
   if ((P.active_mask >> q) & 1) {
-    for (unsigned long long t = 0; t < P.n_tiles; ++t) {
+    for (unsigned long long t = (unsigned long long)lane; t < P.n_tiles; t += 32) {
       const double *src = P.partials + (t * (unsigned long long)P.n_strikes + k) * (2 * kQ);
       s += src[2 * q];
       ss += src[2 * q + 1];
     }
+    for (int o = 16; o > 0; o >>= 1) {
+      s += __shfl_xor_sync(0xffffffffu, s, o);
+      ss += __shfl_xor_sync(0xffffffffu, ss, o);
+    }
   }
+  if (lane != 0) return;
   const double mean = s * P.inv_m;
   double var = ss * P.inv_m - mean * mean;
   if (var < 0.0) var = 0.0;
@@ -240,8 +248,9 @@ cudaError_t launch_payoff(const PayoffParams &P, unsigned long long n_tiles, cud
 }
 
 cudaError_t launch_finalize(const FinalizeParams &P, cudaStream_t stream) {
-  const int n = P.n_strikes * kQ;
-  dev::finalize_kernel<<<(n + 127) / 128, 128, 0, stream>>>(P);
+  const long long threads = (long long)P.n_strikes * kQ * 32;
+  dev::finalize_kernel<<<(unsigned int)((threads + dev::kFinalizeBlock - 1) / dev::kFinalizeBlock),
+                         dev::kFinalizeBlock, 0, stream>>>(P);
   return cudaGetLastError();
 }
 

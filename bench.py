@@ -758,9 +758,10 @@ def time_to_se(eng, m, kind: str, target: float, probe_paths: int = 1 << 22, top
 
     # the same network on randomized QMC paths: sized like qmc_time_to_se from its own probe
     R, quantum = 16, 16 * 2048
-    qprobe = eng.cv_qmc_price(cv_jobs(m, kind, 1 << 20, seed=44)[0], cfg, R)
-    n_cvq = max(-(-int((1 << 20) * (qprobe.price_std_err / (0.85 * target * qprobe.price)) ** 2) // quantum) * quantum,
-                quantum)
+    qps = [eng.cv_qmc_price(cv_jobs(m, kind, 1 << 20, seed=44 + 1000 * i)[0], cfg, R) for i in range(4)]
+    q_se = float(np.sqrt(np.mean([r.price_std_err ** 2 for r in qps])))  # 64 replicates in all
+    q_price = float(np.mean([r.price for r in qps]))
+    n_cvq = max(-(-int((1 << 20) * (q_se / (0.85 * target * q_price)) ** 2) // quantum) * quantum, quantum)
     cvq_last = {"sim_ms": 0.0, "mlp_ms": 0.0, "price_ms": 0.0}
 
     def run_cvq():
@@ -856,14 +857,17 @@ def qmc_time_to_se(eng, m, kind: str = "european", target: float = 1e-4, R: int 
     Bates arithmetic Asian, SchemeNCI factors and Merton jumps, 256 steps) priced by randomized
     quasi-Monte Carlo (Sobol + Brownian bridge for the normals, Sobol uniforms for the NCI and jump
     draws, R digital shifts): wall time to the relative standard error target against plain GPU
-    Monte Carlo.  An untimed probe fixes the QMC error at one size.  The timed run prices the
-    point count that the plain 1/sqrt(n) rate gives for 0.85 x the target (a margin on the
-    R-replicate error estimate, itself noisy), in whole 2048-point blocks per replicate; while the
-    pooled error is still above the target it prices the shortfall on fresh seeds and pools the
-    runs (at most `top_ups` times), every run inside the timed region."""
+    Monte Carlo.  An untimed probe (4 shift sets of R replicates) fixes the QMC error at one size.
+    The timed run prices the point count that the plain 1/sqrt(n) rate gives for 0.85 x the target
+    (a margin on the run's own R-replicate error estimate, itself noisy), in whole 2048-point
+    blocks per replicate; while the pooled error is still above the target it prices the
+    shortfall on fresh seeds and pools the runs (at most `top_ups` times), every run inside the
+    timed region."""
     import torch
-    job, steps = cv_jobs(m, kind, probe_paths)
-    q, _ = eng.qmc_price(job, R)
+    # the error at the probe size from 4 independent shift sets (64 replicates in all): one
+    # 16-replicate estimate carries about 18 % noise and mis-sizes the timed run
+    probes = [eng.qmc_price(cv_jobs(m, kind, probe_paths, seed=700 + i)[0], R)[0] for i in range(4)]
+    q = np.array([[np.mean([p[0, 0] for p in probes])], [np.sqrt(np.mean([p[1, 0] ** 2 for p in probes]))]])
     quantum = R * 2048
 
     def size(n):  # whole 2048-point blocks per replicate

@@ -24,6 +24,7 @@ REBATE_NONE, REBATE_AT_HIT, REBATE_AT_MATURITY = range(3)
 Q_NAMES = ("price", "delta", "gamma", "vega0", "vega1", "theta", "rho", "vanna0", "vanna1", "charm")
 Q_COUNT = len(Q_NAMES)
 MLMC_MAX_LEVELS = 24
+QMC_DEFAULT_DIRECTION_SEED = 6  # MYQL_QMC_DEFAULT_DIRECTION_SEED
 
 
 class HestonParamsC(C.Structure):
@@ -122,6 +123,7 @@ _SIGS = {
     "myql_ctx_set_records_limit": (C.c_int, [C.c_void_p, C.c_uint64]),
     "myql_ctx_set_nci_slopes": (C.c_int, [C.c_void_p, C.c_int]),
     "myql_ctx_set_nci_rows": (C.c_int, [C.c_void_p, C.c_int]),
+    "myql_ctx_set_qmc_direction_seed": (C.c_int, [C.c_void_p, C.c_uint64]),
     "myql_ctx_set_batch_shape": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "myql_batch_last_plan": (C.c_int, [C.c_void_p, C.POINTER(BatchClassPlanC), C.c_size_t,
                                        C.POINTER(C.c_size_t)]),

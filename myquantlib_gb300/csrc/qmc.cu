@@ -256,10 +256,24 @@ Bridge segmented_bridge(int n) {
 struct QmcState : ExtState {
   DevBuf dirs, shift, bridge;
   unsigned int dirs_D = 0;
+  uint64_t dirs_seed = kQmcDirectionSeed;  // the point set in use
+  uint64_t want_seed = kQmcDirectionSeed;  // the point set asked for
   int bridge_n = -1;
 };
 
+QmcState &qmc_state(CtxBase *ctx) {
+  if (!ctx->qmc) ctx->qmc.reset(new QmcState);
+  return *static_cast<QmcState *>(ctx->qmc.get());
+}
+
 }  // namespace
+
+extern "C" myql_status myql_ctx_set_qmc_direction_seed(myql_ctx *ctx_, uint64_t seed) {
+  CtxBase *ctx = reinterpret_cast<CtxBase *>(ctx_);
+  if (!ctx) return set_error(MYQL_ERR_INVALID_ARG, "null context");
+  qmc_state(ctx).want_seed = seed;
+  return MYQL_OK;
+}
 
 extern "C" myql_status myql_qmc_directions(uint32_t D, uint64_t seed, uint32_t *out) {
   if (!out || D == 0 || D > 1u << 16) return set_error(MYQL_ERR_INVALID_ARG, "need 1 <= D <= 65536 and an output");
@@ -289,18 +303,18 @@ myql_status qmc_prepare(CtxBase *ctx, const myql_mc_job &job, const Plan &pl, ui
                                            "of 2048 x replicates");
   if (M / R > (1ull << 32)) return set_error(MYQL_ERR_TOO_LARGE, "at most 2^32 points per replicate");
   if (pl.steps > kQmcMaxSteps) return set_error(MYQL_ERR_UNSUPPORTED, "quasi-Monte Carlo takes at most 512 steps");
-  if (!ctx->qmc) ctx->qmc.reset(new QmcState);
-  QmcState &S = *static_cast<QmcState *>(ctx->qmc.get());
+  QmcState &S = qmc_state(ctx);
   const int NG = 1 + n_nv, NU = 2 * n_nci + (job.model.jump == MYQL_JUMP_MERTON ? 2 : 0);
   const unsigned int D = (unsigned int)pl.steps * (unsigned int)(NG + NU);
   const uint64_t seed = job.config.seed;
   cudaStream_t st = ctx->stream;
   cudaError_t e = cudaSuccess;
   // tables: direction numbers, shifts, bridge
-  // one point set per dimension count (direction numbers from kQmcDirectionSeed); the
-  // job's seed draws the digital shifts, which alone make the replicates independent
-  if (S.dirs_D != D) {
-    const std::vector<uint32_t> V = sobol_directions(D, kQmcDirectionSeed);
+  // one point set per dimension count and direction seed (the context's, by default
+  // kQmcDirectionSeed); the job's seed draws the digital shifts, which alone make the
+  // replicates independent
+  if (S.dirs_D != D || S.dirs_seed != S.want_seed) {
+    const std::vector<uint32_t> V = sobol_directions(D, S.want_seed);
     if ((size_t)D * kQmcBits > V.size() || V[(size_t)(D - 1) * kQmcBits] == 0u)
       return set_error(MYQL_ERR_TOO_LARGE, "too many quasi-Monte Carlo dimensions");
     std::vector<uint32_t> Vt(V.size());  // bit-major on the device: a warp's dimensions are contiguous
@@ -310,6 +324,7 @@ myql_status qmc_prepare(CtxBase *ctx, const myql_mc_job &job, const Plan &pl, ui
     if (e == cudaSuccess) e = cudaMemcpy(S.dirs.p, Vt.data(), Vt.size() * 4, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_status(e, "Sobol directions");
     S.dirs_D = D;
+    S.dirs_seed = S.want_seed;
   }
   std::vector<uint32_t> sh((size_t)R * D);
   uint64_t ss = seed ^ 0x8BB84B93962EACC9ull;

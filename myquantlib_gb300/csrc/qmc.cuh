@@ -10,7 +10,7 @@ namespace myql {
 constexpr int kQmcMaxSteps = 512;
 constexpr int kQmcBits = 32;
 constexpr int kQmcSeg = 32;  // steps per bridge segment
-constexpr uint64_t kQmcDirectionSeed = 0;  // initial direction numbers of the pricers' point sets
+constexpr uint64_t kQmcDirectionSeed = MYQL_QMC_DEFAULT_DIRECTION_SEED;  // the default point set
 
 struct QmcParams {
   SimParams P;                 // plan constants (records, trackers, scenario 0)

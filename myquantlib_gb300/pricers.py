@@ -531,6 +531,11 @@ class Engine:
         _abi.check(self.lib.myql_mlmc_price(self.handle, C.byref(job.c), C.byref(mlmc_cfg), C.byref(res)))
         return res
 
+    def set_qmc_direction_seed(self, seed: int):
+        """The Sobol point set of this context's randomized QMC: the seed of its initial
+        direction numbers (the job's seed draws the digital shifts)."""
+        _abi.check(self.lib.myql_ctx_set_qmc_direction_seed(self.handle, int(seed)))
+
     def qmc_price(self, job: "_Job", n_replicates: int = 16):
         """Randomized quasi-Monte Carlo price rows (myql_qmc_price) and the run statistics."""
         out = np.zeros(2 * _abi.Q_COUNT * job.n_strikes, dtype=np.float64)

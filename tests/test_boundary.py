@@ -149,3 +149,10 @@ def test_result_unpacking_shapes():
     assert np.array_equal(r.vega[1], raw[8]) and np.array_equal(r.charm_std_err, raw[19])
     r1 = m.result_from_raw(raw[:, :1], m.GreekMode.NONE, False)
     assert r1.price == 0.0 and r1.delta is None
+
+
+def test_header_constants_match_the_python_mirror():
+    """The #define constants of include/myql_gpu.h that the Python mirror repeats."""
+    text = (Path(__file__).resolve().parents[1] / "include" / "myql_gpu.h").read_text()
+    seed = re.search(r"#define MYQL_QMC_DEFAULT_DIRECTION_SEED (\d+)", text)
+    assert seed and int(seed.group(1)) == _abi.QMC_DEFAULT_DIRECTION_SEED

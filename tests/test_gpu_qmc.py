@@ -121,3 +121,24 @@ def test_qmc_refuses_more_than_512_steps(engine):
         engine.qmc_price(job(m.HestonModel(H1), m.HestonStepper(m.SchemeNV), m.EuropeanOption(100.0, 1.0),
                              1 << 15, 513), 16)
     assert e.value.status == _abi.ERR_UNSUPPORTED
+
+
+def test_qmc_direction_seed_selects_the_point_set(engine):
+    """Another direction seed gives another randomly initialised Sobol point set: a different
+    but still unbiased estimate; going back to a seed reproduces its estimate bit for bit."""
+    model, stepper, instr, steps = CASES["heston_call"]
+    j = lambda: job(model, stepper, instr(), 1 << 18, steps)  # noqa: E731
+    p, _ = engine.price(job(model, stepper, instr(), 1 << 22, steps, seed=11))
+    try:
+        engine.set_qmc_direction_seed(1)
+        a, _ = engine.qmc_price(j(), 16)
+        engine.set_qmc_direction_seed(2)
+        b, _ = engine.qmc_price(j(), 16)
+        engine.set_qmc_direction_seed(1)
+        c, _ = engine.qmc_price(j(), 16)
+    finally:
+        engine.set_qmc_direction_seed(_abi.QMC_DEFAULT_DIRECTION_SEED)
+    np.testing.assert_array_equal(a, c)
+    assert not np.array_equal(a[0], b[0])
+    for q in (a, b):
+        assert np.all(np.abs(q[0] - p[0]) < 4.0 * np.hypot(q[1], p[1])), (q[0], p[0])

@@ -710,13 +710,14 @@ def _pool(parts):
 def time_to_se(eng, m, kind: str, target: float, probe_paths: int = 1 << 22, top_ups: int = 4) -> dict:
     """Wall time until the relative standard error reaches `target`: plain GPU Monte Carlo
     against the neural control variate, each through the public API.  Untimed probes fix each
-    estimator's variance (the plain engine at probe_paths; a control variate trained once on
-    other pilot paths).  In the timed region each arm prices the path count its probe gives
+    estimator's variance (the plain engine at probe_paths; the control variate trained, untimed,
+    on the very pilot paths its timed arm trains on again, which gives the same network bit for
+    bit).  In the timed region each arm prices the path count its probe gives
     for the target and, while its estimated relative error is still above the target, prices
     more paths on fresh seeds and pools them (at most `top_ups` times).  The control
     variate's timed region includes its own pilot simulation and training.  A third arm runs
     the same control variate on randomized QMC paths (myql_cv_qmc_price, 16 digital shifts),
-    sized in whole 2048-point blocks per replicate from its own untimed probe."""
+    sized by _qmc_size from its own untimed probe."""
     import torch
     job, steps = cv_jobs(m, kind, probe_paths)
     torch.cuda.synchronize()
@@ -727,7 +728,7 @@ def time_to_se(eng, m, kind: str, target: float, probe_paths: int = 1 << 22, top
     n_plain = int(probe_paths * (se / (target * price)) ** 2) + 1
     # the training budget follows the plain estimator's expected time to the target
     cfg = cv_config(m, kind, plain_seconds=t_probe * n_plain / probe_paths)
-    eng.cv_train(cv_jobs(m, kind, 1 << 16)[0], cfg)
+    eng.cv_train(cv_jobs(m, kind, 1 << 16, seed=45)[0], cfg)  # the CV arm's network
     probe = eng.cv_price(cv_jobs(m, kind, probe_paths, seed=43)[0], cfg)
     n_cv = max(int(probe_paths * (probe.price_std_err / (target * probe.price)) ** 2) + 1, 128)
 
@@ -758,10 +759,12 @@ def time_to_se(eng, m, kind: str, target: float, probe_paths: int = 1 << 22, top
 
     # the same network on randomized QMC paths: sized like qmc_time_to_se from its own probe
     R, quantum = 16, 16 * 2048
-    qps = [eng.cv_qmc_price(cv_jobs(m, kind, 1 << 20, seed=44 + 1000 * i)[0], cfg, R) for i in range(4)]
-    q_se = float(np.sqrt(np.mean([r.price_std_err ** 2 for r in qps])))  # 64 replicates in all
-    q_price = float(np.mean([r.price for r in qps]))
-    n_cvq = max(-(-int((1 << 20) * (q_se / (0.85 * target * q_price)) ** 2) // quantum) * quantum, quantum)
+    eng.cv_train(cv_jobs(m, kind, 1 << 16, seed=46)[0], cfg)  # the QMC arm's network
+    def cvq_probe(n, i):
+        r = eng.cv_qmc_price(cv_jobs(m, kind, n, seed=44 + 1000 * i)[0], cfg, R)
+        return r.price, r.price_std_err
+
+    n_cvq, cvq_decay = _qmc_size(cvq_probe, target, quantum)
     cvq_last = {"sim_ms": 0.0, "mlp_ms": 0.0, "price_ms": 0.0}
 
     def run_cvq():
@@ -812,6 +815,7 @@ def time_to_se(eng, m, kind: str, target: float, probe_paths: int = 1 << 22, top
             # the control variate on randomized QMC paths (R = 16 digital shifts), pilot and
             # training inside its timed region as above
             "cv_qmc": {"s": t_cvq, "speedup": t_plain / t_cvq, "points": q_n, "runs": q_runs,
+                       "probe_decay_exponent": cvq_decay,
                        "rel_se": q_err / q_mean, "price": q_mean, "replicate_variance_ratio": cvq_last.get("vr"),
                        "breakdown_s": {"pilot_and_training": trq.total_ms / 1e3,
                                        "price_simulate": cvq_last["sim_ms"] / 1e3,
@@ -851,29 +855,44 @@ def _pool_qmc(parts):
     return mean, float(np.sqrt(sum((p * se) ** 2 for _, se, p in parts))) / n, n
 
 
+def _qmc_size(run, target: float, quantum: int, n1: int = 1 << 19, n2: int = 1 << 21, shifts: int = 4):
+    """Points for a randomized-QMC run to reach the relative standard error `target`, from an
+    untimed probe: the error at two sizes, each from `shifts` shift sets of replicates
+    (run(n, i) -> (price, standard error)), its decay n^-a with a fitted from the two and clamped
+    to [0.5, 0.75] (1/sqrt(n) is plain Monte Carlo's rate; QMC decays faster), and a 0.85 margin
+    on the run's own noisy error estimate; in whole quanta.  Returns (points, a)."""
+    def err(n):
+        rs = [run(n, i) for i in range(shifts)]
+        return float(np.mean([p for p, _ in rs])), float(np.sqrt(np.mean([e * e for _, e in rs])))
+    _, e1 = err(n1)
+    p2, e2 = err(n2)
+    a = float(min(max(np.log(e1 / e2) / np.log(n2 / n1), 0.5), 0.75))
+    need = n2 * (e2 / (0.85 * target * p2)) ** (1.0 / a)
+    return max(-(-int(need) // quantum) * quantum, quantum), a
+
+
 def qmc_time_to_se(eng, m, kind: str = "european", target: float = 1e-4, R: int = 16,
-                   probe_paths: int = 1 << 20, top_ups: int = 4) -> dict:
+                   top_ups: int = 4) -> dict:
     """A control-variate workload (the Heston European call, SchemeNV, 100 steps, or the Double
     Bates arithmetic Asian, SchemeNCI factors and Merton jumps, 256 steps) priced by randomized
     quasi-Monte Carlo (Sobol + Brownian bridge for the normals, Sobol uniforms for the NCI and jump
     draws, R digital shifts): wall time to the relative standard error target against plain GPU
-    Monte Carlo.  An untimed probe (4 shift sets of R replicates) fixes the QMC error at one size.
-    The timed run prices the point count that the plain 1/sqrt(n) rate gives for 0.85 x the target
-    (a margin on the run's own R-replicate error estimate, itself noisy), in whole 2048-point
-    blocks per replicate; while the pooled error is still above the target it prices the
-    shortfall on fresh seeds and pools the runs (at most `top_ups` times), every run inside the
-    timed region."""
+    Monte Carlo.  An untimed probe (_qmc_size: the error at 2^19 and 2^21 points, 4 shift sets of
+    R replicates each, and its fitted decay) sizes the timed run for 0.85 x the target, in whole
+    2048-point blocks per replicate; while the pooled error is still above the target it prices
+    the shortfall on fresh seeds and pools the runs (at most `top_ups` times), every run inside
+    the timed region."""
     import torch
-    # the error at the probe size from 4 independent shift sets (64 replicates in all): one
-    # 16-replicate estimate carries about 18 % noise and mis-sizes the timed run
-    probes = [eng.qmc_price(cv_jobs(m, kind, probe_paths, seed=700 + i)[0], R)[0] for i in range(4)]
-    q = np.array([[np.mean([p[0, 0] for p in probes])], [np.sqrt(np.mean([p[1, 0] ** 2 for p in probes]))]])
     quantum = R * 2048
 
     def size(n):  # whole 2048-point blocks per replicate
         return max(-(-int(n) // quantum) * quantum, quantum)
 
-    n_q = size(probe_paths * (q[1, 0] / (0.85 * target * q[0, 0])) ** 2)
+    def probe(n, i):
+        q, _ = eng.qmc_price(cv_jobs(m, kind, n, seed=700 + i)[0], R)
+        return q[0, 0], q[1, 0]
+
+    n_q, decay = _qmc_size(probe, target, quantum)
     pj, _ = cv_jobs(m, kind, 1 << 22)
     raw, _ = eng.price(pj)
     n_plain = int((1 << 22) * (raw[1, 0] / (target * raw[0, 0])) ** 2) + 1
@@ -895,6 +914,7 @@ def qmc_time_to_se(eng, m, kind: str = "european", target: float = 1e-4, R: int 
     return {"instrument": ("Heston European call (SchemeNV, 100 steps)" if kind == "european" else
                            "Double Bates arithmetic Asian call (SchemeNCI factors, Merton jumps, 256 steps)"),
             "target_rel_se": target, "replicates": R, "qmc_paths": tot, "qmc_runs": runs, "qmc_s": t_q,
+            "probe_decay_exponent": decay,
             "qmc_rel_se": err / mean, "plain_paths": n_plain,
             "plain_s": t_plain, "plain_rel_se": raw[1, 0] / raw[0, 0], "speedup": t_plain / t_q,
             "price_qmc": mean, "price_plain": raw[0, 0]}

@@ -616,16 +616,22 @@ def run_batch(args) -> dict:
     if int(os.environ.get("RANK", "0")) != 0:
         return {}
     eng = m.Engine(0)
-    rq = workloads.uneven_requests(args.batch_jobs)
+    nci = args.batch_scheme == "nci"
+    if nci:  # one table per distinct d, each capped at batch_nci_rows rows (resident together)
+        eng.set_nci_rows(args.batch_nci_rows)
+    rq = workloads.uneven_requests(args.batch_jobs, scheme=m.SchemeNCI if nci else m.SchemeExact)
     jobs = [m.make_job(r.model, m.stepper_for(r.model, r.instrument, r.scheme), r.instrument, r.mode, r.cfg,
                        r.S0, r.r, r.q) for r in rq]
     total = workloads.path_steps(rq)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda:0")
     launches = 0
-    for _ in range(max(args.warmup, 1)):
+    t_first = time.perf_counter()
+    for w in range(max(args.warmup, 1)):
         _, st = eng.price_batch(jobs)
         launches = st.kernel_launches
-    dev_ms, wall = [], []
+        if w == 0:
+            t_first = time.perf_counter() - t_first  # the first batch: tables, tuning, graph
+    dev_ms, wall, fallbacks = [], [], []
     with ClockSampler(0) as clk:
         for _ in range(args.steps):
             flush.zero_()
@@ -634,6 +640,7 @@ def run_batch(args) -> dict:
             _, st = eng.price_batch(jobs)
             wall.append(time.perf_counter() - t0)
             dev_ms.append(st.device_ms)
+            fallbacks.append(int(st.table_fallbacks))
     value = total * args.steps / (sum(dev_ms) / 1e3)
     e2e = total * args.steps / sum(wall)
     line = {"metric": "paths*steps/s", "value": value, "unit": "paths*steps/s", "n_gpus": 1,
@@ -641,19 +648,24 @@ def run_batch(args) -> dict:
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": {"workload": f"{len(jobs)} uneven requests (Heston / Bates-Kou / Double Heston, "
-                                   "arithmetic Asian or up-and-out call, SchemeExact) in one persistent launch",
+                                   f"arithmetic Asian or up-and-out call, {'SchemeNCI' if nci else 'SchemeExact'}) "
+                                   "in one persistent launch",
                        "jobs": len(jobs), "path_steps_per_step": total, "l2": "flushed between steps"},
+            "first_batch_s": t_first,
             "e2e": {"value": e2e, "unit": "paths*steps/s", "h2d_bytes_per_step": None,
                     "d2h_bytes_per_step": 8 * 20 * len(jobs)},
             "gpu_launches": launches * args.steps, "clocks": clk.summary(),
             # per kernel class: the launch shape the batch autotuner picked and its timings
             "tuner": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in p.items()}
                       for p in eng.batch_plan()]}
+    if nci:
+        line["config"]["nci_rows_cap"] = args.batch_nci_rows
+        line["nci_table_fallbacks_per_step"] = statistics.median(fallbacks)
     if not args.no_cpu:
         from oracle import oracle
         oracle.build(ref=False)
         cores = os.cpu_count() or 1
-        n_s = 32
+        n_s = 8 if nci else 32  # the port builds each NCI job's FP64 table, as the reference does
         t0 = time.perf_counter()
         for j in jobs[:n_s]:
             oracle.mc_price(j, oracle.LAYOUT_REFERENCE, cores, fast=True)
@@ -1082,6 +1094,12 @@ def main():
                          "with and without the control variate; c1: plain Heston NV European (configuration 1); "
                          "qmc: randomized QMC (profiling case only, with --ncu-case)")
     ap.add_argument("--batch-jobs", type=int, default=4096)
+    ap.add_argument("--batch-scheme", choices=["nci", "exact"], default="nci",
+                    help="CIR scheme of the batched requests: nci, the dispatcher's default scheme, with "
+                         "capped tables (the default), or exact")
+    ap.add_argument("--batch-nci-rows", type=int, default=64,
+                    help="row cap of each SchemeNCI table under --batch-scheme nci (Poisson counts beyond "
+                         "it take the Wilson-Hilferty quantile, dof >= 2 x cap)")
     ap.add_argument("--ncu-case", action="store_true",
                     help="profiling case: one maturity (T=1), 2^18 paths, two requests, no timing")
     ap.add_argument("--ncu-full", action="store_true",

@@ -1042,15 +1042,18 @@ def run_ncu_cv_case() -> None:
     eng.cv_price(cv_jobs(m, "asian", 1 << 18)[0], cfg)
 
 
-def run_ncu_batch_case() -> None:
+def run_ncu_batch_case(scheme: str = "nci") -> None:
     """A small batched case for ncu: the first 256 uneven requests at up to 2^16 paths, priced twice,
     on the default launch shape (the one the autotuner keeps on the full batch), so that the first
-    batch_kernel launch is a class kernel of the batch graph rather than a tuning candidate."""
+    batch_kernel launch is a class kernel of the batch graph rather than a tuning candidate.  The
+    scheme is the batch bench's (SchemeNCI with 64-row tables, or SchemeExact)."""
     import myquantlib_gb300 as m
     from myquantlib_gb300 import workloads
     eng = m.Engine(0)
     eng.set_batch_shape(128, 1, 0)
-    rq = workloads.uneven_requests(256, max_log2_paths=16.0)
+    if scheme == "nci":
+        eng.set_nci_rows(64)
+    rq = workloads.uneven_requests(256, max_log2_paths=16.0, scheme=m.SchemeNCI if scheme == "nci" else m.SchemeExact)
     jobs = [m.make_job(r.model, m.stepper_for(r.model, r.instrument, r.scheme), r.instrument, r.mode, r.cfg,
                        r.S0, r.r, r.q) for r in rq]
     for _ in range(2):
@@ -1110,7 +1113,7 @@ def main():
         if args.workload == "cv":
             run_ncu_cv_case()
         elif args.workload == "batch":
-            run_ncu_batch_case()
+            run_ncu_batch_case(args.batch_scheme)
         elif args.workload == "c1":
             run_ncu_c1_case()
         elif args.workload == "mlmc":

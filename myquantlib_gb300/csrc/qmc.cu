@@ -95,6 +95,24 @@ __global__ void __launch_bounds__(kSimBlock) qmc_cv_kernel(const __grid_constant
 
 }  // namespace dev
 
+namespace dev {
+// out[i] = high word of splitmix64 value i + 1 of the sequence started at s0 (the host's
+// splitmix(s) called i + 1 times): z = s0 + (i + 1) * golden, then the finaliser
+__global__ void qmc_shift_kernel(unsigned long long s0, unsigned long long n, uint32_t *out) {
+  const unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  unsigned long long z = s0 + (i + 1ull) * 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  out[i] = (uint32_t)((z ^ (z >> 31)) >> 32);
+}
+}  // namespace dev
+
+static cudaError_t launch_qmc_shifts(unsigned long long s0, unsigned long long n, uint32_t *out, cudaStream_t st) {
+  dev::qmc_shift_kernel<<<(unsigned int)((n + 255) / 256), 256, 0, st>>>(s0, n, out);
+  return cudaGetLastError();
+}
+
 static cudaError_t launch_qmc(const QmcParams &Q, int nf, bool pd, cudaStream_t st) {
   const unsigned int grid = (unsigned int)((Q.P.path_end + kSimBlock - 1) / kSimBlock);
   switch (nf * 2 + (pd ? 1 : 0)) {
@@ -326,13 +344,13 @@ myql_status qmc_prepare(CtxBase *ctx, const myql_mc_job &job, const Plan &pl, ui
     S.dirs_D = D;
     S.dirs_seed = S.want_seed;
   }
-  std::vector<uint32_t> sh((size_t)R * D);
-  uint64_t ss = seed ^ 0x8BB84B93962EACC9ull;
-  for (auto &x : sh) x = (uint32_t)(splitmix(ss) >> 32);
-  e = S.shift.ensure(sh.size() * 4);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(S.shift.p, sh.data(), sh.size() * 4, cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // sh is a host temporary
+  // the digital shifts: the high words of the splitmix64 sequence from seed ^ constant, drawn on
+  // the device (value i of the counter-based sequence directly)
+  const uint64_t n_shift = R * (uint64_t)D;
+  e = S.shift.ensure(n_shift * 4);
+  if (e == cudaSuccess) e = launch_qmc_shifts(seed ^ 0x8BB84B93962EACC9ull, n_shift, (uint32_t *)S.shift.p, st);
   if (e != cudaSuccess) return cuda_status(e, "digital shifts");
+  ctx->launches++;
   const int n = pl.steps;
   if (S.bridge_n != n) {
     const Bridge B = segmented_bridge(n);

@@ -426,9 +426,15 @@ def fourier_seeds(eng, m, seeds, nci_slopes: int) -> dict:
     finally:
         eng.set_nci_slopes(0)
     Z = np.stack(zs)                                     # (seed, maturity, quantity, strike)
-    per = np.nanmean(Z, axis=3)                          # strike-averaged signed z per seed
-    mean = np.nanmean(per, axis=0)                       # (maturity, quantity)
-    sem = np.nanstd(per, axis=0, ddof=1) / np.sqrt(len(seeds))
+    # quantities without a Fourier value (the second factor's) are all NaN: left out
+    has = np.isfinite(Z).any(axis=3)                     # (seed, maturity, quantity)
+    per = np.full(Z.shape[:3], np.nan)
+    per[has] = np.nanmean(Z[has], axis=-1)               # strike-averaged signed z per seed
+    mean = np.full(Z.shape[1:3], np.nan)
+    sem = np.zeros(Z.shape[1:3])
+    cols = has.all(axis=0)                               # (maturity, quantity) on every seed
+    mean[cols] = per[:, cols].mean(axis=0)
+    sem[cols] = per[:, cols].std(axis=0, ddof=1) / np.sqrt(len(seeds))
     t = np.where(sem > 0, mean / np.where(sem > 0, sem, 1.0), 0.0)
     names = m._abi.Q_NAMES
     cells = {}

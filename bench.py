@@ -434,7 +434,8 @@ def fourier_seeds(eng, m, seeds, nci_slopes: int) -> dict:
     sem = np.zeros(Z.shape[1:3])
     cols = has.all(axis=0)                               # (maturity, quantity) on every seed
     mean[cols] = per[:, cols].mean(axis=0)
-    sem[cols] = per[:, cols].std(axis=0, ddof=1) / np.sqrt(len(seeds))
+    if len(seeds) > 1:  # one seed has no spread: t stays 0
+        sem[cols] = per[:, cols].std(axis=0, ddof=1) / np.sqrt(len(seeds))
     t = np.where(sem > 0, mean / np.where(sem > 0, sem, 1.0), 0.0)
     names = m._abi.Q_NAMES
     cells = {}

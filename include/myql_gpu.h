@@ -228,6 +228,18 @@ myql_status myql_ctx_set_nci_slopes(myql_ctx *ctx, int mode);
  * the cube is within 6e-6 relative of the exact quantile. */
 myql_status myql_ctx_set_nci_rows(myql_ctx *ctx, int max_rows);
 
+/* Theta and charm of one-factor SchemeNCI Europeans (on, 1; off, 0, the
+ * default).  They difference the scenarios at maturity T +- t_bump, whose
+ * per-step constants differ by about 2 t_bump / T relative; FP32 constants
+ * carry that difference with a systematic relative error of 1e-4 to 1e-2,
+ * which every path shares (the reference's FP64 constants carry it to about
+ * 1e-11).  On, those two scenarios add each constant's FP32 rounding error back
+ * as a second FP32 term (Poisson mean, table scale, drift, diffusion and jump
+ * compensation), a few more FP32 operations per step for those two scenarios.
+ * Their records then differ from requests that price T +- t_bump alone in the
+ * last bits (and, rarely, by a Poisson count). */
+myql_status myql_ctx_set_precise_theta(myql_ctx *ctx, int on);
+
 /* Host-side validation of a job, without a device: the checks myql_mc_price
  * runs before any launch (MYQL_ERR_NV_CONDITION for SchemeNV with
  * sigma^2 > 4 kappa theta, as VolSchemes.hpp:40-41 throws). */

@@ -123,6 +123,7 @@ _SIGS = {
     "myql_ctx_set_records_limit": (C.c_int, [C.c_void_p, C.c_uint64]),
     "myql_ctx_set_nci_slopes": (C.c_int, [C.c_void_p, C.c_int]),
     "myql_ctx_set_nci_rows": (C.c_int, [C.c_void_p, C.c_int]),
+    "myql_ctx_set_precise_theta": (C.c_int, [C.c_void_p, C.c_int]),
     "myql_ctx_set_qmc_direction_seed": (C.c_int, [C.c_void_p, C.c_uint64]),
     "myql_ctx_set_batch_shape": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "myql_batch_last_plan": (C.c_int, [C.c_void_p, C.POINTER(BatchClassPlanC), C.c_size_t,

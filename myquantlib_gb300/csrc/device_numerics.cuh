@@ -545,6 +545,28 @@ __device__ __forceinline__ int poisson_small(float mean, float exp_neg_mean, Xo 
   return poisson_small_u(mean, exp_neg_mean, u01_bits(draw(rng)), cap, caphits);
 }
 
+// poisson_small_u in FP64 on the draw's FP64 uniform x 2^-64 (the reference's
+// uniform_01<double> and sequential inversion, JumpPolicies.hpp:55-75): for a
+// count whose probabilities must keep differences far below FP32 resolution.
+// Out of line: it runs once per path, and inline its FP64 registers would raise the
+// path kernel's register count.  Returns (count, 1 if the loop cap was hit).
+static __device__ __noinline__ int2 poisson_small_fp64(double mean, unsigned long long x, unsigned int cap) {
+  double u = (double)x * 5.421010862427522e-20;  // 2^-64
+  double p = exp(-mean);
+  int k = 0, hit = 0;
+  while (u > p) {
+    if ((unsigned int)k >= cap) {
+      hit = 1;
+      break;
+    }
+    if (p < 1.0e-18 && (double)k > mean) break;
+    u -= p;
+    ++k;
+    p = mean * p / (double)k;
+  }
+  return make_int2(k, hit);
+}
+
 // Exponential(rate) draw: -log(1 - U) / rate from one uniform.
 __device__ __forceinline__ float exp_draw(Xo &rng, float inv_rate) {
   return -__logf(u01c_bits(draw(rng))) * inv_rate;

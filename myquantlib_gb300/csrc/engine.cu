@@ -208,16 +208,27 @@ struct ScDef {
   double dt, T, r;
 };
 
+// x - (double)(float)x, rounded to FP32: what FP32 drops of x
+static float fp32_lo(double x) { return (float)(x - (double)(float)x); }
+
 void fill_factor(FactorConst &fc, const myql_heston_params &h, double v0, int scheme,
-                        double r_part, double dt) {
+                        double r_part, double dt, float *lo) {
   const double k = h.kappa, th = h.theta, s = h.sigma, rho = h.rho;
   fc.v0 = (float)v0;
   // log-S coefficients (ASVJstepper.hpp:276-280)
   const double term = (k * rho / s - 0.5) * dt * 0.5;
-  fc.C0 = (float)((r_part - rho * k * th / s) * dt);
-  fc.C1 = (float)(term - rho / s);
-  fc.C2 = (float)(term + rho / s);
-  fc.C3 = (float)(dt * (1.0 - rho * rho) * 0.5);
+  const double c0 = (r_part - rho * k * th / s) * dt, c1 = term - rho / s, c2 = term + rho / s,
+               c3 = dt * (1.0 - rho * rho) * 0.5;
+  fc.C0 = (float)c0;
+  fc.C1 = (float)c1;
+  fc.C2 = (float)c2;
+  fc.C3 = (float)c3;
+  if (lo) {
+    lo[0] = fp32_lo(c0);
+    lo[1] = fp32_lo(c1);
+    lo[2] = fp32_lo(c2);
+    lo[3] = fp32_lo(c3);
+  }
   if (scheme == MYQL_SCHEME_NV) {  // VolSchemes.hpp:42-48
     const double ex = std::exp(-k * dt * 0.5);
     const double psi = std::fabs(k) < 1e-10 ? dt * 0.5 : (1.0 - ex) / k;
@@ -228,13 +239,17 @@ void fill_factor(FactorConst &fc, const myql_heston_params &h, double v0, int sc
   } else {  // VolSchemes.hpp:121-125 (Exact), :326-330 (NCI)
     const double ex = std::exp(-k * dt);
     const double psi = std::fabs(k) < 1e-10 ? dt : (1.0 - ex) / k;
-    fc.w0 = (float)((2.0 / (s * s * psi)) * ex);
+    const double w0 = (2.0 / (s * s * psi)) * ex;
+    fc.w0 = (float)w0;
+    if (lo) lo[4] = fp32_lo(w0);
     if (scheme == MYQL_SCHEME_EXACT) {
       fc.w1 = (float)(2.0 * k * th / (s * s));
       fc.w2 = (float)(0.5 * s * s * psi);
     } else {
       fc.w1 = (float)(4.0 * k * th / (s * s));
-      fc.w2 = (float)(0.25 * s * s * psi);
+      const double w2 = 0.25 * s * s * psi;
+      fc.w2 = (float)w2;
+      if (lo) lo[5] = fp32_lo(w2);
     }
   }
 }
@@ -399,7 +414,7 @@ myql_status make_plan(const myql_mc_job &job, Plan &pl, bool stepped) {
     } else {
       const double r_part = (d.r - q) / (double)pl.nf;
       for (int f = 0; f < pl.nf; ++f)
-        fill_factor(C.f[f], m.heston[f], d.v0[f], c.scheme[f], r_part, d.dt);
+        fill_factor(C.f[f], m.heston[f], d.v0[f], c.scheme[f], r_part, d.dt, f == 0 ? C.lo : nullptr);
     }
     if (!pl.path_dep && (i == SC_RUP || i == SC_RDN)) C.x_shift = (float)((d.r - r) * d.T);
     // jump window: dt for path-dependent trackers, the whole (bumped) T otherwise
@@ -407,8 +422,10 @@ myql_status make_plan(const myql_mc_job &job, Plan &pl, bool stepped) {
     if (m.jump != MYQL_JUMP_NONE) {
       const double mean = m.jump_lambda * window;
       C.jump_mean = (float)mean;
+      C.jump_mean_d = mean;
       C.jump_exp_neg_mean = (float)std::exp(-mean);
       C.jump_comp = (float)(-m.jump_lambda * kjump * window);
+      C.lo[6] = fp32_lo(-m.jump_lambda * kjump * window);
     }
   }
   // The lockstep kernel merges a v0-bumped scenario's variance path into the
@@ -610,6 +627,10 @@ myql_status run_plan(CtxBase *ctx, const myql_mc_job &job, Plan &pl, double *out
   if (s != MYQL_OK) return s;
   P.states = (unsigned long long *)ctx->st_work.p;
   P.loop_cap = ctx->loop_cap;
+  // opt-in: the one-factor NCI lockstep's T-bumped scenarios with their constants' FP32
+  // rounding errors added back (myql_ctx_set_precise_theta)
+  P.lock_precise = ctx->precise_theta && P.lock_merge && pl.nf == 1 && !pl.path_dep &&
+                   pl.mode == MYQL_GREEKS_FULL && job.config.scheme[0] == MYQL_SCHEME_NCI;
   // NCI tables
   for (int f = 0; f < pl.nf; ++f) {
     if (job.config.scheme[f] != MYQL_SCHEME_NCI) continue;
@@ -792,6 +813,13 @@ myql_status myql_ctx_set_nci_slopes(myql_ctx *ctx, int mode) {
   if (!ctx) return set_error(MYQL_ERR_INVALID_ARG, "null context");
   if (mode != 0 && mode != 1) return set_error(MYQL_ERR_INVALID_ARG, "NCI slope mode is 0 or 1");
   ctx->nci_slopes = mode;
+  return MYQL_OK;
+}
+
+myql_status myql_ctx_set_precise_theta(myql_ctx *ctx, int on) {
+  if (!ctx) return set_error(MYQL_ERR_INVALID_ARG, "null context");
+  if (on != 0 && on != 1) return set_error(MYQL_ERR_INVALID_ARG, "precise theta is 0 or 1");
+  ctx->precise_theta = on;
   return MYQL_OK;
 }
 

@@ -47,6 +47,7 @@ struct CtxBase {
   uint32_t loop_cap = kDefaultLoopCap;
   int nci_slopes = 0;  // NCI table cells: 0 the reference's, 1 exact slopes and a mean-preserving first cell
   int nci_rows_cap = 0;  // at most this many NCI table rows (0: the sizing rule alone, at most 1024)
+  int precise_theta = 0;  // myql_ctx_set_precise_theta
   uint32_t launches = 0;
   uint64_t records_cap_bytes = 2ull << 30;  // per-path record scratch per chunk
   // xoshiro stream-state table of the last (seed, n)
@@ -118,7 +119,7 @@ myql_status validate_job(const myql_mc_job &job);
 // stepped: per-step GBM and jump constants even for Europeans (control variates)
 myql_status make_plan(const myql_mc_job &job, Plan &pl, bool stepped = false);
 void fill_factor(FactorConst &fc, const myql_heston_params &h, double v0, int scheme, double r_part,
-                 double dt);
+                 double dt, float *lo = nullptr);
 unsigned long long u999_threshold();
 double expected_avg_variance(const myql_heston_params &h, double T);
 double jump_variance(const myql_model &m);

@@ -72,6 +72,12 @@ struct ScenarioConst {
   float jump_comp;            // drift compensation of the window
   float x_shift;              // rho bumps of European instruments: log-spot shift (r' - r) T
                               // of a scenario derived from the base path, not simulated
+  // The FP32 rounding of each constant's own FP32 rounding error (exact - (double)(float)
+  // exact): factor 0's C0, C1, C2, C3, w0, w2, then jump_comp.  The precise lockstep kernel
+  // adds them for the T-bumped scenarios, whose constants differ from each other by about
+  // 2 t_bump / T relative: the difference then survives FP32 (myql_ctx_set_precise_theta).
+  float lo[7];
+  double jump_mean_d;         // jump_mean in FP64 (the precise kernel's T-bumped jump counts)
 };
 
 struct SimParams {
@@ -94,6 +100,7 @@ struct SimParams {
   NciTable nci[2];
   unsigned long long nci_u999;  // smallest 64-bit draw whose uniform is >= 0.999
   int lock_merge;               // lockstep kernel: v0-bumped variance paths merge into the base's
+  int lock_precise;             // one-factor NCI lockstep: T-bumped scenarios add ScenarioConst::lo
   // exact-scheme small-alpha constants (VolSchemes.hpp:95-103), per factor
   float sm_p[2], sm_inv_p[2], sm_1mp[2], sm_1ma[2], sm_inv_a[2];
   unsigned long long *states;  // [4][n_streams] xoshiro states, updated in place

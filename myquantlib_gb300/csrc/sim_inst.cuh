@@ -10,6 +10,12 @@ cudaError_t launch_sim_t(const SimParams &P, bool path_dep, cudaStream_t stream)
     // Full Greeks of a European: every simulated scenario in lockstep
     constexpr int n_sc_full = NF == 2 ? 9 : 7;
     if (!path_dep && P.n_sc == n_sc_full) {
+      if constexpr (NF == 1 && S1 == dev::SCH_NCI) {
+        if (P.lock_merge && P.lock_precise) {  // myql_ctx_set_precise_theta
+          dev::simulate_lockstep_kernel<NF, S1, S2, n_sc_full - 2, true, true><<<grid, kSimBlock, 0, stream>>>(P);
+          return cudaGetLastError();
+        }
+      }
       if constexpr (S1 == dev::SCH_NCI && (NF == 1 || S2 == dev::SCH_NCI)) {
         if (P.lock_merge) {
           dev::simulate_lockstep_kernel<NF, S1, S2, n_sc_full - 2, true><<<grid, kSimBlock, 0, stream>>>(P);

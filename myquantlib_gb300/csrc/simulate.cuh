@@ -107,10 +107,9 @@ __device__ __forceinline__ float evolve(float v, Xo &rng, const FactorConst &f,
   }
 }
 
-// Compound-Poisson log jump of one window (JumpPolicies.hpp:55-75, :111-135).
-__device__ __forceinline__ float jump_draw(const SimParams &P, const ScenarioConst &C, Xo &rng,
-                                           unsigned int &caphits) {
-  const int n = poisson_small(C.jump_mean, C.jump_exp_neg_mean, rng, P.loop_cap, caphits);
+// Compound-Poisson log jump of one window (JumpPolicies.hpp:55-75, :111-135),
+// for the jump count n of the window.
+__device__ __forceinline__ float jump_of_count(const SimParams &P, const ScenarioConst &C, int n, Xo &rng) {
   if (n == 0) return C.jump_comp;
   if (P.jump_kind == 1) {
     const float Z = inv_normal_bits(draw(rng));
@@ -127,6 +126,11 @@ __device__ __forceinline__ float jump_draw(const SimParams &P, const ScenarioCon
       total -= exp_draw(rng, P.kou_inv_eta2);
   }
   return C.jump_comp + total;
+}
+
+__device__ __forceinline__ float jump_draw(const SimParams &P, const ScenarioConst &C, Xo &rng,
+                                           unsigned int &caphits) {
+  return jump_of_count(P, C, poisson_small(C.jump_mean, C.jump_exp_neg_mean, rng, P.loop_cap, caphits), rng);
 }
 
 // Tracker state of one path (PathTrackers.hpp:8-301): the running sum of an
@@ -395,11 +399,12 @@ __device__ __forceinline__ void factor_draws(FactorDraws<SCH> &d, Xo &rng, const
 // gathers (independent loads in flight together), then the cubic cells.
 // SUB: the NS = 3 scenarios of lockstep_sub; a table fallback of the base then
 // stands for the base and its `merged` copies.
-template <int SCH, int NS, bool SUB = false>
+template <int SCH, int NS, bool SUB = false, bool PRECISE = false>
 __device__ __forceinline__ void evolve_lockstep(const float (&v)[NS], float (&vn)[NS],
                                                 const FactorDraws<SCH> &d, const SimParams &P,
                                                 int fi, unsigned int &caphits,
                                                 unsigned int &fallbacks, unsigned int merged = 0) {
+  static_assert(!PRECISE || (SUB && NS == 3), "the T-bumped pair of the merged subset");
   auto sc = [](int j) { return SUB ? lockstep_sub(j) : lockstep_sc(j); };
   if (SCH == SCH_NV) {
 #pragma unroll
@@ -414,7 +419,9 @@ __device__ __forceinline__ void evolve_lockstep(const float (&v)[NS], float (&vn
     constexpr bool PAIR = NS == 3;  // scenarios 1 and 2 (T up, T down) on packed pairs
     if constexpr (PAIR) {
       lam[0] = P.sc[sc(0)].f[fi].w0 * v[0];
-      const float2 l = pk::fmul2(make_float2(P.sc[sc(1)].f[fi].w0, P.sc[sc(2)].f[fi].w0), make_float2(v[1], v[2]));
+      float2 l = pk::fmul2(make_float2(P.sc[sc(1)].f[fi].w0, P.sc[sc(2)].f[fi].w0), make_float2(v[1], v[2]));
+      if constexpr (PRECISE)  // + (w0 - fl(w0)) v
+        l = pk::ffma2(make_float2(P.sc[sc(1)].lo[4], P.sc[sc(2)].lo[4]), make_float2(v[1], v[2]), l);
       lam[1] = l.x;
       lam[2] = l.y;
     } else {
@@ -448,7 +455,9 @@ __device__ __forceinline__ void evolve_lockstep(const float (&v)[NS], float (&vn
     }
     if constexpr (PAIR) {
       vn[0] = q[0] * P.sc[sc(0)].f[fi].w2;
-      const float2 w = pk::fmul2(make_float2(q[1], q[2]), make_float2(P.sc[sc(1)].f[fi].w2, P.sc[sc(2)].f[fi].w2));
+      float2 w = pk::fmul2(make_float2(q[1], q[2]), make_float2(P.sc[sc(1)].f[fi].w2, P.sc[sc(2)].f[fi].w2));
+      if constexpr (PRECISE)  // + q (w2 - fl(w2))
+        w = pk::ffma2(make_float2(q[1], q[2]), make_float2(P.sc[sc(1)].lo[5], P.sc[sc(2)].lo[5]), w);
       vn[1] = w.x;
       vn[2] = w.y;
     } else {
@@ -483,7 +492,7 @@ __device__ __forceinline__ NciOne nci_step_one(float lam, float scale, const Nci
 }
 
 // evolve_lockstep of one NCI factor with merged variance paths (see lockstep_sub).
-template <int NS>
+template <int NS, bool PRECISE = false>
 __device__ __forceinline__ void evolve_merged(const float (&v)[NS], float (&vn)[NS],
                                               const FactorDraws<SCH_NCI> &d, const SimParams &P,
                                               int fi, unsigned int &caphits,
@@ -497,7 +506,7 @@ __device__ __forceinline__ void evolve_merged(const float (&v)[NS], float (&vn)[
   }
   const float v3[3] = {v[0], v[3], v[4]};
   float o3[3];
-  evolve_lockstep<SCH_NCI, 3, true>(v3, o3, d, P, fi, caphits, fallbacks, nm);
+  evolve_lockstep<SCH_NCI, 3, true, PRECISE>(v3, o3, d, P, fi, caphits, fallbacks, nm);
 #pragma unroll
   for (int j = 0; j < NS; ++j) {
     if (j == 3 || j == 4) {
@@ -517,7 +526,7 @@ __device__ __forceinline__ void evolve_merged(const float (&v)[NS], float (&vn)[
 // One time step of every simulated scenario of one path: the loop body of the lockstep
 // kernels.  MERGE: the v0-bumped scenarios' variance paths merge into the base's (every
 // factor on NCI, and P.lock_merge: the host found their NCI constants equal).
-template <int NF, int S1, int S2, int NSIM, bool MERGE>
+template <int NF, int S1, int S2, int NSIM, bool MERGE, bool PRECISE = false>
 __device__ __forceinline__ void lockstep_step(const SimParams &P, Xo &rng, float (&X)[NSIM], float (&va)[NSIM],
                                               float (&vb)[NSIM], unsigned int &caphits,
                                               unsigned int &fallbacks) {
@@ -527,8 +536,9 @@ __device__ __forceinline__ void lockstep_step(const SimParams &P, Xo &rng, float
   factor_draws<S1>(da, rng, P, 0);
   if (NF == 2) factor_draws<S2>(db, rng, P, 1);
   float van[NSIM], vbn[NSIM];
+  static_assert(!PRECISE || (MERGE && NF == 1), "the merged one-factor kernel");
   if constexpr (MERGE) {
-    evolve_merged<NSIM>(va, van, da, P, 0, caphits, fallbacks);
+    evolve_merged<NSIM, PRECISE>(va, van, da, P, 0, caphits, fallbacks);
     if constexpr (NF == 2) evolve_merged<NSIM>(vb, vbn, db, P, 1, caphits, fallbacks);
   } else {
     evolve_lockstep<S1, NSIM>(va, van, da, P, 0, caphits, fallbacks);
@@ -549,10 +559,19 @@ __device__ __forceinline__ void lockstep_step(const SimParams &P, Xo &rng, float
     for (int j = 1; j + 1 < NSIM; j += 2) {
       const FactorConst &f = P.sc[lockstep_sc(j)].f[0], &g = P.sc[lockstep_sc(j + 1)].f[0];
       const float2 v0 = make_float2(va[j], va[j + 1]), v1 = make_float2(van[j], van[j + 1]);
-      const float2 c3 = pk::fmul2(make_float2(f.C3, g.C3), pk::fadd2(v0, v1));
+      const float2 sv = pk::fadd2(v0, v1);
+      float2 c3 = pk::fmul2(make_float2(f.C3, g.C3), sv);
+      float2 drift = pk::ffma2(make_float2(f.C2, g.C2), v1,
+                                pk::ffma2(make_float2(f.C1, g.C1), v0, make_float2(f.C0, g.C0)));
+      if constexpr (PRECISE) {
+        if (lockstep_sc(j) == SC_TUP) {  // the T-bumped pair: + the constants' FP32 rounding errors
+          const float *lf = P.sc[SC_TUP].lo, *lg = P.sc[SC_TDN].lo;
+          c3 = pk::ffma2(make_float2(lf[3], lg[3]), sv, c3);
+          drift = pk::fadd2(drift, pk::ffma2(make_float2(lf[2], lg[2]), v1,
+                                             pk::ffma2(make_float2(lf[1], lg[1]), v0, make_float2(lf[0], lg[0]))));
+        }
+      }
       const float2 root = make_float2(sqrt_approx(c3.x), sqrt_approx(c3.y));
-      const float2 drift = pk::ffma2(make_float2(f.C2, g.C2), v1,
-                                      pk::ffma2(make_float2(f.C1, g.C1), v0, make_float2(f.C0, g.C0)));
       const float2 x = pk::fadd2(make_float2(X[j], X[j + 1]), pk::ffma2(root, make_float2(G, G), drift));
       X[j] = x.x;
       X[j + 1] = x.y;
@@ -589,7 +608,7 @@ __device__ __forceinline__ void lockstep_start(const SimParams &P, float (&X)[NS
 // Path end: one jump over each scenario's (bumped) maturity, drawn from the state after
 // the last step (the base scenario's draws advance the stream), then the records,
 // the two rho scenarios derived from the base.
-template <int NSIM>
+template <int NSIM, bool PRECISE = false>
 __device__ __forceinline__ void lockstep_finish(const SimParams &P, Xo &rng, float (&X)[NSIM], size_t col,
                                                 unsigned int &caphits) {
   if (P.jump_kind) {
@@ -597,7 +616,15 @@ __device__ __forceinline__ void lockstep_finish(const SimParams &P, Xo &rng, flo
 #pragma unroll
     for (int j = 0; j < NSIM; ++j) {
       Xo r = after;
-      X[j] += jump_draw(P, P.sc[lockstep_sc(j)], r, caphits);
+      if (PRECISE && (lockstep_sc(j) == SC_TUP || lockstep_sc(j) == SC_TDN)) {
+        // the T-bumped windows' means differ by 2 t_bump lambda: their count in FP64, and
+        // the compensation's FP32 rounding error added back
+        const ScenarioConst &C = P.sc[lockstep_sc(j)];
+        const int2 nj = poisson_small_fp64(C.jump_mean_d, draw(r), P.loop_cap);
+        caphits += (unsigned int)nj.y;
+        X[j] += jump_of_count(P, C, nj.x, r) + C.lo[6];
+      } else
+        X[j] += jump_draw(P, P.sc[lockstep_sc(j)], r, caphits);
       if (j == 0) rng = r;
     }
   }
@@ -609,7 +636,7 @@ __device__ __forceinline__ void lockstep_finish(const SimParams &P, Xo &rng, flo
   P.records[(size_t)SC_RDN * F * P.rec_stride + col] = X[0] + P.sc[SC_RDN].x_shift;
 }
 
-template <int NF, int S1, int S2, int NSIM, bool MERGE = false>
+template <int NF, int S1, int S2, int NSIM, bool MERGE = false, bool PRECISE = false>
 __global__ void __launch_bounds__(kSimBlock) simulate_lockstep_kernel(
     const __grid_constant__ SimParams P) {
   static_assert(NF >= 1 && S1 != SCH_EXACT && S2 != SCH_EXACT, "lockstep needs NV/NCI factors");
@@ -627,8 +654,8 @@ __global__ void __launch_bounds__(kSimBlock) simulate_lockstep_kernel(
   for (unsigned long long i = P.path_begin + s; i < P.path_end; i += S) {
     float X[NSIM], va[NSIM], vb[NSIM];
     lockstep_start<NSIM>(P, X, va, vb);
-    for (int k = 0; k < n; ++k) lockstep_step<NF, S1, S2, NSIM, MERGE>(P, rng, X, va, vb, caphits, fallbacks);
-    lockstep_finish<NSIM>(P, rng, X, (size_t)(i - P.rec_offset), caphits);
+    for (int k = 0; k < n; ++k) lockstep_step<NF, S1, S2, NSIM, MERGE, PRECISE>(P, rng, X, va, vb, caphits, fallbacks);
+    lockstep_finish<NSIM, PRECISE>(P, rng, X, (size_t)(i - P.rec_offset), caphits);
   }
   P.states[s] = rng.a;
   P.states[(size_t)S + s] = rng.b;

@@ -445,6 +445,13 @@ class Engine:
         the rows take the Wilson-Hilferty quantile and are counted in table_fallbacks."""
         _abi.check(self.lib.myql_ctx_set_nci_rows(self.handle, int(max_rows)))
 
+    def set_precise_theta(self, on: bool):
+        """Theta and charm of one-factor SchemeNCI Europeans with the T-bumped scenarios'
+        constants carried to beyond FP32 (their FP32 rounding errors added back), so the
+        difference over 2 t_bump keeps its precision; off (the default) keeps every
+        scenario's records equal to a single-maturity request's."""
+        _abi.check(self.lib.myql_ctx_set_precise_theta(self.handle, 1 if on else 0))
+
     def price(self, job: "_Job") -> tuple[np.ndarray, _abi.McStatsC]:
         out = np.zeros(2 * _abi.Q_COUNT * job.n_strikes, dtype=np.float64)
         st = _abi.McStatsC()

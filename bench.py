@@ -410,12 +410,13 @@ def fourier_summary(m, z: np.ndarray) -> dict:
             "frac_abs_z_above_2": float(np.mean(a > 2.0))}
 
 
-def fourier_seeds(eng, m, seeds, nci_slopes: int) -> dict:
+def fourier_seeds(eng, m, seeds, nci_slopes: int, precise_theta: bool = False) -> dict:
     """The strip on several seeds against the Fourier oracle.  Per (maturity, quantity) the
     strike-averaged signed z is averaged over the seeds; with independent seeds its spread
     gives a standard error, so a residual bias shows as a mean that stays away from 0 by
     several of those standard errors (one seed cannot tell correlation from bias)."""
     eng.set_nci_slopes(nci_slopes)
+    eng.set_precise_theta(precise_theta)
     try:
         zs = []
         for sd in seeds:
@@ -425,6 +426,7 @@ def fourier_seeds(eng, m, seeds, nci_slopes: int) -> dict:
             zs.append(fourier_z(eng, m, js))
     finally:
         eng.set_nci_slopes(0)
+        eng.set_precise_theta(False)
     Z = np.stack(zs)                                     # (seed, maturity, quantity, strike)
     # quantities without a Fourier value (the second factor's) are all NaN: left out
     has = np.isfinite(Z).any(axis=3)                     # (seed, maturity, quantity)
@@ -446,7 +448,7 @@ def fourier_seeds(eng, m, seeds, nci_slopes: int) -> dict:
     a = np.abs(Z[np.isfinite(Z)])
     worst = max(cells.items(), key=lambda kv: abs(kv[1]["t"]))
     return {"seeds": list(seeds), "nci_cells": "exact slopes, mean-preserving first cell" if nci_slopes
-            else "the reference's", "comparisons": int(a.size),
+            else "the reference's", "precise_theta": precise_theta, "comparisons": int(a.size),
             "pooled_frac_abs_z_above_3": float(np.mean(a > 3.0)),
             "pooled_frac_abs_z_above_2": float(np.mean(a > 2.0)),
             "max_abs_mean_z": float(np.nanmax(np.abs(mean))), "max_abs_t": float(np.nanmax(np.abs(t))),
@@ -492,6 +494,8 @@ def strip_reports(eng, m, jobs, local: int, args) -> dict:
         seeds = tuple(range(SEED, SEED + args.fourier_seeds))
         out["fourier_seeds_exact_nci"] = fourier_seeds(eng, m, seeds, 1)
         out["fourier_seeds"] = fourier_seeds(eng, m, seeds, 0)
+        # theta and charm with the T-bumped constants carried beyond FP32 (opt-in mode)
+        out["fourier_seeds_exact_nci_precise_theta"] = fourier_seeds(eng, m, seeds, 1, precise_theta=True)
     except Exception as exc:  # the oracle is a report, not the measurement
         out["fourier_check"] = {"error": repr(exc)}
     out["e2e_cold"] = cold_e2e(m, local)

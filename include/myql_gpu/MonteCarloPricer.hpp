@@ -443,6 +443,11 @@ inline bool &thread_exact_nci() {
   thread_local bool on = false;
   return on;
 }
+// The precise-theta mode of this thread's pricers, kept the same way.
+inline bool &thread_precise_theta() {
+  thread_local bool on = false;
+  return on;
+}
 struct ThreadCtx {
   myql_ctx *ctx = nullptr;
   int device = -1;
@@ -468,6 +473,10 @@ inline myql_ctx *context() {
     tc.device = dev;
     if (thread_exact_nci()) {
       s = myql_ctx_set_nci_slopes(tc.ctx, 1);
+      if (s != MYQL_OK) raise(s);
+    }
+    if (thread_precise_theta()) {
+      s = myql_ctx_set_precise_theta(tc.ctx, 1);
       if (s != MYQL_OK) raise(s);
     }
   }
@@ -573,6 +582,16 @@ inline void set_device(int device) { detail::thread_device() = device; }
 inline void set_exact_nci_tables(bool on) {
   detail::thread_exact_nci() = on;
   const myql_status s = myql_ctx_set_nci_slopes(detail::context(), on ? 1 : 0);
+  if (s != MYQL_OK) detail::raise(s);
+}
+
+// Theta and charm of this thread's one-factor SchemeNCI Full-Greek European pricers:
+// false (default) every scenario in plain FP32 constants, true the T-bumped scenarios
+// with their constants' FP32 rounding errors added back (see myql_ctx_set_precise_theta).
+// The choice holds for the calling thread, across set_device().
+inline void set_precise_theta(bool on) {
+  detail::thread_precise_theta() = on;
+  const myql_status s = myql_ctx_set_precise_theta(detail::context(), on ? 1 : 0);
   if (s != MYQL_OK) detail::raise(s);
 }
 

@@ -84,6 +84,21 @@ int main(int argc, char **argv) {
   const auto ml = mlmc.calculate(100.0, 0.02, 0.0, DownAndOutPut<>(100.0, 80.0, 1.0));
   std::printf("{\"mlmc_price\": %.17g, \"mlmc_se\": %.17g, \"mlmc_levels\": %zu, \"mlmc_delta\": %.17g}\n",
               ml.price, ml.price_std_err, ml.paths_per_level.size(), ml.delta);
+  // precise theta (one-factor SchemeNCI, Full Greeks): the same price, a theta of its own
+  {
+    const HestonParams hn{2.0, 0.05, 0.9, -0.6, 0.05};
+    BatesModel bn(hn, MertonParams{0.5, -0.1, 0.15});
+    MonteCarloConfig fc;
+    fc.num_paths = 1u << 16;
+    fc.time_steps = 200;
+    MonteCarloPricer<BatesModel, BatesStepper<SchemeNCI>, Eur, GreekMode::Full> pf(bn, fc);
+    const auto a = pf.calculate(100.0, 0.02, 0.0, Eur(100.0, 1.0));
+    set_precise_theta(true);
+    const auto b = pf.calculate(100.0, 0.02, 0.0, Eur(100.0, 1.0));
+    set_precise_theta(false);
+    std::printf("{\"full_price\": [%.17g, %.17g], \"full_theta\": [%.17g, %.17g], \"theta_se\": %.17g}\n",
+                a.price, b.price, a.theta, b.theta, a.theta_std_err);
+  }
   // an invalid request surfaces as the reference's exception type
   try {
     HestonModel bad(HestonParams{1.5, 0.04, 0.9, -0.7, 0.04});

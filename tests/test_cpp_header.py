@@ -114,4 +114,8 @@ def test_header_prices_on_the_gpu(tmp_path):
     assert 0.4 < res["delta"] < 0.8
     assert lines[1]["mlmc_levels"] >= 3 and lines[1]["mlmc_delta"] == 0.0
     assert 1.0 < lines[1]["mlmc_price"] < 4.0 and lines[1]["mlmc_se"] > 0
-    assert lines[2]["nv_error"] == "runtime_error"
+    fl = lines[2]
+    assert fl["full_price"][0] == fl["full_price"][1]          # the base scenario is unchanged
+    assert fl["full_theta"][0] != fl["full_theta"][1]          # the T-bumped scenarios are not
+    assert abs(fl["full_theta"][0] - fl["full_theta"][1]) < fl["theta_se"]
+    assert lines[3]["nv_error"] == "runtime_error"

@@ -507,19 +507,27 @@ __device__ __forceinline__ void evolve_merged(const float (&v)[NS], float (&vn)[
   const float v3[3] = {v[0], v[3], v[4]};
   float o3[3];
   evolve_lockstep<SCH_NCI, 3, true, PRECISE>(v3, o3, d, P, fi, caphits, fallbacks, nm);
+  unsigned int todo = 0;  // the v0-bumped scenarios that have not merged yet
 #pragma unroll
   for (int j = 0; j < NS; ++j) {
-    if (j == 3 || j == 4) {
-      vn[j] = o3[j - 2];
-    } else if (j == 0 || same[j]) {
-      vn[j] = o3[0];
-    } else {
-      const FactorConst &f = P.sc[lockstep_sc(j)].f[fi];
-      const NciOne o = nci_step_one(f.w0 * v[j], f.w2, P.nci[fi], d.xp, d.U, d.x2, d.pos, P.loop_cap);
-      vn[j] = o.v;
-      caphits += o.caphits;
-      fallbacks += o.fallbacks;
-    }
+    vn[j] = (j == 3 || j == 4) ? o3[j - 2] : o3[0];
+    todo |= lockstep_merges(j) && !same[j] ? 1u << j : 0u;
+  }
+  // One copy of their inversion, run once per pending scenario: lanes waiting on different
+  // scenarios run it together, and the step's code holds one copy instead of one per scenario.
+#pragma unroll 1
+  while (todo) {
+    const int j = __ffs(todo) - 1;
+    todo &= todo - 1;
+    float vj = v[1];
+#pragma unroll
+    for (int k = 2; k < NS; ++k) vj = k == j ? v[k] : vj;
+    const FactorConst &f = P.sc[lockstep_sc(j)].f[fi];
+    const NciOne o = nci_step_one(f.w0 * vj, f.w2, P.nci[fi], d.xp, d.U, d.x2, d.pos, P.loop_cap);
+#pragma unroll
+    for (int k = 1; k < NS; ++k) vn[k] = k == j ? o.v : vn[k];
+    caphits += o.caphits;
+    fallbacks += o.fallbacks;
   }
 }
 

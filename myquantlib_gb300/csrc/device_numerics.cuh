@@ -395,12 +395,12 @@ __device__ __forceinline__ int poisson_eval(float lam, float U, float W, unsigne
 }
 
 // poisson_eval for NS means on one draw (the bumped scenarios of one path):
-// each N[j] equals poisson_eval(lam[j], U, W, x), where W = inv_normal_bits(x)
-// is computed only if some mean needs it.  The central estimates run as
+// each N[j] equals poisson_eval(lam[j], U, W, x), W = inv_normal_bits(x) from
+// the caller (read only where some mean is above kPoissonAsymMin).  The central estimates run as
 // straight-line code and the summations share one loop, so the scenarios'
 // arithmetic interleaves and the loop overhead is paid once.
 template <int NS>
-__device__ __forceinline__ void poisson_eval_n(const float (&lam)[NS], float U,
+__device__ __forceinline__ void poisson_eval_n(const float (&lam)[NS], float U, float W,
                                                unsigned long long x, unsigned int cap,
                                                unsigned int &caphits, int (&N)[NS]) {
   float X[NS], lim[NS];
@@ -414,7 +414,6 @@ __device__ __forceinline__ void poisson_eval_n(const float (&lam)[NS], float U,
     big |= lam[j] > kPoissonAsymMin;
   }
   if (big) {
-    const float W = inv_normal_bits(x);
     const bool central = fabsf(W) < 3.0f;
     float S[NS], Del[NS];
     if (central) {

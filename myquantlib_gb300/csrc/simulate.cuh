@@ -378,6 +378,7 @@ struct FactorDraws {
   float Z = 0.0f;                     // NV: Gaussian of the variance step
   unsigned long long xp = 0, x2 = 0;  // NCI: Poisson and chi-squared draws
   float U = 0.0f;                     // NCI: uniform of xp
+  float W = 0.0f;                     // NCI: normal quantile of xp (Giles' estimate)
   NciPos pos{};                       // NCI: table cell of x2
 };
 
@@ -389,6 +390,7 @@ __device__ __forceinline__ void factor_draws(FactorDraws<SCH> &d, Xo &rng, const
   } else if (SCH == SCH_NCI) {
     d.xp = draw(rng);
     d.U = u01_bits(d.xp);
+    d.W = inv_normal_bits(d.xp);  // once per step for every scenario's inversion
     d.x2 = draw(rng);
     d.pos = nci_pos(P.nci[fi], d.x2, P.nci_u999);
   }
@@ -428,7 +430,7 @@ __device__ __forceinline__ void evolve_lockstep(const float (&v)[NS], float (&vn
 #pragma unroll
       for (int j = 0; j < NS; ++j) lam[j] = P.sc[sc(j)].f[fi].w0 * v[j];
     }
-    poisson_eval_n<NS>(lam, d.U, d.xp, P.loop_cap, caphits, N);
+    poisson_eval_n<NS>(lam, d.U, d.W, d.xp, P.loop_cap, caphits, N);
     const NciTable &tab = P.nci[fi];
     float4 c[NS];
 #pragma unroll
@@ -476,11 +478,10 @@ struct NciOne {
   unsigned int caphits, fallbacks;
 };
 __device__ __forceinline__ NciOne nci_step_one(float lam, float scale, const NciTable &tab,
-                                               unsigned long long xp, float U,
+                                               unsigned long long xp, float U, float W,
                                                unsigned long long x2, NciPos pos,
                                                unsigned int cap) {
   NciOne o{0.0f, 0u, 0u};
-  const float W = lam > kPoissonAsymMin ? inv_normal_bits(xp) : 0.0f;
   const int N = poisson_eval(lam, U, W, xp, cap, o.caphits);
   float q = nci_cubic(nci_cell(tab, N, pos), pos.t);
   if (N >= tab.rows) {
@@ -523,7 +524,7 @@ __device__ __forceinline__ void evolve_merged(const float (&v)[NS], float (&vn)[
 #pragma unroll
     for (int k = 2; k < NS; ++k) vj = k == j ? v[k] : vj;
     const FactorConst &f = P.sc[lockstep_sc(j)].f[fi];
-    const NciOne o = nci_step_one(f.w0 * vj, f.w2, P.nci[fi], d.xp, d.U, d.x2, d.pos, P.loop_cap);
+    const NciOne o = nci_step_one(f.w0 * vj, f.w2, P.nci[fi], d.xp, d.U, d.W, d.x2, d.pos, P.loop_cap);
 #pragma unroll
     for (int k = 1; k < NS; ++k) vn[k] = k == j ? o.v : vn[k];
     caphits += o.caphits;

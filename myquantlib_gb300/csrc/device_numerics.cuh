@@ -61,11 +61,24 @@ __device__ __forceinline__ unsigned long long xo_next(Xo &s) {
 }
 
 // One uniform_real_distribution<double>(0,1) draw: the double of x / 2^64 is
-// rejected when it rounds to 1.0, i.e. for x >= 2^64 - 2^10.
-__device__ __forceinline__ unsigned long long draw(Xo &s) {
+// rejected when it rounds to 1.0, i.e. for x >= 2^64 - 2^10 (2^-54 of draws).
+// The redraws run out of line, so the path kernels' loops hold no cold copy of
+// the generator.
+struct XoDraw {
+  Xo s;
+  unsigned long long x;
+};
+static __device__ __noinline__ XoDraw draw_again(Xo s) {
   unsigned long long x = xo_next(s);
   while (x >= 0xFFFFFFFFFFFFFC00ull) x = xo_next(s);
-  return x;
+  return XoDraw{s, x};
+}
+__device__ __forceinline__ unsigned long long draw(Xo &s) {
+  const unsigned long long x = xo_next(s);
+  if (x < 0xFFFFFFFFFFFFFC00ull) return x;
+  const XoDraw r = draw_again(s);
+  s = r.s;
+  return r.x;
 }
 
 // x * 2^-64 rounded down to 24 significant bits (relative precision at any scale).

@@ -387,6 +387,14 @@ __device__ __forceinline__ float poisson_sum(float lam, float U, float lim, unsi
   }
 }
 
+// poisson_sum out of line, for the deep upper tail (U >= kPoissonUFast, one
+// draw in 1e5) of the multi-mean inversion: (X, loop-cap hits).
+static __device__ __noinline__ float2 poisson_sum_tail(float lam, float U, float lim, unsigned int cap) {
+  unsigned int hits = 0;
+  const float X = poisson_sum(lam, U, lim, cap, hits);
+  return make_float2(X, (float)hits);
+}
+
 __device__ __forceinline__ int poisson_eval(float lam, float U, float W, unsigned long long x,
                                             unsigned int cap, unsigned int &caphits) {
   float X = 0.0f, lim = kPoissonSumAll;
@@ -452,10 +460,15 @@ __device__ __forceinline__ void poisson_eval_n(const float (&lam)[NS], float U, 
 #pragma unroll
   for (int j = 0; j < NS; ++j) any |= act[j];
   if (any && !(U < kPoissonUFast)) {
-    // deep upper tail (one draw in 1e5): the scalar summation with its tail exit
+    // deep upper tail (one draw in 1e5): the scalar summation with its tail exit, out of line
 #pragma unroll
-    for (int j = 0; j < NS; ++j)
-      if (act[j]) X[j] = poisson_sum(lam[j], U, lim[j], cap, caphits);
+    for (int j = 0; j < NS; ++j) {
+      if (act[j]) {
+        const float2 r = poisson_sum_tail(lam[j], U, lim[j], cap);
+        X[j] = r.x;
+        caphits += (unsigned int)r.y;
+      }
+    }
     any = false;
   }
   if (any) {

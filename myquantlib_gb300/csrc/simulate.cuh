@@ -59,13 +59,17 @@ __device__ __forceinline__ float nci_cubic(const float4 &c, float t) {
   return fmaf(fmaf(fmaf(c.w, t, c.z), t, c.y), t, c.x);
 }
 
-// Wilson-Hilferty cube for rows beyond the table (dof >= d + 2*rows).
-__device__ __forceinline__ float nci_beyond(const NciTable &tab, int N, unsigned long long x2) {
-  const float nu = tab.d + 2.0f * (float)N;
+// Wilson-Hilferty cube for rows beyond the table (dof >= d + 2*rows).  Out of line: a
+// count past the rows is rare, and inline its inverse normal would sit in every step.
+static __device__ __noinline__ float nci_beyond_d(float d, int N, unsigned long long x2) {
+  const float nu = d + 2.0f * (float)N;
   const float z = inv_normal_bits(x2);
   const float h = 2.0f / (9.0f * nu);
   const float b = 1.0f - h + z * sqrtf(h);
   return fmaxf(nu * b * b * b, 0.0f);
+}
+__device__ __forceinline__ float nci_beyond(const NciTable &tab, int N, unsigned long long x2) {
+  return nci_beyond_d(tab.d, N, x2);
 }
 
 // Chi-squared quantile of row N (d + 2N degrees of freedom) at the cell p of x2.

@@ -59,17 +59,22 @@ __device__ __forceinline__ float nci_cubic(const float4 &c, float t) {
   return fmaf(fmaf(fmaf(c.w, t, c.z), t, c.y), t, c.x);
 }
 
-// Wilson-Hilferty cube for rows beyond the table (dof >= d + 2*rows).  Out of line: a
-// count past the rows is rare, and inline its inverse normal would sit in every step.
-static __device__ __noinline__ float nci_beyond_d(float d, int N, unsigned long long x2) {
+// Wilson-Hilferty cube for rows beyond the table (dof >= d + 2*rows).
+__device__ __forceinline__ float nci_beyond_wh(float d, int N, unsigned long long x2) {
   const float nu = d + 2.0f * (float)N;
   const float z = inv_normal_bits(x2);
   const float h = 2.0f / (9.0f * nu);
   const float b = 1.0f - h + z * sqrtf(h);
   return fmaxf(nu * b * b * b, 0.0f);
 }
+// The same, out of line, for the lockstep kernels: with the headline tables a count past
+// the rows is rare, and inline its inverse normal would sit in every step.  (The batched
+// kernels' capped tables send many counts past the rows; they keep it inline.)
+static __device__ __noinline__ float nci_beyond_cold(float d, int N, unsigned long long x2) {
+  return nci_beyond_wh(d, N, x2);
+}
 __device__ __forceinline__ float nci_beyond(const NciTable &tab, int N, unsigned long long x2) {
-  return nci_beyond_d(tab.d, N, x2);
+  return nci_beyond_cold(tab.d, N, x2);
 }
 
 // Chi-squared quantile of row N (d + 2N degrees of freedom) at the cell p of x2.
@@ -77,7 +82,7 @@ __device__ __forceinline__ float nci_row(const NciTable &tab, int N, const NciPo
                                          unsigned long long x2, unsigned int &fallbacks) {
   if (N < tab.rows) return nci_cubic(nci_cell(tab, N, p), p.t);
   ++fallbacks;
-  return nci_beyond(tab, N, x2);
+  return nci_beyond_wh(tab.d, N, x2);
 }
 
 __device__ __forceinline__ float nci_quantile(const NciTable &tab, int N,
